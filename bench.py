@@ -1,0 +1,386 @@
+"""Benchmark: particle-steps/s of the Langevin step on one GB300.
+
+Workload (the single large system): N = 2^20 particles at number density
+0.8 in a cubic periodic box (an FCC lattice of 64^3 cells, a = (4/0.8)^(1/3),
+L = 109.438), LennardJones plugin with ljNum 6, yukawaStrength 0 and
+kT * wellDepth = epsilon = 1 at kT = 1.5, cutOff 2.5, Maxwell-Boltzmann
+velocities at kT = 1.5, gamma = 1, dt = 0.002, cell grid 43^3.  One step =
+forces -> push -> nextSystem -> cell-list rebuild (system.cpp:187-206).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Prints one JSON line.  `value` times the mixed-precision form (FP32 pairs,
+Kahan sums, FP64 update) with state resident in HBM; `plain_fp64` times the
+FP64 plain form on the same melted state; `force_rel_err` is the mixed form's
+force error against FP64 on that state; `e2e` runs the reference-layout
+drop-ins (cells_build -> force_evaluate -> nextSystem) on host buffers in
+pinned memory, every copy inside the timed region.  `--impl reference` times
+the CPU implementation of the path (oracle/_ref when present, else the
+oracle's restatement) on the host cores.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s, 1 GB300: FP32-mixed vs FP64 plain at <=1e-5 rel force err"
+UNIT = "particle-steps/s"
+KT, WD, RC, LJN, DT, GAMMA = 1.5, 1.0 / 1.5, 2.5, 6, 0.002, 1.0
+FLOPS_PER_PAIR_LJ = 30   # algorithmic FLOPs per in-range ordered pair (FMA = 2)
+FLOPS_VGB = 60           # algorithmic FP64 FLOPs per particle of the vGB update
+
+
+def workload(cells=64):
+    from proteinsim2015_gb300 import init
+    a = (4.0 / 0.8) ** (1.0 / 3.0)
+    box = cells * a
+    pos = init.fcc(cells, a).reshape(-1)
+    n = pos.size // 3
+    scale = int(math.floor(box / RC))
+    vel = init.maxwell(n, KT, seed=90210).reshape(-1)
+    return dict(n=n, box=box, scale=scale, cell_size=box / scale, pos=pos, vel=vel,
+                radius=np.full(n, 0.5), cells=cells)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh)
+    except (OSError, ValueError):
+        return {}
+
+
+def cpu_steps(w, threads):
+    """A stepping closure over the oracle restatement on the host cores:
+    run(k) advances the workload k whole steps (noise reused cyclically,
+    which does not change the work)."""
+    from oracle import port
+    port.set_threads(threads)
+    g = port.geom(w["n"], w["box"], w["cell_size"], w["scale"])
+    f = port.make_force(port.LJ, RC, kT=KT, well_depth=WD, lj_num=LJN, yuk_str=0.0)
+    c = port.vgb_coeffs(GAMMA, DT, KT)
+    st = port.State(w["pos"], w["radius"], vel=w["vel"])
+    noise = np.random.default_rng(1).standard_normal(w["n"] * 6)
+    cells = [None]
+
+    def run(k):
+        err, hi, cse, srt, _ = port.run(g, f, c, DT, st, k, noise, vel_freq=1000,
+                                        cells=cells[0])
+        cells[0] = (hi, cse, srt)
+        if err:
+            raise RuntimeError("oracle step failed with %d" % err)
+    return run
+
+
+def cpu_port_rate(w, budget_s, threads):
+    """particle-steps/s of the oracle restatement on the same workload, over
+    whole steps until about budget_s elapse (after one warm-up step)."""
+    run = cpu_steps(w, threads)
+    run(1)
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        run(1)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= budget_s or steps >= 1000:
+            break
+    return w["n"] * steps / el, steps, el
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    w = workload()
+    # The reference cannot travel to the GPU machine (its tree is absent
+    # there); its CPU path is the oracle restatement, pinned bit-exact to the
+    # reference's own code by tests/test_oracle_golden.py.
+    kind = "port"
+    run = cpu_steps(w, threads)
+    nw = max(1, min(args.warmup, 3))
+    t_w = time.perf_counter()
+    run(nw)
+    per = (time.perf_counter() - t_w) / nw
+    # one step of this arm is one whole step of the workload on the CPU; the
+    # number of timed steps is bounded so the run ends within a few minutes
+    k = max(1, min(args.steps, int(60.0 / max(per, 1e-3))))
+    t0 = time.perf_counter()
+    run(k)
+    el = time.perf_counter() - t0
+    v = w["n"] * k / el
+    sample = ("N=%d LJ rho=0.8 from the FCC start, %d whole steps of %d requested "
+              "(oracle restatement of the reference, %d threads)" % (w["n"], k, args.steps,
+                                                                     threads))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws,
+            "steps": k, "warmup": nw, "ms_per_step": 1e3 * el / k,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": "lj_rho0.8_N2^20", "n_particles": w["n"],
+                                            "box": w["box"], "cell_scale": w["scale"]},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": kind,
+                             "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def cpu_baseline(w, cores, w_gpu_sum=None, w_now=None):
+    """The oracle restatement on the host cores over a bounded sample (about
+    15 s) of the same workload; failures are reported, with diagnostics of
+    the starting state, instead of ending the run."""
+    try:
+        v, steps, secs = cpu_port_rate(w, 15.0, cores)
+        return {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                "sample": "N=%d, %d whole steps (%.1f s) of the same workload" % (
+                    w["n"], steps, secs)}
+    except Exception as e:  # report, do not hide: the GPU numbers stay valid
+        diag = {"error": str(e), "pos_sum_fresh": float(np.sum(w["pos"]))}
+        if w_gpu_sum is not None:
+            diag["pos_sum_at_start"] = w_gpu_sum
+            diag["pos_sum_after_gpu"] = float(np.sum(w_now["pos"]))
+        try:
+            from scipy.spatial import cKDTree
+            p = np.mod(w["pos"].reshape(-1, 3), w["box"])
+            d, _ = cKDTree(p, boxsize=w["box"]).query(p, k=2)
+            diag["min_pair_distance"] = float(d[:, 1].min())
+        except Exception as e2:
+            diag["kdtree"] = str(e2)
+        return {"value": None, "unit": UNIT, "cores": cores, "kind": "port", "diag": diag}
+
+
+def pinned(n):
+    import torch
+    return torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+
+
+def e2e_dropin(psim, w, state, n_steps):
+    """The reference's step loop on host arrays with the GPU drop-ins:
+    force_evaluate -> nextSystem (with push) -> cells_build.  Returns
+    (particle-steps/s, h2d bytes/step, d2h bytes/step)."""
+    n, box, scale = w["n"], w["box"], w["scale"]
+    g = psim.geometry(n, box, box / scale, scale)
+    p = psim.make_force("LJ", RC, kT=KT, well_depth=WD, lj_num=LJN, yukawa_strength=0.0)
+    buf = {k: pinned(3 * n) for k in ("pos", "pos0", "vel", "frc", "frc0")}
+    for k in buf:
+        buf[k][:] = state[k]
+    mass = pinned(n)
+    mass[:] = 1.0
+    rad = pinned(n)
+    rad[:] = 0.5
+    it = psim.Integrator(n, gamma=GAMMA, dt=DT, kT=KT, vel_freq=1000)
+    hi, cse, srt = psim.cells_build(g, buf["pos"], rad)
+    t_cur = DT  # continue as a normal step
+    ncell = scale ** 3
+    t0 = time.perf_counter()
+    for _ in range(n_steps):
+        f = psim.force_evaluate(p, g, srt, hi, cse, precision=psim.PRECISION_MIXED)
+        it.next_system(t_cur, box, buf["pos"], buf["pos0"], buf["vel"], buf["frc"], buf["frc0"],
+                       mass, particle_force=f)
+        hi, cse, srt = psim.cells_build(g, buf["pos"], rad)
+        t_cur += DT
+    el = time.perf_counter() - t0
+    h2d = (32 * n + 8 * n + 8 * ncell) + (24 * n * 6 + 8 * n) + (24 * n + 8 * n)
+    d2h = 24 * n + 24 * n * 5 + (8 * n + 8 * ncell + 32 * n)
+    it.close()
+    return n * n_steps / el, h2d, d2h
+
+
+def run_gpu(args):
+    import proteinsim2015_gb300 as psim
+    ws, rank, local = dist_env()
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    dev = local
+    if psim.device_count() <= dev:
+        raise SystemExit("no CUDA device %d" % dev)
+    w = workload()
+    pos_sum = float(np.sum(w["pos"]))
+    n, box, scale = w["n"], w["box"], w["scale"]
+    g = psim.geometry(n, box, box / scale, scale)
+    p = psim.make_force("LJ", RC, kT=KT, well_depth=WD, lj_num=LJN, yukawa_strength=0.0)
+    seed = 90210 + 7919 * rank   # independent replicas per rank
+    s = psim.System(g, p, gamma=GAMMA, dt=DT, kT=KT, vel_freq=1000, seed=seed,
+                    precision=psim.PRECISION_MIXED, device=dev)
+    s.upload(w["pos"], w["radius"], vel=w["vel"])
+    s.step(max(args.warmup, 3))          # W >= 3 untimed warm-up steps (melting the lattice)
+    if dist:
+        dist.barrier()
+    with ClockSampler(dev) as clk:
+        ms = s.time_steps(args.steps)
+    if dist:
+        import torch
+        t = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = ws * n * args.steps / (ms * 1e-3)
+    if rank != 0:
+        dist.barrier()
+        return 0
+    # ---- per-phase device times on the mixed form (roofline of the force pass)
+    prof = s.profile(20)
+    pairs = s.pair_count(RC)
+    if args.profile_only:
+        print(json.dumps({"profile_only": True, "value": value, "unit": UNIT,
+                          "ms_per_step": ms / args.steps, "phases_ms": prof,
+                          "pairs_per_particle": pairs}))
+        s.close()
+        return 0
+    state = s.download()
+    # ---- plain FP64 form on the same melted state
+    s64 = psim.System(g, p, gamma=GAMMA, dt=DT, kT=KT, vel_freq=1000, seed=seed,
+                      precision=psim.PRECISION_FP64, device=dev)
+    s64.upload(state["pos"], w["radius"], vel=state["vel"], pos0=state["pos0"],
+               frc=state["frc"], frc0=state["frc0"])
+    s64.step(2)
+    k64 = max(5, min(args.steps // 20, 50))
+    ms64 = s64.time_steps(k64)
+    prof64 = s64.profile(3)
+    plain = n * k64 / (ms64 * 1e-3)
+    # ---- force error of the mixed form against FP64 on the melted state
+    hi, cse, srt = s.download_cells()
+    f64 = psim.force_evaluate(p, g, srt, hi, cse, precision=psim.PRECISION_FP64)
+    f32 = psim.force_evaluate(p, g, srt, hi, cse, precision=psim.PRECISION_MIXED)
+    ferr = float(np.linalg.norm(f32 - f64) / np.linalg.norm(f64))
+    fmax = float(np.max(np.abs(f32 - f64).reshape(-1, 3).max(1) /
+                     np.maximum(np.abs(f64).reshape(-1, 3).max(1), 1e-300)))
+    s64.close()
+    # ---- end to end through the reference-layout drop-ins on pinned host buffers
+    e2e_steps = max(3, min(args.steps // 50, 10))
+    e2e_v, h2d, d2h = e2e_dropin(psim, w, state, e2e_steps)
+    # ---- roofline of the dominant kernel (the force pass)
+    fp32_peak = psim.measure_fp32_peak(dev)
+    f_ms = prof["force_ms"]
+    flops_launch = n * pairs * FLOPS_PER_PAIR_LJ
+    achieved = flops_launch / (f_ms * 1e-3) / 1e12
+    peaks = measured_peaks()
+    # ---- CPU baseline: the oracle restatement on the host cores, bounded sample
+    cores = os.cpu_count() or 1
+    cpu = cpu_baseline(workload(), cores, w_gpu_sum=pos_sum, w_now=w)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32-pair/f64-update",
+        "data": "synthetic FCC-melt start, seeded Maxwell-Boltzmann velocities",
+        "config": {"workload": "lj_rho0.8_N2^20", "n_particles": n, "box": box,
+                   "cell_scale": scale, "cell_size": box / scale, "potential": "LJ 12-6 rc=2.5",
+                   "kT": KT, "gamma": GAMMA, "dt": DT, "precision": "mixed",
+                   "noise": "philox", "parallelism": "replicas" if ws > 1 else "single",
+                   "l2": "inputs larger than L2 (FP64 SoA state ~300 MB, sorted copies 32 MB)"},
+        "plain_fp64": {"value": plain, "unit": UNIT, "steps": k64, "ms_per_step": ms64 / k64,
+                       "force_ms": prof64["force_ms"]},
+        "speedup_vs_fp64": value / plain,
+        "force_rel_err": ferr, "force_rel_err_max_particle": fmax,
+        "phases_ms": {k: round(v, 5) for k, v in prof.items()},
+        "pairs_per_particle": pairs,
+        "e2e": {"value": e2e_v, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "steps": e2e_steps,
+                "path": "force_evaluate -> next_system -> cells_build on pinned host arrays"},
+        "gpu_launches": args.steps * s.launches_per_step(),
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak,
+                     "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": None,
+                     "kernel": "force_mixed_kernel<LJPair>",
+                     "algorithmic": "%d FLOP/pair x %.2f pairs/particle x N per launch" % (
+                         FLOPS_PER_PAIR_LJ, pairs),
+                     "peak_source": "measured FP32 FMA probe (MEASURED_PEAKS.json has no FP32 figure)",
+                     "hbm_peak_gbs": peaks.get("hbm_gbs")},
+        "cpu_baseline": cpu,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+    if dist:
+        dist.barrier()
+    s.close()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--profile-only", action="store_true",
+                    help="time the mixed form and its phases only (short runs under ncu)")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,284 @@
+/*
+ * psim_gb300.h -- C ABI of the GB300-native ProteinSim2015 Langevin step.
+ *
+ * One library, libpsim_gb300.so, runs the reference's hot path on one GPU
+ * (sm_103a): the hashed cell-list rebuild, pair forces from the IForce
+ * plugins (AOPotential, LennardJones, Calibration) and the van Gunsteren-
+ * Berendsen stochastic-dynamics integrator.  Plain pointers and sizes only.
+ *
+ * Three layers of entry points:
+ *   1. Drop-ins that take the reference's own host arrays (psim_cells_build,
+ *      psim_force_evaluate, psim_integrator_*): each replaces one reference
+ *      routine, cited beside it, with the same array layouts.  Host buffers in,
+ *      host buffers out; the copies to and from the GPU are inside the call.
+ *   2. A device-resident system (psim_system_*): the whole step loop of
+ *      system::run on the GPU with no per-step host traffic.
+ *   3. Plugin parameters (psim_force_params_*): the settings.cfg keys each
+ *      plugin reads, so a plugin's getForce(config*) factory maps onto a
+ *      device pair functor.
+ *
+ * Status codes are the reference's exit codes (ClusteredCore/src/utilities/
+ * error.cpp:27-68; the loader's 100 from ClusteredUI/src/runSim.cpp:41-58),
+ * returned instead of terminating the process.
+ *
+ * Array layouts (the reference's, ClusteredCore/include/system.h:33-38):
+ *   pos, pos0, vel, frc, frc0   3n doubles, xyz per particle, original order
+ *   particle_hash_index         2n int32 (cell hash, original index), sorted
+ *   cell_start_end              2*s^3 uint32 (start, end); empty = 0xffffffff
+ *   sorted_particles            4n doubles {x, y, z, radius}, sorted order
+ *   particle_force              3n doubles, original order
+ */
+#ifndef PSIM_GB300_H
+#define PSIM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    PSIM_OK = 0,
+    PSIM_ERR_LOAD = 100,             /* plugin not loadable (runSim.cpp:41-58) */
+    PSIM_ERR_INIT = 7701,            /* error.cpp:27-32 */
+    PSIM_ERR_CELL_BOUNDS = 7702,     /* error.cpp:34-38: a particle hashed outside the grid */
+    PSIM_ERR_PARTICLE_BOUNDS = 7703, /* error.cpp:40-45: particle.cpp:67-69 */
+    PSIM_ERR_OVERLAP = 7704,         /* error.cpp:47-55: AOPotential.cpp:85-88 */
+    PSIM_ERR_NAN_FORCE = 7705,       /* error.cpp:57-62: AOPotential.cpp:105-109 */
+    PSIM_ERR_INPUT = 7706,           /* error.cpp:64-68: invalid arguments */
+    PSIM_ERR_CUDA = 7790,            /* CUDA runtime failure, see psim_last_error_string */
+    PSIM_ERR_NO_DEVICE = 7791        /* no CUDA device */
+};
+
+typedef enum {
+    PSIM_FORCE_AO = 1,          /* AOPotential/src/AOPotential.cpp */
+    PSIM_FORCE_LJ = 2,          /* LennardJones/src/LJPotential.cpp */
+    PSIM_FORCE_CALIBRATION = 3, /* Calibration/src/Calibration.cpp */
+    PSIM_FORCE_AO_YUKAWA = 4    /* AO + LJ(n) summed (the reference evaluates one plugin only) */
+} psim_force_kind;
+
+typedef enum {
+    PSIM_PRECISION_FP64 = 0,  /* plain form: FP64 throughout, reference operation order */
+    PSIM_PRECISION_MIXED = 1  /* FP32 pair math + Kahan-compensated FP32 sums, FP64 update */
+} psim_precision;
+
+typedef enum {
+    PSIM_NOISE_PHILOX = 0,   /* counter-based Philox4x32-10 Gaussians keyed by (seed, particle) */
+    PSIM_NOISE_INJECTED = 1  /* caller-supplied Gaussians in the reference draw order */
+} psim_noise_mode;
+
+/* Pair-force parameters under the reference's settings.cfg keys.
+ * AOPotential.cpp:33-59: kT, wellDepth (0.261), cutOff (1.1).
+ * LJPotential.cpp:29-62: kT, wellDepth (10), yukawaStrength (8), ljNum (18),
+ *                        cutOff (2.5), debyeLength (0.5).
+ * Calibration.cpp:30-39: cutOff (1.1).
+ * PSIM_FORCE_AO_YUKAWA: the AO part uses kT/well_depth/cutoff, the LJ(n)
+ * part kT/well_depth2/yukawa_strength/debye_length/lj_num/cutoff2. */
+typedef struct {
+    int32_t kind;
+    int32_t lj_num;
+    double kT;
+    double cutoff;
+    double well_depth;
+    double yukawa_strength;
+    double debye_length;
+    double cutoff2;
+    double well_depth2;
+} psim_force_params;
+
+/* Cell-grid geometry: mirrors systemState's boxSize/cellSize/cellScale
+ * (ClusteredCore/include/structs/systemState.h:7-19), widened to double so a
+ * box need not be an integer.  Requires scale >= 3, cell_size * scale == box
+ * and cell_size >= the largest cutoff (checked; the reference does not). */
+typedef struct {
+    int32_t n_particles;
+    int32_t cell_scale;
+    double box_size;
+    double cell_size;
+} psim_geometry;
+
+/* vGB coefficients (brownianIntegrator.cpp:27-99, :111-175). */
+typedef struct {
+    double y, coeff0, coeff1, coeff2, coeff3;
+    double sig1, sig2, corr, dev;
+    double goy2, goy3, hn, gn;
+} psim_vgb_coeffs;
+
+/* Integrator settings: the brownianIntegrator keys of settings.cfg
+ * (brownianIntegrator.cpp:33-83): gamma (0.5), timeStep (0.001), kT (1),
+ * velFreq (1000), seed (90210). */
+typedef struct {
+    double gamma;
+    double dt;
+    double kT;
+    int32_t vel_freq;
+    int32_t seed;
+} psim_integrator_config;
+
+/* ------------------------------------------------------------ general */
+
+/* Version of this ABI (bumped on any layout change). */
+int psim_abi_version(void);
+/* Text of the last error on the calling thread ("" if none). */
+const char* psim_last_error_string(void);
+/* Number of usable CUDA devices (0 on a machine without a GPU). */
+int psim_device_count(void);
+
+/* ---------------------------------------------------- plugin parameters */
+
+/* Fill params from settings.cfg text (key = value lines; '#' at column 0
+ * starts a comment, as config.cpp:27-56) with the plugin's defaults for
+ * missing keys.  plugin is the reference plugin name: "AOPotential",
+ * "LennardJones", "Calibration", or "AOYukawa" for the composite, whose LJ
+ * part reads the keys prefixed "yukawa." (e.g. "yukawa.cutOff").
+ * Replaces the plugin constructors AOPotential.cpp:33-59,
+ * LJPotential.cpp:29-62, Calibration.cpp:30-39.  Returns PSIM_ERR_LOAD for
+ * an unknown plugin name. */
+int psim_force_params_from_settings(const char* plugin, const char* settings_text,
+                                    psim_force_params* out);
+
+/* The AO coefficients coEff1/coEff2 (AOPotential.cpp:50-55). */
+int psim_ao_coefficients(double kT, double well_depth, double cutoff, double* coeff1,
+                         double* coeff2);
+
+/* ------------------------------------ drop-ins on the reference layout */
+
+/* system::hashParticles + sortParticles + clearCells + reorderParticles
+ * (ClusteredCore/src/system/systemHandling.cpp:33-85, system.h:166).
+ * pos: 3n original order; radius: n.  Outputs particle_hash_index (2n),
+ * cell_start_end (2*s^3) and sorted_particles (4n).  Within a cell particles
+ * are ordered by original index (the reference's sort is unstable; cell
+ * membership and hashes are identical). */
+int psim_cells_build(const psim_geometry* geom, const double* pos, const double* radius,
+                     int32_t* particle_hash_index, uint32_t* cell_start_end,
+                     double* sorted_particles);
+
+/* defaultForceManager::getAcceleration (defaultForceManager.cpp:55-65) with
+ * the plugin's getAcceleration/iterCells (e.g. AOPotential.cpp:61-175) on
+ * a cell list in the reference layout.  Writes particle_force (3n, original
+ * order).  Returns PSIM_ERR_OVERLAP / PSIM_ERR_NAN_FORCE where the
+ * reference would have exited with those codes. */
+int psim_force_evaluate(const psim_force_params* params, const psim_geometry* geom,
+                        int32_t precision, const double* sorted_particles,
+                        const int32_t* particle_hash_index, const uint32_t* cell_start_end,
+                        double* particle_force);
+
+/* The brownianIntegrator constructor's coefficient set-up
+ * (brownianIntegrator.cpp:27-99).  gamma == 0 reproduces the reference's
+ * non-finite noise widths; such coefficients are refused by the steppers. */
+int psim_vgb_coefficients(double gamma, double dt, double kT, psim_vgb_coeffs* out);
+
+/* brownianIntegrator: the object holding the per-particle noise memory
+ * (memX/Y/Z, memCorrX/Y/Z) and the velocity counter
+ * (ClusteredCore/include/integrator.h:20-158).  Device-resident. */
+typedef struct psim_integrator psim_integrator;
+psim_integrator* psim_integrator_create(const psim_integrator_config* cfg, int32_t n_particles);
+void psim_integrator_destroy(psim_integrator* integ);
+
+/* system::pushParticleForce (systemHandling.cpp:87-92) when particle_force is
+ * not NULL, then brownianIntegrator::nextSystem (brownianIntegrator.cpp:
+ * 181-356) on host arrays in original order.  current_time == 0 selects
+ * firstStep as the reference does.  noise: n*6 Gaussians in the reference
+ * draw order (firstStep uses the first 3 per particle) for
+ * PSIM_NOISE_INJECTED, ignored for PSIM_NOISE_PHILOX.  pos/pos0/vel/frc/frc0
+ * are updated in place.  box_size: the box edge L. */
+int psim_integrator_next_system(psim_integrator* integ, double current_time, double box_size,
+                                int32_t noise_mode, const double* noise,
+                                const double* particle_force, double* pos, double* pos0,
+                                double* vel, double* frc, double* frc0, const double* mass);
+
+/* --------------------------------------------- device-resident system */
+
+typedef struct psim_system psim_system;
+
+typedef struct {
+    psim_geometry geom;
+    psim_integrator_config integ;
+    psim_force_params force;
+    int32_t precision;   /* psim_precision */
+    int32_t noise_mode;  /* psim_noise_mode */
+    int32_t device;      /* CUDA device ordinal */
+} psim_system_config;
+
+/* Creates the system and its device buffers (the role of system::system,
+ * system.cpp:69-103, without the random initialisation: states are uploaded). */
+psim_system* psim_system_create(const psim_system_config* cfg);
+void psim_system_destroy(psim_system* sys);
+
+/* Loads a particle state (original order, reference layout) and builds the
+ * first cell list (system.cpp:101-103).  pos0/vel/frc/frc0/mass may be NULL
+ * (zeros; mass 1).  The step counter restarts at 0, so the next step is the
+ * reference's firstStep, as after RecoverySystem (systemRecovery.cpp:43-81). */
+int psim_system_upload(psim_system* sys, const double* pos, const double* pos0,
+                       const double* vel, const double* frc, const double* frc0,
+                       const double* radius, const double* mass);
+
+/* Injected noise for PSIM_NOISE_INJECTED: n_steps*n*6 doubles, step-major,
+ * then particle (original index), then the 6 draws of one normal step
+ * (xi_x, xi_y, xi_z, mem_x, mem_y, mem_z; firstStep uses the first 3).
+ * Covers steps [first_step, first_step + n_steps) of the step counter. */
+int psim_system_set_noise(psim_system* sys, const double* noise, int32_t n_steps,
+                          int32_t first_step);
+
+/* Runs n_steps iterations of system::run's hot loop (system.cpp:187-206):
+ * forces, push, nextSystem, cell-list rebuild.  Asynchronous launches; the
+ * call waits for the GPU at the end and returns the first error any step
+ * raised (the state is then that of the failing step). */
+int psim_system_step(psim_system* sys, int32_t n_steps);
+
+/* Enqueues n_steps without waiting (timing loops); errors are latched and
+ * returned by the next psim_system_step / psim_system_sync. */
+int psim_system_step_async(psim_system* sys, int32_t n_steps);
+int psim_system_sync(psim_system* sys);
+
+/* Current state in original order.  Any pointer may be NULL. */
+int psim_system_download(psim_system* sys, double* pos, double* pos0, double* vel,
+                         double* frc, double* frc0);
+/* Current cell list in the reference layout.  Any pointer may be NULL. */
+int psim_system_download_cells(psim_system* sys, int32_t* particle_hash_index,
+                               uint32_t* cell_start_end, double* sorted_particles);
+
+/* Snapshot on a side stream: positions (3n, original order) are copied into
+ * host memory without stalling the step stream; psim_system_snapshot_wait
+ * blocks until that copy is complete.  host_pos should be pinned
+ * (cudaHostAlloc) for the copy to be asynchronous. */
+int psim_system_snapshot_async(psim_system* sys, double* host_pos);
+int psim_system_snapshot_wait(psim_system* sys);
+
+/* Step counter (0 = next step is firstStep) and velocity counter. */
+int psim_system_get_step(psim_system* sys, int64_t* step, int32_t* vel_counter);
+
+/* The CUDA stream all step kernels are launched on (cudaStream_t). */
+void* psim_system_stream(psim_system* sys);
+
+/* Per-phase device time of the last n_steps, measured with CUDA events on
+ * the step stream: out_ms[0] forces, [1] integrator, [2] cell-list rebuild,
+ * [3] total.  Runs n_steps steps. */
+int psim_system_profile(psim_system* sys, int32_t n_steps, double* out_ms);
+
+/* Number of kernel launches one step issues (for launch accounting). */
+int psim_system_launches_per_step(psim_system* sys);
+
+/* Occupancy of the current cell list: max and mean particles per cell. */
+int psim_system_cell_occupancy(psim_system* sys, int32_t* max_occ, double* mean_occ);
+
+/* Enqueues n_steps and returns their device time in milliseconds, measured
+ * with CUDA events recorded on the step stream around the launches. */
+int psim_system_time_steps(psim_system* sys, int32_t n_steps, double* ms);
+
+/* Mean number of ordered pairs (i, j != i) closer than `cutoff` per
+ * particle in the current cell list (diagnostic for the pair-work count). */
+int psim_system_pair_count(psim_system* sys, double cutoff, double* mean_pairs);
+
+/* ----------------------------------------------------------- measurement */
+
+/* Sustained FP32 FMA throughput of `device` in TFLOP/s (an FMA = 2 flops),
+ * measured with a register-resident FMA-chain kernel over all SMs; the
+ * denominator of the force pass's FP32 roofline. */
+int psim_measure_fp32_peak(int32_t device, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PSIM_GB300_H */

@@ -1,0 +1,1335 @@
+// psim_api.cu -- host implementation of the C ABI (include/psim_gb300.h).
+//
+// Validation, settings.cfg parsing for the plugin parameters, the reference-
+// layout drop-ins, and the device-resident system whose step is
+//   force -> memset(next counts) -> vGB (+hash, count) -> scan -> scatter ->
+//   canonicalise (+gather, step counter)
+// captured once per buffer phase into CUDA graphs.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/psim_gb300.h"
+#include "psim_kernels.cuh"
+
+using namespace psim;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+#define PSIM_CUDA(call)                                                                     \
+    do {                                                                                    \
+        cudaError_t e_ = (call);                                                            \
+        if (e_ != cudaSuccess)                                                              \
+            return fail(PSIM_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                        __FILE__, __LINE__);                                                \
+    } while (0)
+
+int code_from_bits(uint32_t bits) {
+    // the reference's exit order inside a step: force pass (overlap, NaN),
+    // then the integrator (bounds), then the hash
+    if (bits & EBIT_OVERLAP) return PSIM_ERR_OVERLAP;
+    if (bits & EBIT_NAN) return PSIM_ERR_NAN_FORCE;
+    if (bits & EBIT_BOUNDS) return PSIM_ERR_PARTICLE_BOUNDS;
+    if (bits & EBIT_CELL) return PSIM_ERR_CELL_BOUNDS;
+    if (bits & (EBIT_NOISE | EBIT_INDEX)) return PSIM_ERR_INPUT;
+    return PSIM_OK;
+}
+
+const char* bits_text(uint32_t bits) {
+    if (bits & EBIT_OVERLAP) return "significant particle overlap (r < 0.8 (Ri + Rj))";
+    if (bits & EBIT_NAN) return "non-finite force";
+    if (bits & EBIT_BOUNDS) return "particle out of bounds after the periodic wrap";
+    if (bits & EBIT_CELL) return "particle hashed outside the cell grid";
+    if (bits & EBIT_NOISE) return "injected noise does not cover the step";
+    if (bits & EBIT_INDEX) return "an index or cell range in the input is out of bounds";
+    return "";
+}
+
+// ------------------------------------------------------------- settings.cfg
+
+// config.cpp:27-56: "key = value" lines, '#' in column 0 starts a comment,
+// whitespace around key and value is trimmed.  Values parse like std::stod /
+// std::stoi: the leading number counts ("10;" is 10).
+struct Settings {
+    std::vector<std::pair<std::string, std::string>> kv;
+    explicit Settings(const char* text) {
+        if (!text) return;
+        const char* p = text;
+        while (*p) {
+            const char* e = p;
+            while (*e && *e != '\n') ++e;
+            std::string line(p, e);
+            if (!line.empty() && line.back() == '\r') line.pop_back();
+            if (!line.empty() && line[0] != '#') {
+                size_t eq = line.find('=');
+                std::string key = line.substr(0, eq), val = eq == std::string::npos ? "" : line.substr(eq + 1);
+                auto trim = [](std::string& s) {
+                    size_t a = s.find_first_not_of(" \t\r\n\v\f");
+                    size_t b = s.find_last_not_of(" \t\r\n\v\f");
+                    s = (a == std::string::npos) ? std::string() : s.substr(a, b - a + 1);
+                };
+                trim(key);
+                trim(val);
+                bool found = false;
+                for (auto& q : kv)
+                    if (q.first == key) { q.second = val; found = true; }
+                if (!found) kv.emplace_back(key, val);
+            }
+            p = *e ? e + 1 : e;
+        }
+    }
+    const std::string* find(const std::string& k) const {
+        for (auto& q : kv)
+            if (q.first == k) return &q.second;
+        return nullptr;
+    }
+    bool get_double(const std::string& k, double def, double* out) const {
+        const std::string* v = find(k);
+        if (!v) { *out = def; return true; }
+        char* end = nullptr;
+        double d = strtod(v->c_str(), &end);
+        if (end == v->c_str()) return false;
+        *out = d;
+        return true;
+    }
+    bool get_int(const std::string& k, int def, int* out) const {
+        const std::string* v = find(k);
+        if (!v) { *out = def; return true; }
+        char* end = nullptr;
+        long d = strtol(v->c_str(), &end, 10);
+        if (end == v->c_str()) return false;
+        *out = (int)d;
+        return true;
+    }
+};
+
+// ------------------------------------------------------------- validation
+
+int check_params(const psim_force_params* p) {
+    if (!p) return fail(PSIM_ERR_INPUT, "force params are NULL");
+    if (p->kind < 1 || p->kind > 4) return fail(PSIM_ERR_INPUT, "unknown force kind %d", p->kind);
+    if (!(p->cutoff > 0.0) || !std::isfinite(p->cutoff))
+        return fail(PSIM_ERR_INPUT, "cutOff must be positive and finite");
+    if ((p->kind == 1 || p->kind == 4) && !(p->cutoff > 1.0))
+        return fail(PSIM_ERR_INPUT, "AO cutOff must exceed 1 (coefficients divide by cutOff - 1)");
+    if (p->kind == 2 || p->kind == 4) {
+        if (p->lj_num < 0 || p->lj_num > 64) return fail(PSIM_ERR_INPUT, "ljNum out of range");
+        if (!(p->debye_length > 0.0)) return fail(PSIM_ERR_INPUT, "debyeLength must be positive");
+    }
+    if (p->kind == 4 && !(p->cutoff2 > 0.0))
+        return fail(PSIM_ERR_INPUT, "the composite needs the LJ part's cutOff");
+    return PSIM_OK;
+}
+
+double max_cutoff(const psim_force_params* p) {
+    return p->kind == 4 ? std::max(p->cutoff, p->cutoff2) : p->cutoff;
+}
+
+int make_geom(const psim_geometry* gm, double rc_max, DevGeom* g) {
+    if (!gm) return fail(PSIM_ERR_INPUT, "geometry is NULL");
+    if (gm->n_particles < 0) return fail(PSIM_ERR_INPUT, "negative particle count");
+    if (gm->cell_scale < 3)
+        return fail(PSIM_ERR_INPUT, "cellScale %d < 3: the 27-cell stencil would visit a cell twice",
+                    gm->cell_scale);
+    if (gm->cell_scale > 256) return fail(PSIM_ERR_INPUT, "cellScale %d > 256", gm->cell_scale);
+    if (!(gm->box_size > 0.0) || !(gm->cell_size > 0.0))
+        return fail(PSIM_ERR_INPUT, "box and cell size must be positive");
+    double span = gm->cell_size * gm->cell_scale;
+    if (std::fabs(span - gm->box_size) > 1e-9 * gm->box_size)
+        return fail(PSIM_ERR_INPUT, "cellSize * cellScale (%.17g) != boxSize (%.17g)", span,
+                    gm->box_size);
+    if (rc_max > 0.0 && gm->cell_size < rc_max)
+        return fail(PSIM_ERR_INPUT, "cellSize %.9g is below the cutoff %.9g", gm->cell_size, rc_max);
+    g->n = gm->n_particles;
+    g->s = gm->cell_scale;
+    g->s2 = g->s * g->s;
+    g->ncell = g->s2 * g->s;
+    g->L = gm->box_size;
+    g->half = g->L / 2.0;
+    double fl = std::floor(g->L);
+    g->half_uv = (fl == g->L && g->L < 2147483647.0) ? (double)(((int)g->L) / 2) : g->L / 2.0;
+    g->cs = gm->cell_size;
+    g->inv_cs = 1.0 / gm->cell_size;
+    g->Lhi = (float)g->L;
+    g->Llo = (float)(g->L - (double)g->Lhi);
+    return PSIM_OK;
+}
+
+void ao_coeffs(double kT, double wd, double rc, double* c1, double* c2) {  // AOPotential.cpp:50-55
+    double q = rc / (rc - 1.0);
+    double a1 = -kT * wd * q * q * q;
+    double a2 = -3.0 / (2.0 * rc);
+    double a3 = 1.0 / (2.0 * rc * rc * rc);
+    *c1 = -a1 * a2;
+    *c2 = -3.0 * a1 * a3;
+}
+
+ForceSetup make_setup(const psim_force_params* p, double L) {
+    ForceSetup fs{};
+    fs.kind = p->kind;
+    double rc_ao = p->cutoff;
+    double rc_lj = p->kind == 4 ? p->cutoff2 : p->cutoff;
+    double c1, c2;
+    ao_coeffs(p->kT, p->well_depth, rc_ao, &c1, &c2);
+    fs.ao.rc2 = rc_ao * rc_ao;
+    fs.ao.c1 = c1;
+    fs.ao.c2 = c2;
+    fs.ao.rc2f = (float)fs.ao.rc2;
+    fs.ao.c1f = (float)c1;
+    fs.ao.c2f = (float)c2;
+    double wd_lj = p->kind == 4 ? p->well_depth2 : p->well_depth;
+    fs.lj.rc2 = rc_lj * rc_lj;
+    fs.lj.kTwd = p->kT * wd_lj;
+    fs.lj.n = p->lj_num;
+    fs.lj.four_n = 4.0 * p->lj_num;
+    fs.lj.yuk = p->yukawa_strength;
+    fs.lj.lambda = p->debye_length;
+    fs.lj.inv_lambda = 1.0 / p->debye_length;
+    fs.lj.rc2f = (float)fs.lj.rc2;
+    fs.lj.kTwdf = (float)fs.lj.kTwd;
+    fs.lj.four_nf = (float)fs.lj.four_n;
+    fs.lj.yukf = (float)fs.lj.yuk;
+    fs.lj.lambdaf = (float)fs.lj.lambda;
+    fs.lj.inv_lambdaf = (float)fs.lj.inv_lambda;
+    fs.cal.rc2 = p->cutoff * p->cutoff;
+    fs.cal.rc2f = (float)fs.cal.rc2;
+    fs.rc_max = max_cutoff(p);
+    // The FP32 prefilter sees positions rounded to FP32 (error <= ulp(L)/2
+    // each, plus the rounding of L and of the difference): bound the error
+    // of a separation by 4 ulp(L) and widen the cutoff by that much.
+    double ulpL = std::ldexp(1.0, std::ilogb(std::max(L, 1.0)) - 23);
+    double rpre = fs.rc_max * (1.0 + 1e-6) + 4.0 * ulpL + 1e-6;
+    fs.pre_rc2f = (float)(rpre * rpre * (1.0 + 1e-6));
+    return fs;
+}
+
+// brownianIntegrator.cpp:27-99 with setupHigh/setupLow/setupZero (:111-175)
+void vgb_coeffs(double gamma, double dt, double kT, psim_vgb_coeffs* c) {
+    double y = gamma * dt;
+    c->y = y;
+    {
+        double ty = 2.0 * y;
+        c->coeff0 = exp(-y);
+        double aa1 = 1.0 - c->coeff0;
+        double aa2 = 0.5 * y * (1.0 + c->coeff0) - aa1;
+        double aa3 = y - aa1;
+        c->coeff1 = aa1 / y;
+        c->coeff2 = aa2 / (y * y);
+        c->coeff3 = aa3 / (y * y);
+        c->sig1 = 2.0 * y - 3.0 + 4.0 * exp(-y) - exp(-ty);
+        c->sig2 = -2.0 * y - 3.0 + 4.0 * exp(y) - exp(ty);
+        c->gn = exp(y) - ty - exp(-y);
+        c->goy2 = c->gn / (y * y);
+        c->goy3 = c->gn / (y * y * y);
+        c->hn = y / (exp(y) - exp(-y));
+    }
+    if (gamma < 0.05) {  // series expansion (setupLow); coEff0 keeps setupHigh's value
+        double y1 = y, y2 = y1 * y1, y3 = y2 * y1, y4 = y3 * y1, y5 = y4 * y1;
+        double y6 = y5 * y1, y7 = y6 * y1, y8 = y7 * y1, y9 = y8 * y1;
+        c->coeff1 = 1.0 - 0.5 * y1 + (1.0 / 6.0) * y2 - (1.0 / 24.0) * y3 + (1.0 / 120.0) * y4;
+        c->coeff2 = (1.0 / 12.0) * y1 - (1.0 / 24.0) * y2 + (1.0 / 80.0) * y3 - (1.0 / 360.0) * y4;
+        c->coeff3 = 0.5 - (1.0 / 6.0) * y1 + (1.0 / 24.0) * y2 - (1.0 / 120.0) * y3;
+        c->sig1 = +(2.0 / 3.0) * y3 - 0.5 * y4 + (7.0 / 30.0) * y5 - (1.0 / 12.0) * y6
+                  + (31.0 / 1260.0) * y7 - (1.0 / 160.0) * y8 + (127.0 / 90720.0) * y9;
+        c->sig2 = -(2.0 / 3.0) * y3 - 0.5 * y4 - (7.0 / 30.) * y5 - (1.0 / 12.0) * y6
+                  - (31.0 / 1260.0) * y7 - (1.0 / 160.0) * y8 - (127.0 / 90720.0) * y9;
+        c->goy2 = (1.0 / 3.0) * y1 + (1.0 / 60.0) * y3;
+        c->goy3 = 1.0 / 3.0 + (1.0 / 60.0) * y2;
+        c->hn = 0.5 - (1.00 / 12.0) * y2 + (7.0 / 720.0) * y4;
+        c->gn = (1.0 / 3.0) * y3 + (1.0 / 60.0) * y5;
+    }
+    if (gamma == 0) {
+        c->coeff0 = 1.0;
+        c->coeff1 = 1.0;
+        c->coeff2 = 0.0;
+        c->coeff3 = 0.5;
+    }
+    double gamma2 = gamma * gamma;
+    c->sig1 = sqrt(+kT * c->sig1 / gamma2);
+    c->sig2 = sqrt(-kT * c->sig2 / gamma2);
+    c->corr = (kT / (gamma2)) * (c->gn / (c->sig1 * c->sig2));
+    c->dev = sqrt(1.0 - (c->corr * c->corr));
+}
+
+int make_vgb_params(const psim_integrator_config* ic, VgbParams* p) {
+    if (!ic) return fail(PSIM_ERR_INPUT, "integrator config is NULL");
+    if (!(ic->dt > 0.0)) return fail(PSIM_ERR_INPUT, "timeStep must be positive");
+    if (ic->vel_freq < 0) return fail(PSIM_ERR_INPUT, "velFreq must be >= 0");
+    psim_vgb_coeffs c;
+    vgb_coeffs(ic->gamma, ic->dt, ic->kT, &c);
+    const double v[] = {c.coeff0, c.coeff1, c.coeff2, c.coeff3, c.sig1,
+                        c.sig2,   c.corr,   c.dev,    c.goy2,   c.goy3, c.hn};
+    for (double x : v)
+        if (!std::isfinite(x))
+            return fail(PSIM_ERR_INPUT,
+                        "vGB coefficients are not finite for gamma=%g dt=%g kT=%g (the "
+                        "reference's gamma == 0 set-up divides by gamma^2)",
+                        ic->gamma, ic->dt, ic->kT);
+    p->dt = ic->dt;
+    p->dt2 = ic->dt * ic->dt;
+    p->dt3 = ic->dt * p->dt2;
+    p->dt_inv = 1.0 / ic->dt;
+    p->c0 = 1.0 + c.coeff0;
+    p->coeff0 = c.coeff0;
+    p->coeff1 = c.coeff1;
+    p->coeff2 = c.coeff2;
+    p->coeff3 = c.coeff3;
+    p->sig1 = c.sig1;
+    p->sig2 = c.sig2;
+    p->corr = c.corr;
+    p->dev = c.dev;
+    p->goy2 = c.goy2;
+    p->goy3 = c.goy3;
+    p->hn = c.hn;
+    p->vel_freq = ic->vel_freq;
+    p->seed = (uint32_t)ic->seed;
+    return PSIM_OK;
+}
+
+int ensure_device() {
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return fail(PSIM_ERR_NO_DEVICE, "no CUDA device available (%s)",
+                    e == cudaSuccess ? "count 0" : cudaGetErrorString(e));
+    }
+    return PSIM_OK;
+}
+
+// ------------------------------------------------------------- buffers
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t b) {
+        if (b <= bytes && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMalloc(&p, b ? b : 16);
+        if (e == cudaSuccess) bytes = b;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+// A temporary device buffer freed when it leaves scope.
+struct ScopedBuf : DevBuf {
+    ~ScopedBuf() { release(); }
+};
+
+// Scratch for the reference-layout drop-ins, grown on demand, one set per
+// process (calls are serialised by a mutex).
+struct Workspace {
+    std::mutex mu;
+    int device = -1;
+    cudaStream_t st = nullptr;
+    DevBuf pos, radius, xyz, key, rank, tmp, perm, tag_in, tag_out, radius_out, cellid, count,
+        start, scratch, posd, posh, posl, hash_index, cse, sorted, force, fxyz, err;
+};
+Workspace g_ws;
+
+int ws_begin(Workspace& w) {
+    int dev = 0;
+    PSIM_CUDA(cudaGetDevice(&dev));
+    if (w.st && w.device != dev) {
+        // the caller switched devices: drop the old device's buffers
+        DevBuf* all[] = {&w.pos, &w.radius, &w.xyz, &w.key, &w.rank, &w.tmp, &w.perm, &w.tag_in,
+                         &w.tag_out, &w.radius_out, &w.cellid, &w.count, &w.start, &w.scratch,
+                         &w.posd, &w.posh, &w.posl, &w.hash_index, &w.cse, &w.sorted, &w.force,
+                         &w.fxyz, &w.err};
+        for (DevBuf* b : all) { b->p = nullptr; b->bytes = 0; }
+        w.st = nullptr;
+    }
+    if (!w.st) {
+        PSIM_CUDA(cudaStreamCreateWithFlags(&w.st, cudaStreamNonBlocking));
+        w.device = dev;
+    }
+    return PSIM_OK;
+}
+
+}  // namespace
+
+// ===================================================================== C ABI
+
+extern "C" {
+
+int psim_abi_version(void) { return 1; }
+
+const char* psim_last_error_string(void) { return g_last_error.c_str(); }
+
+int psim_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+int psim_ao_coefficients(double kT, double well_depth, double cutoff, double* coeff1,
+                         double* coeff2) {
+    if (!coeff1 || !coeff2) return fail(PSIM_ERR_INPUT, "NULL output");
+    ao_coeffs(kT, well_depth, cutoff, coeff1, coeff2);
+    return PSIM_OK;
+}
+
+int psim_force_params_from_settings(const char* plugin, const char* text, psim_force_params* out) {
+    if (!plugin || !out) return fail(PSIM_ERR_INPUT, "NULL argument");
+    Settings s(text);
+    std::string name(plugin);
+    psim_force_params p{};
+    bool ok = true;
+    double kT = 1.0;
+    ok &= s.get_double("kT", 1.0, &kT);
+    p.kT = kT;
+    if (name == "AOPotential" || name == "AO") {            // AOPotential.cpp:40-47
+        p.kind = PSIM_FORCE_AO;
+        ok &= s.get_double("wellDepth", 0.261, &p.well_depth);
+        ok &= s.get_double("cutOff", 1.1, &p.cutoff);
+        p.lj_num = 18;
+        p.debye_length = 0.5;
+    } else if (name == "LennardJones" || name == "LJ") {    // LJPotential.cpp:31-55
+        p.kind = PSIM_FORCE_LJ;
+        ok &= s.get_double("wellDepth", 10.0, &p.well_depth);
+        ok &= s.get_double("yukawaStrength", 8.0, &p.yukawa_strength);
+        ok &= s.get_int("ljNum", 18, &p.lj_num);
+        ok &= s.get_double("cutOff", 2.5, &p.cutoff);
+        ok &= s.get_double("debyeLength", 0.5, &p.debye_length);
+    } else if (name == "Calibration" || name == "Cal") {    // Calibration.cpp:33-36
+        p.kind = PSIM_FORCE_CALIBRATION;
+        ok &= s.get_double("cutOff", 1.1, &p.cutoff);
+        p.lj_num = 18;
+        p.debye_length = 0.5;
+    } else if (name == "AOYukawa") {
+        p.kind = PSIM_FORCE_AO_YUKAWA;
+        ok &= s.get_double("wellDepth", 0.261, &p.well_depth);
+        ok &= s.get_double("cutOff", 1.1, &p.cutoff);
+        ok &= s.get_double("yukawa.wellDepth", 10.0, &p.well_depth2);
+        ok &= s.get_double("yukawa.yukawaStrength", 8.0, &p.yukawa_strength);
+        ok &= s.get_int("yukawa.ljNum", 0, &p.lj_num);
+        ok &= s.get_double("yukawa.cutOff", 2.5, &p.cutoff2);
+        ok &= s.get_double("yukawa.debyeLength", 0.5, &p.debye_length);
+    } else {
+        return fail(PSIM_ERR_LOAD, "unknown force plugin '%s'", plugin);
+    }
+    if (!ok) return fail(PSIM_ERR_INPUT, "a settings value for plugin '%s' is not a number", plugin);
+    *out = p;
+    return PSIM_OK;
+}
+
+int psim_vgb_coefficients(double gamma, double dt, double kT, psim_vgb_coeffs* out) {
+    if (!out) return fail(PSIM_ERR_INPUT, "NULL output");
+    vgb_coeffs(gamma, dt, kT, out);
+    return PSIM_OK;
+}
+
+// ----------------------------------------------------------- cells drop-in
+
+int psim_cells_build(const psim_geometry* gm, const double* pos, const double* radius,
+                     int32_t* hash_index, uint32_t* cse, double* sorted) {
+    DevGeom g;
+    int rc = make_geom(gm, 0.0, &g);
+    if (rc) return rc;
+    if (g.n > 0 && (!pos || !radius)) return fail(PSIM_ERR_INPUT, "NULL positions or radii");
+    if ((rc = ensure_device())) return rc;
+    Workspace& w = g_ws;
+    std::lock_guard<std::mutex> lk(w.mu);
+    if ((rc = ws_begin(w))) return rc;
+    const size_t n = (size_t)g.n, nc = (size_t)g.ncell;
+    PSIM_CUDA(w.pos.ensure(24 * n));
+    PSIM_CUDA(w.radius.ensure(8 * n));
+    PSIM_CUDA(w.xyz.ensure(24 * n));
+    PSIM_CUDA(w.key.ensure(4 * n));
+    PSIM_CUDA(w.rank.ensure(4 * n));
+    PSIM_CUDA(w.tmp.ensure(4 * n));
+    PSIM_CUDA(w.perm.ensure(4 * n));
+    PSIM_CUDA(w.tag_in.ensure(4 * n));
+    PSIM_CUDA(w.tag_out.ensure(4 * n));
+    PSIM_CUDA(w.radius_out.ensure(8 * n));
+    PSIM_CUDA(w.cellid.ensure(4 * n));
+    PSIM_CUDA(w.count.ensure(4 * nc));
+    PSIM_CUDA(w.start.ensure(4 * nc));
+    PSIM_CUDA(w.scratch.ensure(4 * scan_scratch_ints(g.ncell)));
+    PSIM_CUDA(w.posd.ensure(32 * n));
+    PSIM_CUDA(w.posh.ensure(16 * n));
+    PSIM_CUDA(w.hash_index.ensure(8 * n));
+    PSIM_CUDA(w.cse.ensure(8 * nc));
+    PSIM_CUDA(w.sorted.ensure(32 * n));
+    PSIM_CUDA(w.err.ensure(4));
+    cudaStream_t st = w.st;
+    double* x = w.xyz.as<double>();
+    PSIM_CUDA(cudaMemcpyAsync(w.pos.p, pos, 24 * n, cudaMemcpyHostToDevice, st));
+    PSIM_CUDA(cudaMemcpyAsync(w.radius.p, radius, 8 * n, cudaMemcpyHostToDevice, st));
+    PSIM_CUDA(cudaMemsetAsync(w.count.p, 0, 4 * nc, st));
+    PSIM_CUDA(cudaMemsetAsync(w.err.p, 0, 4, st));
+    PSIM_CUDA(launch_split_xyz(g.n, w.pos.as<double>(), nullptr, 0, x, x + n, x + 2 * n, st));
+    PSIM_CUDA(launch_hash_count(g.n, x, x + n, x + 2 * n, g, w.key.as<int>(), w.rank.as<int>(),
+                                w.count.as<int>(), w.err.as<uint32_t>(), st));
+    PSIM_CUDA(launch_scan(w.count.as<int>(), w.start.as<int>(), g.ncell, w.scratch.as<int>(), st));
+    PSIM_CUDA(launch_scatter(g.n, w.key.as<int>(), w.rank.as<int>(), w.start.as<int>(),
+                             w.tmp.as<int>(), nullptr, st));
+    PSIM_CUDA(launch_fill_int_iota(g.n, w.tag_in.as<int>(), st));
+    CanonArgs ca{};
+    ca.n = g.n;
+    ca.tmp = w.tmp.as<int>();
+    ca.key = w.key.as<int>();
+    ca.start = w.start.as<int>();
+    ca.count = w.count.as<int>();
+    ca.tag_in = w.tag_in.as<int>();
+    ca.radius_in = w.radius.as<double>();
+    ca.x = x;
+    ca.y = x + n;
+    ca.z = x + 2 * n;
+    ca.perm = w.perm.as<int>();
+    ca.tag_out = w.tag_out.as<int>();
+    ca.radius_out = w.radius_out.as<double>();
+    ca.cellid = w.cellid.as<int>();
+    ca.posd = w.posd.as<double4_32a>();
+    ca.posh = w.posh.as<float4>();
+    PSIM_CUDA(launch_canonicalize(ca, st));
+    PSIM_CUDA(launch_export_cells(g.n, g.ncell, w.cellid.as<int>(), w.tag_out.as<int>(),
+                                  w.posd.as<double4_32a>(), w.start.as<int>(), w.count.as<int>(),
+                                  w.hash_index.as<int32_t>(), w.cse.as<uint32_t>(),
+                                  w.sorted.as<double>(), st));
+    uint32_t bits = 0;
+    PSIM_CUDA(cudaMemcpyAsync(&bits, w.err.p, 4, cudaMemcpyDeviceToHost, st));
+    if (hash_index)
+        PSIM_CUDA(cudaMemcpyAsync(hash_index, w.hash_index.p, 8 * n, cudaMemcpyDeviceToHost, st));
+    if (cse) PSIM_CUDA(cudaMemcpyAsync(cse, w.cse.p, 8 * nc, cudaMemcpyDeviceToHost, st));
+    if (sorted) PSIM_CUDA(cudaMemcpyAsync(sorted, w.sorted.p, 32 * n, cudaMemcpyDeviceToHost, st));
+    PSIM_CUDA(cudaStreamSynchronize(st));
+    if (bits) return fail(code_from_bits(bits), "%s", bits_text(bits));
+    return PSIM_OK;
+}
+
+// ----------------------------------------------------------- force drop-in
+
+int psim_force_evaluate(const psim_force_params* params, const psim_geometry* gm,
+                        int32_t precision, const double* sorted, const int32_t* hash_index,
+                        const uint32_t* cse, double* force) {
+    int rc = check_params(params);
+    if (rc) return rc;
+    DevGeom g;
+    if ((rc = make_geom(gm, max_cutoff(params), &g))) return rc;
+    if (precision != PSIM_PRECISION_FP64 && precision != PSIM_PRECISION_MIXED)
+        return fail(PSIM_ERR_INPUT, "unknown precision %d", precision);
+    if (g.n > 0 && (!sorted || !hash_index || !cse || !force))
+        return fail(PSIM_ERR_INPUT, "NULL array");
+    if ((rc = ensure_device())) return rc;
+    ForceSetup fs = make_setup(params, g.L);
+    Workspace& w = g_ws;
+    std::lock_guard<std::mutex> lk(w.mu);
+    if ((rc = ws_begin(w))) return rc;
+    const size_t n = (size_t)g.n, nc = (size_t)g.ncell;
+    PSIM_CUDA(w.sorted.ensure(32 * n));
+    PSIM_CUDA(w.hash_index.ensure(8 * n));
+    PSIM_CUDA(w.cse.ensure(8 * nc));
+    PSIM_CUDA(w.posd.ensure(32 * n));
+    PSIM_CUDA(w.posh.ensure(16 * n));
+    PSIM_CUDA(w.posl.ensure(16 * n));
+    PSIM_CUDA(w.cellid.ensure(4 * n));
+    PSIM_CUDA(w.tag_out.ensure(4 * n));
+    PSIM_CUDA(w.start.ensure(4 * nc));
+    PSIM_CUDA(w.count.ensure(4 * nc));
+    PSIM_CUDA(w.fxyz.ensure(24 * n));
+    PSIM_CUDA(w.force.ensure(24 * n));
+    PSIM_CUDA(w.err.ensure(4));
+    cudaStream_t st = w.st;
+    PSIM_CUDA(cudaMemcpyAsync(w.sorted.p, sorted, 32 * n, cudaMemcpyHostToDevice, st));
+    PSIM_CUDA(cudaMemcpyAsync(w.hash_index.p, hash_index, 8 * n, cudaMemcpyHostToDevice, st));
+    PSIM_CUDA(cudaMemcpyAsync(w.cse.p, cse, 8 * nc, cudaMemcpyHostToDevice, st));
+    PSIM_CUDA(cudaMemsetAsync(w.err.p, 0, 4, st));
+    PSIM_CUDA(launch_import_sorted(g.n, w.sorted.as<double>(), w.hash_index.as<int32_t>(), g,
+                                   w.posd.as<double4_32a>(), w.posh.as<float4>(),
+                                   w.posl.as<float4>(), w.cellid.as<int>(), w.tag_out.as<int>(),
+                                   w.err.as<uint32_t>(), st));
+    PSIM_CUDA(launch_import_cse(g.ncell, g.n, w.cse.as<uint32_t>(), w.start.as<int>(),
+                                w.count.as<int>(), w.err.as<uint32_t>(), st));
+    // a position outside the grid has no home cell: stop before the force pass
+    uint32_t bits = 0;
+    PSIM_CUDA(cudaMemcpyAsync(&bits, w.err.p, 4, cudaMemcpyDeviceToHost, st));
+    PSIM_CUDA(cudaStreamSynchronize(st));
+    if (bits) return fail(code_from_bits(bits), "%s", bits_text(bits));
+    double* f = w.fxyz.as<double>();
+    CellView cv{w.posd.as<double4_32a>(), w.posh.as<float4>(), w.posl.as<float4>(),
+                w.cellid.as<int>(), w.start.as<int>(), w.count.as<int>()};
+    ForceOut out{f, f + n, f + 2 * n, w.err.as<uint32_t>()};
+    if (precision == PSIM_PRECISION_FP64)
+        PSIM_CUDA(launch_forces_fp64(fs, g, cv, out, st));
+    else
+        PSIM_CUDA(launch_forces_mixed(fs, g, cv, out, st));
+    PSIM_CUDA(launch_unsort_force(g.n, w.tag_out.as<int>(), f, f + n, f + 2 * n,
+                                  w.force.as<double>(), st));
+    PSIM_CUDA(cudaMemcpyAsync(&bits, w.err.p, 4, cudaMemcpyDeviceToHost, st));
+    PSIM_CUDA(cudaMemcpyAsync(force, w.force.p, 24 * n, cudaMemcpyDeviceToHost, st));
+    PSIM_CUDA(cudaStreamSynchronize(st));
+    if (bits) return fail(code_from_bits(bits), "%s", bits_text(bits));
+    return PSIM_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------ integrator
+
+struct psim_integrator {
+    int device = 0;
+    int n = 0;
+    cudaStream_t st = nullptr;
+    VgbParams vp{};
+    int vel_counter = 0;
+    long long steps = 0;
+    DevBuf mem, mem_corr, pos, pos0, vel, frc, frc0, mass, noise, err;
+};
+
+extern "C" {
+
+psim_integrator* psim_integrator_create(const psim_integrator_config* cfg, int32_t n) {
+    if (n < 0) { fail(PSIM_ERR_INPUT, "negative particle count"); return nullptr; }
+    VgbParams vp;
+    if (make_vgb_params(cfg, &vp)) return nullptr;
+    if (ensure_device()) return nullptr;
+    psim_integrator* it = new psim_integrator();
+    it->n = n;
+    it->vp = vp;
+    cudaGetDevice(&it->device);
+    const size_t b = 24 * (size_t)n;
+    if (cudaStreamCreateWithFlags(&it->st, cudaStreamNonBlocking) != cudaSuccess ||
+        it->mem.ensure(b) || it->mem_corr.ensure(b) || it->pos.ensure(b) || it->pos0.ensure(b) ||
+        it->vel.ensure(b) || it->frc.ensure(b) || it->frc0.ensure(b) ||
+        it->mass.ensure(8 * (size_t)n) || it->err.ensure(4) ||
+        cudaMemset(it->mem.p, 0, b) || cudaMemset(it->mem_corr.p, 0, b)) {
+        fail(PSIM_ERR_CUDA, "integrator allocation failed: %s", cudaGetErrorString(cudaGetLastError()));
+        psim_integrator_destroy(it);
+        return nullptr;
+    }
+    return it;
+}
+
+void psim_integrator_destroy(psim_integrator* it) {
+    if (!it) return;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(it->device);
+    DevBuf* all[] = {&it->mem, &it->mem_corr, &it->pos, &it->pos0, &it->vel, &it->frc,
+                     &it->frc0, &it->mass, &it->noise, &it->err};
+    for (DevBuf* b : all) b->release();
+    if (it->st) cudaStreamDestroy(it->st);
+    cudaSetDevice(prev);
+    delete it;
+}
+
+int psim_integrator_next_system(psim_integrator* it, double current_time, double box,
+                                int32_t noise_mode, const double* noise,
+                                const double* particle_force, double* pos, double* pos0,
+                                double* vel, double* frc, double* frc0, const double* mass) {
+    if (!it) return fail(PSIM_ERR_INPUT, "NULL integrator");
+    if (!(box > 0.0)) return fail(PSIM_ERR_INPUT, "box size must be positive");
+    if (noise_mode == PSIM_NOISE_INJECTED && !noise && it->n > 0)
+        return fail(PSIM_ERR_INPUT, "injected noise mode needs a noise array");
+    if (it->n > 0 && (!pos || !pos0 || !vel || !frc || !frc0 || !mass))
+        return fail(PSIM_ERR_INPUT, "NULL particle array");
+    int prev = 0;
+    PSIM_CUDA(cudaGetDevice(&prev));
+    PSIM_CUDA(cudaSetDevice(it->device));
+    const size_t n = (size_t)it->n, b = 24 * n;
+    cudaStream_t st = it->st;
+    PSIM_CUDA(cudaMemcpyAsync(it->pos.p, pos, b, cudaMemcpyHostToDevice, st));
+    PSIM_CUDA(cudaMemcpyAsync(it->pos0.p, pos0, b, cudaMemcpyHostToDevice, st));
+    PSIM_CUDA(cudaMemcpyAsync(it->vel.p, vel, b, cudaMemcpyHostToDevice, st));
+    if (particle_force) {  // pushParticleForce: frc0 <- frc, frc <- particleForce
+        PSIM_CUDA(cudaMemcpyAsync(it->frc0.p, frc, b, cudaMemcpyHostToDevice, st));
+        PSIM_CUDA(cudaMemcpyAsync(it->frc.p, particle_force, b, cudaMemcpyHostToDevice, st));
+    } else {
+        PSIM_CUDA(cudaMemcpyAsync(it->frc.p, frc, b, cudaMemcpyHostToDevice, st));
+        PSIM_CUDA(cudaMemcpyAsync(it->frc0.p, frc0, b, cudaMemcpyHostToDevice, st));
+    }
+    PSIM_CUDA(cudaMemcpyAsync(it->mass.p, mass, 8 * n, cudaMemcpyHostToDevice, st));
+    const double* dnoise = nullptr;
+    if (noise_mode == PSIM_NOISE_INJECTED) {
+        PSIM_CUDA(it->noise.ensure(48 * n));
+        PSIM_CUDA(cudaMemcpyAsync(it->noise.p, noise, 48 * n, cudaMemcpyHostToDevice, st));
+        dnoise = it->noise.as<double>();
+    }
+    PSIM_CUDA(cudaMemsetAsync(it->err.p, 0, 4, st));
+    const bool first = (current_time == 0);  // nextSystem, brownianIntegrator.cpp:183
+    VgbAosArgs a{};
+    a.n = it->n;
+    a.first = first ? 1 : 0;
+    a.vel_step = (!first && (it->vp.vel_freq == 0 || it->vel_counter == it->vp.vel_freq)) ? 1 : 0;
+    a.pos = it->pos.as<double>();
+    a.pos0 = it->pos0.as<double>();
+    a.vel = it->vel.as<double>();
+    a.frc = it->frc.as<double>();
+    a.frc0 = it->frc0.as<double>();
+    a.mass = it->mass.as<double>();
+    a.mem = it->mem.as<double>();
+    a.mem_corr = it->mem_corr.as<double>();
+    a.noise = dnoise;
+    a.seed = it->vp.seed;
+    a.philox_step = it->steps;
+    a.err = it->err.as<uint32_t>();
+    PSIM_CUDA(launch_vgb_aos(a, it->vp, box, st));
+    uint32_t bits = 0;
+    PSIM_CUDA(cudaMemcpyAsync(&bits, it->err.p, 4, cudaMemcpyDeviceToHost, st));
+    PSIM_CUDA(cudaMemcpyAsync(pos, it->pos.p, b, cudaMemcpyDeviceToHost, st));
+    PSIM_CUDA(cudaMemcpyAsync(pos0, it->pos0.p, b, cudaMemcpyDeviceToHost, st));
+    PSIM_CUDA(cudaMemcpyAsync(vel, it->vel.p, b, cudaMemcpyDeviceToHost, st));
+    if (particle_force) {
+        PSIM_CUDA(cudaMemcpyAsync(frc0, it->frc0.p, b, cudaMemcpyDeviceToHost, st));
+        PSIM_CUDA(cudaMemcpyAsync(frc, it->frc.p, b, cudaMemcpyDeviceToHost, st));
+    }
+    PSIM_CUDA(cudaStreamSynchronize(st));
+    if (!first)  // brownianIntegrator.cpp:291-292
+        it->vel_counter = (it->vel_counter == it->vp.vel_freq) ? 0 : it->vel_counter + 1;
+    it->steps++;
+    cudaSetDevice(prev);
+    if (bits) return fail(code_from_bits(bits), "%s", bits_text(bits));
+    return PSIM_OK;
+}
+
+}  // extern "C"
+
+// ================================================================ system
+
+struct psim_system {
+    psim_system_config cfg{};
+    int device = 0;
+    cudaStream_t st = nullptr, side = nullptr;
+    cudaEvent_t ev_snap_ready = nullptr, ev_snap_done = nullptr;
+    cudaEvent_t ev[5] = {};
+    DevGeom g{};
+    ForceSetup fs{};
+    VgbParams vp{};
+    int n = 0, ncell = 0;
+    // storage-order state (ping-pong) and order-dependent arrays
+    DevBuf pos[2], pos0[2], mem[2], frc[3], tag[2], radius[2], inv_mass[2], perm[2], count[2];
+    DevBuf cellid, key, rank, tmp, start, scratch, posd, posh, posl, vel, err, state, occ, noise,
+        snap;
+    long long noise_first = 0, noise_steps = 0;
+    long long total = 0;      // steps since upload, as the host has enqueued them
+    bool uploaded = false;
+    bool snap_pending = false;
+    cudaGraphExec_t graph[6] = {};
+    uint32_t latched = 0;
+};
+
+namespace {
+
+struct Phase {
+    int sb, ob, cb, pb, fprev, fcur;
+};
+
+// Buffer roles after `t` steps (t = 0: just uploaded).  Period 6: the
+// ping-pong pairs flip every step, the three force buffers rotate.
+Phase phase_of(long long t) {
+    Phase p;
+    const int par = (int)(t & 1);
+    p.sb = par;
+    p.ob = par;
+    p.cb = par;
+    p.pb = par;
+    p.fprev = (int)(t % 3);
+    p.fcur = (p.fprev + 1) % 3;
+    return p;
+}
+
+double* d3(DevBuf& b, int n, int k) { return b.as<double>() + (size_t)k * n; }
+
+int enqueue_step(psim_system* s, long long t, cudaEvent_t* evs) {
+    const Phase ph = phase_of(t);
+    const int n = s->n;
+    cudaStream_t st = s->st;
+    const int sb = ph.sb, nsb = 1 - ph.sb, ob = ph.ob, nob = 1 - ph.ob, cb = ph.cb, ncb = 1 - ph.cb;
+    const int pb = ph.pb, npb = 1 - ph.pb;
+    if (evs) PSIM_CUDA(cudaEventRecord(evs[0], st));
+    // forces on the current cell order
+    CellView cv{s->posd.as<double4_32a>(), s->posh.as<float4>(), s->posl.as<float4>(),
+                s->cellid.as<int>(), s->start.as<int>(), s->count[cb].as<int>()};
+    ForceOut fo{d3(s->frc[ph.fcur], n, 0), d3(s->frc[ph.fcur], n, 1), d3(s->frc[ph.fcur], n, 2),
+                s->err.as<uint32_t>()};
+    if (s->cfg.precision == PSIM_PRECISION_FP64)
+        PSIM_CUDA(launch_forces_fp64(s->fs, s->g, cv, fo, st));
+    else
+        PSIM_CUDA(launch_forces_mixed(s->fs, s->g, cv, fo, st));
+    if (evs) PSIM_CUDA(cudaEventRecord(evs[1], st));
+    // integrator: pushParticleForce + nextSystem, hash + count into the next grid
+    PSIM_CUDA(cudaMemsetAsync(s->count[ncb].p, 0, 4 * (size_t)s->ncell, st));
+    VgbSystemArgs a{};
+    a.n = n;
+    a.perm = s->perm[pb].as<int>();
+    a.tag = s->tag[ob].as<int>();
+    a.inv_mass = s->inv_mass[ob].as<double>();
+    a.x = d3(s->pos[sb], n, 0); a.y = d3(s->pos[sb], n, 1); a.z = d3(s->pos[sb], n, 2);
+    a.x0 = d3(s->pos0[sb], n, 0); a.y0 = d3(s->pos0[sb], n, 1); a.z0 = d3(s->pos0[sb], n, 2);
+    a.mx = d3(s->mem[sb], n, 0); a.my = d3(s->mem[sb], n, 1); a.mz = d3(s->mem[sb], n, 2);
+    a.fx = fo.fx; a.fy = fo.fy; a.fz = fo.fz;
+    a.gx = d3(s->frc[ph.fprev], n, 0); a.gy = d3(s->frc[ph.fprev], n, 1);
+    a.gz = d3(s->frc[ph.fprev], n, 2);
+    a.vel = s->vel.as<double>();
+    a.ox = d3(s->pos[nsb], n, 0); a.oy = d3(s->pos[nsb], n, 1); a.oz = d3(s->pos[nsb], n, 2);
+    a.ox0 = d3(s->pos0[nsb], n, 0); a.oy0 = d3(s->pos0[nsb], n, 1); a.oz0 = d3(s->pos0[nsb], n, 2);
+    a.omx = d3(s->mem[nsb], n, 0); a.omy = d3(s->mem[nsb], n, 1); a.omz = d3(s->mem[nsb], n, 2);
+    a.key = s->key.as<int>();
+    a.rank = s->rank.as<int>();
+    a.count = s->count[ncb].as<int>();
+    a.err = s->err.as<uint32_t>();
+    a.state = s->state.as<StepState>();
+    NoiseView nz{s->cfg.noise_mode, s->noise.as<double>(), s->noise_first, s->noise_steps};
+    PSIM_CUDA(launch_vgb_system(a, s->vp, s->g, nz, st));
+    if (evs) PSIM_CUDA(cudaEventRecord(evs[2], st));
+    // rebuild: scan, scatter, canonicalise into the next order
+    PSIM_CUDA(launch_scan(s->count[ncb].as<int>(), s->start.as<int>(), s->ncell,
+                          s->scratch.as<int>(), st));
+    PSIM_CUDA(launch_scatter(n, s->key.as<int>(), s->rank.as<int>(), s->start.as<int>(),
+                             s->tmp.as<int>(), s->err.as<uint32_t>(), st));
+    CanonArgs ca{};
+    ca.n = n;
+    ca.tmp = s->tmp.as<int>();
+    ca.key = s->key.as<int>();
+    ca.start = s->start.as<int>();
+    ca.count = s->count[ncb].as<int>();
+    ca.tag_in = s->tag[ob].as<int>();
+    ca.radius_in = s->radius[ob].as<double>();
+    ca.inv_mass_in = s->inv_mass[ob].as<double>();
+    ca.x = a.ox; ca.y = a.oy; ca.z = a.oz;
+    ca.perm = s->perm[npb].as<int>();
+    ca.tag_out = s->tag[nob].as<int>();
+    ca.radius_out = s->radius[nob].as<double>();
+    ca.inv_mass_out = s->inv_mass[nob].as<double>();
+    ca.cellid = s->cellid.as<int>();
+    ca.posd = s->cfg.precision == PSIM_PRECISION_FP64 ? s->posd.as<double4_32a>() : nullptr;
+    ca.posh = s->posh.as<float4>();
+    ca.posl = s->cfg.precision == PSIM_PRECISION_MIXED ? s->posl.as<float4>() : nullptr;
+    ca.state = s->state.as<StepState>();
+    ca.advance = 1;
+    ca.vel_freq = s->vp.vel_freq;
+    ca.err = s->err.as<uint32_t>();
+    PSIM_CUDA(launch_canonicalize(ca, st));
+    if (evs) PSIM_CUDA(cudaEventRecord(evs[3], st));
+    return PSIM_OK;
+}
+
+int graph_for(psim_system* s, int phase, cudaGraphExec_t* out) {
+    if (s->graph[phase]) { *out = s->graph[phase]; return PSIM_OK; }
+    cudaGraph_t g = nullptr;
+    PSIM_CUDA(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal));
+    int rc = enqueue_step(s, phase, nullptr);
+    cudaError_t e = cudaStreamEndCapture(s->st, &g);
+    if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+    if (e != cudaSuccess) return fail(PSIM_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&s->graph[phase], g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(PSIM_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+    *out = s->graph[phase];
+    return PSIM_OK;
+}
+
+void drop_graphs(psim_system* s) {
+    for (auto& g : s->graph)
+        if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+}
+
+struct DeviceGuard {
+    int prev = 0;
+    explicit DeviceGuard(int d) { cudaGetDevice(&prev); cudaSetDevice(d); }
+    ~DeviceGuard() { cudaSetDevice(prev); }
+};
+
+// Waits for the stream, reads the error word and the device step counter,
+// and re-aligns the host's step count with the steps the device completed.
+int settle(psim_system* s) {
+    PSIM_CUDA(cudaStreamSynchronize(s->st));
+    uint32_t bits = 0;
+    StepState ss{};
+    PSIM_CUDA(cudaMemcpy(&bits, s->err.p, 4, cudaMemcpyDeviceToHost));
+    PSIM_CUDA(cudaMemcpy(&ss, s->state.p, sizeof ss, cudaMemcpyDeviceToHost));
+    s->total = ss.step;
+    if (bits) {
+        s->latched = bits;
+        return fail(code_from_bits(bits), "step %lld: %s", ss.step, bits_text(bits));
+    }
+    return PSIM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+psim_system* psim_system_create(const psim_system_config* cfg) {
+    if (!cfg) { fail(PSIM_ERR_INPUT, "NULL config"); return nullptr; }
+    if (check_params(&cfg->force)) return nullptr;
+    if (cfg->precision != PSIM_PRECISION_FP64 && cfg->precision != PSIM_PRECISION_MIXED) {
+        fail(PSIM_ERR_INPUT, "unknown precision %d", cfg->precision);
+        return nullptr;
+    }
+    if (cfg->noise_mode != PSIM_NOISE_PHILOX && cfg->noise_mode != PSIM_NOISE_INJECTED) {
+        fail(PSIM_ERR_INPUT, "unknown noise mode %d", cfg->noise_mode);
+        return nullptr;
+    }
+    DevGeom g;
+    if (make_geom(&cfg->geom, max_cutoff(&cfg->force), &g)) return nullptr;
+    VgbParams vp;
+    if (make_vgb_params(&cfg->integ, &vp)) return nullptr;
+    if (ensure_device()) return nullptr;
+    int ndev = 0;
+    cudaGetDeviceCount(&ndev);
+    if (cfg->device < 0 || cfg->device >= ndev) {
+        fail(PSIM_ERR_INPUT, "device %d out of range", cfg->device);
+        return nullptr;
+    }
+    DeviceGuard dg(cfg->device);
+    psim_system* s = new psim_system();
+    s->cfg = *cfg;
+    s->device = cfg->device;
+    s->g = g;
+    s->vp = vp;
+    s->fs = make_setup(&cfg->force, g.L);
+    s->n = g.n;
+    s->ncell = g.ncell;
+    const size_t n = (size_t)g.n, nc = (size_t)g.ncell;
+    bool ok = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaEventCreateWithFlags(&s->ev_snap_ready, cudaEventDisableTiming) == cudaSuccess &&
+              cudaEventCreateWithFlags(&s->ev_snap_done, cudaEventDisableTiming) == cudaSuccess;
+    for (auto& e : s->ev) ok = ok && cudaEventCreate(&e) == cudaSuccess;
+    for (int k = 0; k < 2 && ok; ++k) {
+        ok = !s->pos[k].ensure(24 * n) && !s->pos0[k].ensure(24 * n) && !s->mem[k].ensure(24 * n) &&
+             !s->tag[k].ensure(4 * n) && !s->radius[k].ensure(8 * n) &&
+             !s->inv_mass[k].ensure(8 * n) && !s->perm[k].ensure(4 * n) &&
+             !s->count[k].ensure(4 * nc);
+    }
+    for (int k = 0; k < 3 && ok; ++k) ok = !s->frc[k].ensure(24 * n);
+    ok = ok && !s->cellid.ensure(4 * n) && !s->key.ensure(4 * n) && !s->rank.ensure(4 * n) &&
+         !s->tmp.ensure(4 * n) && !s->start.ensure(4 * nc) &&
+         !s->scratch.ensure(4 * scan_scratch_ints(g.ncell)) && !s->posh.ensure(16 * n) &&
+         !s->vel.ensure(24 * n) && !s->err.ensure(4) && !s->state.ensure(sizeof(StepState)) &&
+         !s->occ.ensure(4);
+    if (ok && cfg->precision == PSIM_PRECISION_FP64) ok = !s->posd.ensure(32 * n);
+    if (ok && cfg->precision == PSIM_PRECISION_MIXED) ok = !s->posl.ensure(16 * n);
+    if (ok) ok = cudaMemset(s->err.p, 0, 4) == cudaSuccess &&
+                 cudaMemset(s->state.p, 0, sizeof(StepState)) == cudaSuccess;
+    if (!ok) {
+        fail(PSIM_ERR_CUDA, "system allocation failed: %s", cudaGetErrorString(cudaGetLastError()));
+        psim_system_destroy(s);
+        return nullptr;
+    }
+    return s;
+}
+
+void psim_system_destroy(psim_system* s) {
+    if (!s) return;
+    DeviceGuard dg(s->device);
+    if (s->st) cudaStreamSynchronize(s->st);
+    if (s->side) cudaStreamSynchronize(s->side);
+    drop_graphs(s);
+    DevBuf* arrs[] = {&s->cellid, &s->key, &s->rank, &s->tmp, &s->start, &s->scratch, &s->posd,
+                      &s->posh, &s->posl, &s->vel, &s->err, &s->state, &s->occ, &s->noise,
+                      &s->snap};
+    for (DevBuf* b : arrs) b->release();
+    for (int k = 0; k < 2; ++k) {
+        s->pos[k].release(); s->pos0[k].release(); s->mem[k].release(); s->tag[k].release();
+        s->radius[k].release(); s->inv_mass[k].release(); s->perm[k].release();
+        s->count[k].release();
+    }
+    for (int k = 0; k < 3; ++k) s->frc[k].release();
+    for (auto& e : s->ev) if (e) cudaEventDestroy(e);
+    if (s->ev_snap_ready) cudaEventDestroy(s->ev_snap_ready);
+    if (s->ev_snap_done) cudaEventDestroy(s->ev_snap_done);
+    if (s->st) cudaStreamDestroy(s->st);
+    if (s->side) cudaStreamDestroy(s->side);
+    delete s;
+}
+
+int psim_system_upload(psim_system* s, const double* pos, const double* pos0, const double* vel,
+                       const double* frc, const double* frc0, const double* radius,
+                       const double* mass) {
+    if (!s) return fail(PSIM_ERR_INPUT, "NULL system");
+    if (s->n > 0 && (!pos || !radius)) return fail(PSIM_ERR_INPUT, "positions and radii are required");
+    DeviceGuard dg(s->device);
+    const int n = s->n;
+    const size_t b = 24 * (size_t)n;
+    cudaStream_t st = s->st;
+    PSIM_CUDA(cudaStreamSynchronize(st));
+    // the upload is "after step -1": storage order = original order
+    const Phase ph = phase_of(0);
+    const int sb = ph.sb, ob = ph.ob, pb = ph.pb;
+    ScopedBuf stage;
+    PSIM_CUDA(stage.ensure(b));
+    auto load3 = [&](const double* src, DevBuf& dst) -> int {
+        if (src) {
+            PSIM_CUDA(cudaMemcpyAsync(stage.p, src, b, cudaMemcpyHostToDevice, st));
+            PSIM_CUDA(launch_split_xyz(n, stage.as<double>(), nullptr, 0, d3(dst, n, 0),
+                                       d3(dst, n, 1), d3(dst, n, 2), st));
+        } else {
+            PSIM_CUDA(cudaMemsetAsync(dst.p, 0, b, st));
+        }
+        return PSIM_OK;
+    };
+    int rc;
+    if ((rc = load3(pos, s->pos[sb]))) return rc;
+    if ((rc = load3(pos0 ? pos0 : pos, s->pos0[sb]))) return rc;
+    PSIM_CUDA(cudaMemsetAsync(s->mem[sb].p, 0, b, st));
+    if ((rc = load3(frc, s->frc[ph.fprev]))) return rc;
+    if ((rc = load3(frc0, s->frc[(ph.fprev + 2) % 3]))) return rc;
+    if (vel) PSIM_CUDA(cudaMemcpyAsync(s->vel.p, vel, b, cudaMemcpyHostToDevice, st));
+    else PSIM_CUDA(cudaMemsetAsync(s->vel.p, 0, b, st));
+    // original-order tags, radii and 1/m of "order -1"
+    std::vector<double> inv((size_t)n, 1.0);
+    if (mass)
+        for (int i = 0; i < n; ++i) inv[i] = 1.0 / mass[i];
+    PSIM_CUDA(cudaMemcpyAsync(s->radius[1 - ob].p, radius, 8 * (size_t)n, cudaMemcpyHostToDevice, st));
+    PSIM_CUDA(cudaMemcpyAsync(s->inv_mass[1 - ob].p, inv.data(), 8 * (size_t)n,
+                              cudaMemcpyHostToDevice, st));
+    PSIM_CUDA(launch_fill_int_iota(n, s->tag[1 - ob].as<int>(), st));
+    PSIM_CUDA(launch_fill_int_iota(n, s->perm[1 - pb].as<int>(), st));
+    PSIM_CUDA(cudaMemsetAsync(s->err.p, 0, 4, st));
+    PSIM_CUDA(cudaMemsetAsync(s->state.p, 0, sizeof(StepState), st));
+    // first cell list (system.cpp:101-103)
+    PSIM_CUDA(cudaMemsetAsync(s->count[ph.cb].p, 0, 4 * (size_t)s->ncell, st));
+    PSIM_CUDA(launch_hash_count(n, d3(s->pos[sb], n, 0), d3(s->pos[sb], n, 1),
+                                d3(s->pos[sb], n, 2), s->g, s->key.as<int>(), s->rank.as<int>(),
+                                s->count[ph.cb].as<int>(), s->err.as<uint32_t>(), st));
+    PSIM_CUDA(launch_scan(s->count[ph.cb].as<int>(), s->start.as<int>(), s->ncell,
+                          s->scratch.as<int>(), st));
+    PSIM_CUDA(launch_scatter(n, s->key.as<int>(), s->rank.as<int>(), s->start.as<int>(),
+                             s->tmp.as<int>(), nullptr, st));
+    CanonArgs ca{};
+    ca.n = n;
+    ca.tmp = s->tmp.as<int>();
+    ca.key = s->key.as<int>();
+    ca.start = s->start.as<int>();
+    ca.count = s->count[ph.cb].as<int>();
+    ca.tag_in = s->tag[1 - ob].as<int>();
+    ca.radius_in = s->radius[1 - ob].as<double>();
+    ca.inv_mass_in = s->inv_mass[1 - ob].as<double>();
+    ca.x = d3(s->pos[sb], n, 0); ca.y = d3(s->pos[sb], n, 1); ca.z = d3(s->pos[sb], n, 2);
+    ca.perm = s->perm[pb].as<int>();
+    ca.tag_out = s->tag[ob].as<int>();
+    ca.radius_out = s->radius[ob].as<double>();
+    ca.inv_mass_out = s->inv_mass[ob].as<double>();
+    ca.cellid = s->cellid.as<int>();
+    ca.posd = s->cfg.precision == PSIM_PRECISION_FP64 ? s->posd.as<double4_32a>() : nullptr;
+    ca.posh = s->posh.as<float4>();
+    ca.posl = s->cfg.precision == PSIM_PRECISION_MIXED ? s->posl.as<float4>() : nullptr;
+    PSIM_CUDA(launch_canonicalize(ca, st));
+    uint32_t bits = 0;
+    PSIM_CUDA(cudaMemcpyAsync(&bits, s->err.p, 4, cudaMemcpyDeviceToHost, st));
+    PSIM_CUDA(cudaStreamSynchronize(st));
+    stage.release();
+    s->total = 0;
+    s->latched = 0;
+    s->uploaded = true;
+    if (bits) {
+        s->latched = bits;
+        return fail(code_from_bits(bits), "upload: %s", bits_text(bits));
+    }
+    return PSIM_OK;
+}
+
+int psim_system_set_noise(psim_system* s, const double* noise, int32_t n_steps, int32_t first) {
+    if (!s) return fail(PSIM_ERR_INPUT, "NULL system");
+    if (n_steps < 0 || first < 0) return fail(PSIM_ERR_INPUT, "negative noise range");
+    if (n_steps > 0 && !noise) return fail(PSIM_ERR_INPUT, "NULL noise");
+    DeviceGuard dg(s->device);
+    PSIM_CUDA(cudaStreamSynchronize(s->st));
+    const size_t b = (size_t)n_steps * (size_t)s->n * 6 * sizeof(double);
+    void* old = s->noise.p;
+    PSIM_CUDA(s->noise.ensure(b));
+    if (s->noise.p != old) drop_graphs(s);  // graphs hold the buffer address
+    if (b) PSIM_CUDA(cudaMemcpy(s->noise.p, noise, b, cudaMemcpyHostToDevice));
+    if (s->noise_first != first || s->noise_steps != n_steps) drop_graphs(s);
+    s->noise_first = first;
+    s->noise_steps = n_steps;
+    return PSIM_OK;
+}
+
+int psim_system_step_async(psim_system* s, int32_t n_steps) {
+    if (!s) return fail(PSIM_ERR_INPUT, "NULL system");
+    if (!s->uploaded) return fail(PSIM_ERR_INPUT, "no state uploaded");
+    if (s->latched) return fail(code_from_bits(s->latched), "%s", bits_text(s->latched));
+    if (n_steps < 0) return fail(PSIM_ERR_INPUT, "negative step count");
+    DeviceGuard dg(s->device);
+    for (int ph = 0; ph < 6 && n_steps > 0; ++ph) {  // capture before anything is in flight
+        cudaGraphExec_t ge;
+        if (!s->graph[ph]) {
+            PSIM_CUDA(cudaStreamSynchronize(s->st));
+            int rc = graph_for(s, ph, &ge);
+            if (rc) return rc;
+        }
+    }
+    for (int k = 0; k < n_steps; ++k) {
+        cudaGraphExec_t ge;
+        int rc = graph_for(s, (int)(s->total % 6), &ge);
+        if (rc) return rc;
+        PSIM_CUDA(cudaGraphLaunch(ge, s->st));
+        s->total++;
+    }
+    return PSIM_OK;
+}
+
+int psim_system_sync(psim_system* s) {
+    if (!s) return fail(PSIM_ERR_INPUT, "NULL system");
+    DeviceGuard dg(s->device);
+    return settle(s);
+}
+
+int psim_system_step(psim_system* s, int32_t n_steps) {
+    int rc = psim_system_step_async(s, n_steps);
+    if (rc) return rc;
+    return psim_system_sync(s);
+}
+
+int psim_system_download(psim_system* s, double* pos, double* pos0, double* vel, double* frc,
+                         double* frc0) {
+    if (!s) return fail(PSIM_ERR_INPUT, "NULL system");
+    if (!s->uploaded) return fail(PSIM_ERR_INPUT, "no state uploaded");
+    DeviceGuard dg(s->device);
+    int rc = settle(s);
+    if (rc && rc != code_from_bits(s->latched)) return rc;
+    const Phase ph = phase_of(s->total);
+    const int n = s->n;
+    const size_t b = 24 * (size_t)n;
+    cudaStream_t st = s->st;
+    // storage order is the previous cell order: its tags are tag[1 - ob]
+    const int* tg = s->tag[1 - ph.ob].as<int>();
+    ScopedBuf stage;
+    PSIM_CUDA(stage.ensure(b));
+    auto get3 = [&](DevBuf& src, const int* perm, double* dst) -> int {
+        if (!dst) return PSIM_OK;
+        PSIM_CUDA(launch_merge_xyz(n, d3(src, n, 0), d3(src, n, 1), d3(src, n, 2), tg, perm,
+                                   stage.as<double>(), st));
+        PSIM_CUDA(cudaMemcpyAsync(dst, stage.p, b, cudaMemcpyDeviceToHost, st));
+        PSIM_CUDA(cudaStreamSynchronize(st));
+        return PSIM_OK;
+    };
+    if ((rc = get3(s->pos[ph.sb], nullptr, pos))) return rc;
+    if ((rc = get3(s->pos0[ph.sb], nullptr, pos0))) return rc;
+    if ((rc = get3(s->frc[ph.fprev], nullptr, frc))) return rc;
+    // frc0 is the force of two orders back, reached through the previous permutation
+    if ((rc = get3(s->frc[(ph.fprev + 2) % 3], s->perm[1 - ph.pb].as<int>(), frc0))) return rc;
+    if (vel) {
+        PSIM_CUDA(cudaMemcpyAsync(vel, s->vel.p, b, cudaMemcpyDeviceToHost, st));
+        PSIM_CUDA(cudaStreamSynchronize(st));
+    }
+    stage.release();
+    return s->latched ? code_from_bits(s->latched) : PSIM_OK;
+}
+
+int psim_system_download_cells(psim_system* s, int32_t* hash_index, uint32_t* cse,
+                               double* sorted) {
+    if (!s) return fail(PSIM_ERR_INPUT, "NULL system");
+    if (!s->uploaded) return fail(PSIM_ERR_INPUT, "no state uploaded");
+    DeviceGuard dg(s->device);
+    int rc = settle(s);
+    if (rc && rc != code_from_bits(s->latched)) return rc;
+    const Phase ph = phase_of(s->total);
+    const int n = s->n;
+    cudaStream_t st = s->st;
+    ScopedBuf hb, cb, sb, pd;
+    PSIM_CUDA(hb.ensure(8 * (size_t)n));
+    PSIM_CUDA(cb.ensure(8 * (size_t)s->ncell));
+    PSIM_CUDA(sb.ensure(32 * (size_t)n));
+    const double4_32a* posd = s->posd.as<double4_32a>();
+    if (s->cfg.precision != PSIM_PRECISION_FP64) {
+        // the mixed form keeps no FP64 sorted copy: gather one from the storage order
+        PSIM_CUDA(pd.ensure(32 * (size_t)n));
+        PSIM_CUDA(launch_gather_posd(n, s->perm[ph.pb].as<int>(), d3(s->pos[ph.sb], n, 0),
+                                     d3(s->pos[ph.sb], n, 1), d3(s->pos[ph.sb], n, 2),
+                                     s->radius[ph.ob].as<double>(), pd.as<double4_32a>(), st));
+        posd = pd.as<double4_32a>();
+    }
+    PSIM_CUDA(launch_export_cells(n, s->ncell, s->cellid.as<int>(), s->tag[ph.ob].as<int>(), posd,
+                                  s->start.as<int>(), s->count[ph.cb].as<int>(),
+                                  hb.as<int32_t>(), cb.as<uint32_t>(), sb.as<double>(), st));
+    if (hash_index)
+        PSIM_CUDA(cudaMemcpyAsync(hash_index, hb.p, 8 * (size_t)n, cudaMemcpyDeviceToHost, st));
+    if (cse) PSIM_CUDA(cudaMemcpyAsync(cse, cb.p, 8 * (size_t)s->ncell, cudaMemcpyDeviceToHost, st));
+    if (sorted) PSIM_CUDA(cudaMemcpyAsync(sorted, sb.p, 32 * (size_t)n, cudaMemcpyDeviceToHost, st));
+    PSIM_CUDA(cudaStreamSynchronize(st));
+    return PSIM_OK;
+}
+
+int psim_system_snapshot_async(psim_system* s, double* host_pos) {
+    if (!s || !host_pos) return fail(PSIM_ERR_INPUT, "NULL argument");
+    if (!s->uploaded) return fail(PSIM_ERR_INPUT, "no state uploaded");
+    DeviceGuard dg(s->device);
+    const int n = s->n;
+    const size_t b = 24 * (size_t)n;
+    PSIM_CUDA(s->snap.ensure(b));
+    const Phase ph = phase_of(s->total);
+    // the previous snapshot's copy must have left the staging buffer
+    if (s->snap_pending) PSIM_CUDA(cudaStreamWaitEvent(s->st, s->ev_snap_done, 0));
+    PSIM_CUDA(launch_merge_xyz(n, d3(s->pos[ph.sb], n, 0), d3(s->pos[ph.sb], n, 1),
+                               d3(s->pos[ph.sb], n, 2), s->tag[1 - ph.ob].as<int>(), nullptr,
+                               s->snap.as<double>(), s->st));
+    PSIM_CUDA(cudaEventRecord(s->ev_snap_ready, s->st));
+    PSIM_CUDA(cudaStreamWaitEvent(s->side, s->ev_snap_ready, 0));
+    PSIM_CUDA(cudaMemcpyAsync(host_pos, s->snap.p, b, cudaMemcpyDeviceToHost, s->side));
+    PSIM_CUDA(cudaEventRecord(s->ev_snap_done, s->side));
+    s->snap_pending = true;
+    return PSIM_OK;
+}
+
+int psim_system_snapshot_wait(psim_system* s) {
+    if (!s) return fail(PSIM_ERR_INPUT, "NULL system");
+    DeviceGuard dg(s->device);
+    if (s->snap_pending) PSIM_CUDA(cudaEventSynchronize(s->ev_snap_done));
+    s->snap_pending = false;
+    return PSIM_OK;
+}
+
+int psim_system_get_step(psim_system* s, int64_t* step, int32_t* vel_counter) {
+    if (!s) return fail(PSIM_ERR_INPUT, "NULL system");
+    DeviceGuard dg(s->device);
+    PSIM_CUDA(cudaStreamSynchronize(s->st));
+    StepState ss{};
+    PSIM_CUDA(cudaMemcpy(&ss, s->state.p, sizeof ss, cudaMemcpyDeviceToHost));
+    if (step) *step = ss.step;
+    if (vel_counter) *vel_counter = ss.vel_counter;
+    return PSIM_OK;
+}
+
+void* psim_system_stream(psim_system* s) { return s ? (void*)s->st : nullptr; }
+
+int psim_system_profile(psim_system* s, int32_t n_steps, double* out_ms) {
+    if (!s || !out_ms) return fail(PSIM_ERR_INPUT, "NULL argument");
+    if (!s->uploaded) return fail(PSIM_ERR_INPUT, "no state uploaded");
+    DeviceGuard dg(s->device);
+    double acc[4] = {0, 0, 0, 0};
+    for (int k = 0; k < n_steps; ++k) {
+        int rc = enqueue_step(s, s->total, s->ev);
+        if (rc) return rc;
+        s->total++;
+        PSIM_CUDA(cudaEventSynchronize(s->ev[3]));
+        float a = 0, b = 0, c = 0;
+        PSIM_CUDA(cudaEventElapsedTime(&a, s->ev[0], s->ev[1]));
+        PSIM_CUDA(cudaEventElapsedTime(&b, s->ev[1], s->ev[2]));
+        PSIM_CUDA(cudaEventElapsedTime(&c, s->ev[2], s->ev[3]));
+        acc[0] += a; acc[1] += b; acc[2] += c; acc[3] += a + b + c;
+    }
+    for (int k = 0; k < 4; ++k) out_ms[k] = n_steps > 0 ? acc[k] / n_steps : 0.0;
+    return settle(s);
+}
+
+int psim_system_launches_per_step(psim_system* s) {
+    (void)s;
+    return 7;  // force, vGB, scan x3, scatter, canonicalise (+1 memset node)
+}
+
+int psim_system_cell_occupancy(psim_system* s, int32_t* max_occ, double* mean_occ) {
+    if (!s) return fail(PSIM_ERR_INPUT, "NULL system");
+    DeviceGuard dg(s->device);
+    int rc = settle(s);
+    if (rc && rc != code_from_bits(s->latched)) return rc;
+    const Phase ph = phase_of(s->total);
+    PSIM_CUDA(cudaMemsetAsync(s->occ.p, 0, 4, s->st));
+    PSIM_CUDA(launch_occupancy(s->ncell, s->count[ph.cb].as<int>(), s->occ.as<int>(), s->st));
+    int mx = 0;
+    PSIM_CUDA(cudaMemcpyAsync(&mx, s->occ.p, 4, cudaMemcpyDeviceToHost, s->st));
+    PSIM_CUDA(cudaStreamSynchronize(s->st));
+    if (max_occ) *max_occ = mx;
+    if (mean_occ) *mean_occ = s->ncell ? (double)s->n / s->ncell : 0.0;
+    return PSIM_OK;
+}
+
+int psim_system_time_steps(psim_system* s, int32_t n_steps, double* ms) {
+    if (!s || !ms) return fail(PSIM_ERR_INPUT, "NULL argument");
+    DeviceGuard dg(s->device);
+    // capture the graphs first so the timed region holds only launches
+    int rc = psim_system_step_async(s, 0);
+    if (rc) return rc;
+    for (int ph = 0; ph < 6; ++ph) {
+        cudaGraphExec_t ge;
+        if (!s->graph[ph]) {
+            PSIM_CUDA(cudaStreamSynchronize(s->st));
+            if ((rc = graph_for(s, ph, &ge))) return rc;
+        }
+    }
+    PSIM_CUDA(cudaStreamSynchronize(s->st));
+    PSIM_CUDA(cudaEventRecord(s->ev[0], s->st));
+    if ((rc = psim_system_step_async(s, n_steps))) return rc;
+    PSIM_CUDA(cudaEventRecord(s->ev[1], s->st));
+    PSIM_CUDA(cudaEventSynchronize(s->ev[1]));
+    float t = 0.f;
+    PSIM_CUDA(cudaEventElapsedTime(&t, s->ev[0], s->ev[1]));
+    *ms = t;
+    return settle(s);
+}
+
+int psim_system_pair_count(psim_system* s, double cutoff, double* mean_pairs) {
+    if (!s || !mean_pairs) return fail(PSIM_ERR_INPUT, "NULL argument");
+    if (!s->uploaded) return fail(PSIM_ERR_INPUT, "no state uploaded");
+    if (cutoff > s->g.cs) return fail(PSIM_ERR_INPUT, "cutoff beyond the cell size");
+    DeviceGuard dg(s->device);
+    int rc = settle(s);
+    if (rc) return rc;
+    const Phase ph = phase_of(s->total);
+    ScopedBuf tot;
+    PSIM_CUDA(tot.ensure(8));
+    PSIM_CUDA(cudaMemsetAsync(tot.p, 0, 8, s->st));
+    CellView cv{s->posd.as<double4_32a>(), s->posh.as<float4>(), s->posl.as<float4>(),
+                s->cellid.as<int>(), s->start.as<int>(), s->count[ph.cb].as<int>()};
+    PSIM_CUDA(launch_pair_count(s->g, cv, (float)(cutoff * cutoff), tot.as<unsigned long long>(),
+                                s->st));
+    unsigned long long h = 0;
+    PSIM_CUDA(cudaMemcpyAsync(&h, tot.p, 8, cudaMemcpyDeviceToHost, s->st));
+    PSIM_CUDA(cudaStreamSynchronize(s->st));
+    *mean_pairs = s->n ? (double)h / s->n : 0.0;
+    return PSIM_OK;
+}
+
+int psim_measure_fp32_peak(int32_t device, double* tflops) {
+    if (!tflops) return fail(PSIM_ERR_INPUT, "NULL argument");
+    int rc = ensure_device();
+    if (rc) return rc;
+    DeviceGuard dg(device);
+    int sms = 0;
+    PSIM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    const int threads = 256, blocks = sms * 8, iters = 4096;
+    ScopedBuf sink;
+    PSIM_CUDA(sink.ensure(4));
+    cudaEvent_t a, b;
+    PSIM_CUDA(cudaEventCreate(&a));
+    PSIM_CUDA(cudaEventCreate(&b));
+    PSIM_CUDA(launch_fma_probe(blocks, threads, 64, sink.as<float>(), 0));  // warm-up
+    float best = 1e30f;
+    for (int r = 0; r < 5; ++r) {
+        PSIM_CUDA(cudaEventRecord(a, 0));
+        PSIM_CUDA(launch_fma_probe(blocks, threads, iters, sink.as<float>(), 0));
+        PSIM_CUDA(cudaEventRecord(b, 0));
+        PSIM_CUDA(cudaEventSynchronize(b));
+        float t = 0.f;
+        PSIM_CUDA(cudaEventElapsedTime(&t, a, b));
+        if (t < best) best = t;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    const double flops = 2.0 * 8.0 * 16.0 * (double)iters * threads * (double)blocks;
+    *tflops = flops / (best * 1e-3) / 1e12;
+    return PSIM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,188 @@
+// psim_device.cuh -- device-side building blocks shared by the kernels.
+//
+//   DevGeom      the cell grid (systemState's boxSize/cellSize/cellScale)
+//   error bits   latched by kernels, mapped to the reference's exit codes
+//   pair functors, one per IForce plugin: the __device__ form of the
+//                plugin's per-pair force (AOPotential.cpp:90-110,
+//                LJPotential.cpp:96-109, Calibration.cpp:75-81)
+//   Philox4x32-10 counter-based Gaussians (Salmon et al., SC'11)
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace psim {
+
+// ----------------------------------------------------------------- errors
+enum : uint32_t {
+    EBIT_BOUNDS = 1u,     // 7703 particle outside [0, L) after the wrap
+    EBIT_OVERLAP = 2u,    // 7704 r < 0.8 (Ri + Rj)
+    EBIT_NAN = 4u,        // 7705 non-finite AO force
+    EBIT_CELL = 8u,       // 7702 particle hashed outside the grid
+    EBIT_NOISE = 16u,     // 7706 injected noise buffer does not cover the step
+    EBIT_INDEX = 32u,     // 7706 a caller-supplied index or cell range is out of bounds
+};
+
+// ----------------------------------------------------------------- geometry
+struct DevGeom {
+    int n;          // particles
+    int s;          // cellScale
+    int s2;         // s*s
+    int ncell;      // s^3
+    double L;       // boxSize
+    double half;    // L / 2.0          (pbcDist, utilities.cpp:85)
+    double half_uv; // int(L) / 2       (unitVectorAdv with int L, utilities.cpp:124)
+    double cs;      // cellSize
+    double inv_cs;  // 1 / cellSize (fast path of the cell hash)
+    float Lhi, Llo; // L as a float pair (Lhi + Llo == L to ~1e-14)
+};
+
+// floor(x / cs) exactly as the reference computes it (systemHandling.cpp:39-41):
+// a multiply by 1/cs decides unless x/cs lies within 1e-9 of an integer, in
+// which case the correctly rounded division decides.
+__device__ __forceinline__ int cell_coord(double x, const DevGeom& g) {
+    double q = x * g.inv_cs;
+    double f = floor(q);
+    double fr = q - f;
+    if (fr > 1e-9 && fr < 1.0 - 1e-9) return (int)f;
+    return (int)floor(x / g.cs);
+}
+
+// Neighbour cell index wrapped into [0, s) as the reference does
+// ((c % s) + s when negative, AOPotential.cpp:154-160), and the periodic
+// image it implies (-1, 0 or +1 boxes).
+__device__ __forceinline__ int wrap_cell(int c, int s, int& shift) {
+    int w = c % s;
+    if (w < 0) w += s;
+    shift = (c - w) / s;
+    return w;
+}
+
+// ------------------------------------------------------------ pair functors
+// fnet64: the plugin's FP64 per-pair magnitude in the reference's operation
+// order, except that integer powers use binary powering and divisions by r2
+// or r multiply by 1/r (a few ulp, far inside the 1e-12 parity tolerance).
+// fnet32: the same formula in FP32 for the mixed form.
+
+template <typename T>
+__device__ __forceinline__ T powi_binary(T base, int e) {  // utilities.cpp:144-154
+    T ans = T(1);
+    while (e) {
+        if (e & 1) ans *= base;
+        e >>= 1;
+        base *= base;
+    }
+    return ans;
+}
+
+template <typename T>
+__device__ __forceinline__ T pow36(T rinv) {
+    T r2 = rinv * rinv, r4 = r2 * r2, r8 = r4 * r4, r16 = r8 * r8, r32 = r16 * r16;
+    return r32 * r4;
+}
+
+// AOPotential: fNet = -(36 r^-38 + coEff1/r + coEff2 r)   (AOPotential.cpp:90-99)
+struct AOPair {
+    double rc2, c1, c2;
+    float rc2f, c1f, c2f;
+    static constexpr bool kCheckNan = true;
+    __device__ __forceinline__ double fnet64(double r2, double r, double rinv, double) const {
+        double r36 = pow36(rinv);
+        double r38 = r36 * (rinv * rinv);
+        double f = 36.0 * r38 + c1 * rinv + c2 * r;
+        return -f;
+    }
+    __device__ __forceinline__ float fnet32(float r2, float r, float rinv, float) const {
+        float r36 = pow36(rinv);
+        float r38 = r36 * (rinv * rinv);
+        return -(36.0f * r38 + c1f * rinv + c2f * r);
+    }
+};
+
+// LennardJones: fNet = -kT wd [(2L-1) 4n L / r + yukStr e^{-r/lambda} (lambda + r)/r^2],
+// L = (size/r)^n                                          (LJPotential.cpp:96-109)
+struct LJPair {
+    double rc2, kTwd, four_n, yuk, lambda, inv_lambda;
+    float rc2f, kTwdf, four_nf, yukf, lambdaf, inv_lambdaf;
+    int n;
+    static constexpr bool kCheckNan = false;
+    __device__ __forceinline__ double fnet64(double r2, double r, double rinv, double size) const {
+        double lj = powi_binary(size * rinv, n);
+        double attract = (2.0 * lj) - 1.0;
+        attract *= (four_n * rinv * lj);
+        double repel = 0.0;
+        if (yuk != 0.0) {
+            double e = exp(-1.0 * (r * inv_lambda));
+            repel = e * (rinv * rinv * (lambda + r) * yuk);
+        }
+        return -kTwd * (attract + repel);
+    }
+    __device__ __forceinline__ float fnet32(float r2, float r, float rinv, float size) const {
+        float lj = powi_binary(size * rinv, n);
+        float attract = (2.0f * lj - 1.0f) * (four_nf * rinv * lj);
+        float repel = 0.0f;
+        if (yukf != 0.0f) repel = __expf(-r * inv_lambdaf) * (rinv * rinv * (lambdaf + r) * yukf);
+        return -kTwdf * (attract + repel);
+    }
+};
+
+// Calibration: fNet = -36 r^-37                           (Calibration.cpp:75-81)
+struct CalPair {
+    double rc2;
+    float rc2f;
+    static constexpr bool kCheckNan = false;
+    __device__ __forceinline__ double fnet64(double, double, double rinv, double) const {
+        return -(36.0 * (pow36(rinv) * rinv));
+    }
+    __device__ __forceinline__ float fnet32(float, float, float rinv, float) const {
+        return -(36.0f * (pow36(rinv) * rinv));
+    }
+};
+
+// ---------------------------------------------------------------- Philox
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as
+// easy as 1, 2, 3", SC'11): counter (step, draw-group, particle, 0), key
+// (seed, stream tag).
+struct Philox4 {
+    uint32_t v[4];
+};
+
+__device__ __forceinline__ Philox4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2,
+                                                 uint32_t c3, uint32_t k0, uint32_t k1) {
+    const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+    const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        uint32_t hi0 = __umulhi(M0, c0), lo0 = M0 * c0;
+        uint32_t hi1 = __umulhi(M1, c2), lo1 = M1 * c2;
+        uint32_t n0 = hi1 ^ c1 ^ k0, n1 = lo1, n2 = hi0 ^ c3 ^ k1, n3 = lo0;
+        c0 = n0; c1 = n1; c2 = n2; c3 = n3;
+        k0 += W0; k1 += W1;
+    }
+    return Philox4{{c0, c1, c2, c3}};
+}
+
+// Two Gaussians from two 32-bit words by the Box-Muller transform in FP32
+// (the reference itself stores every other deviate as a float,
+// fastRandom.h:16).
+__device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, double& z0, double& z1) {
+    float u1 = ((float)(a >> 8) + 1.0f) * (1.0f / 16777216.0f);  // (0, 1]
+    float u2 = (float)(b >> 8) * (1.0f / 16777216.0f);            // [0, 1)
+    float rad = sqrtf(-2.0f * logf(u1));
+    float sn, cs;
+    sincospif(2.0f * u2, &sn, &cs);
+    z0 = (double)(rad * cs);
+    z1 = (double)(rad * sn);
+}
+
+// Six Gaussians for (particle tag, step): the normal step's xi_x..z, mem_x..z.
+__device__ __forceinline__ void philox_gaussians6(uint32_t seed, uint32_t tag, uint32_t step,
+                                                  double g[6]) {
+    Philox4 a = philox4x32_10(step, 0u, tag, 0u, seed, 0x5053494Du);
+    Philox4 b = philox4x32_10(step, 1u, tag, 0u, seed, 0x5053494Du);
+    box_muller(a.v[0], a.v[1], g[0], g[1]);
+    box_muller(a.v[2], a.v[3], g[2], g[3]);
+    box_muller(b.v[0], b.v[1], g[4], g[5]);
+}
+
+}  // namespace psim

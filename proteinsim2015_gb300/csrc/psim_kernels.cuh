@@ -1,0 +1,193 @@
+// psim_kernels.cuh -- launch interfaces between the host layer (psim_api.cu)
+// and the kernel translation units:
+//   psim_exact.cu  FP64 kernels built without FMA contraction (the plain
+//                  force form, the vGB update, the cell hash)
+//   psim_mixed.cu  the FP32-pair / Kahan-sum force form
+//   psim_cells.cu  counting sort, scan, reorder, layout conversions
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "psim_device.cuh"
+
+namespace psim {
+
+// A plugin's device functor set, built on the host from psim_force_params.
+struct ForceSetup {
+    int kind;          // psim_force_kind
+    AOPair ao;
+    LJPair lj;
+    CalPair cal;
+    double rc_max;     // largest cutoff: cell_size must be >= rc_max
+    float pre_rc2f;    // conservative FP32 prefilter bound on r^2 (FP64 form)
+};
+
+// Positions and cell ranges in sorted (cell) order, as the force kernels read them.
+struct CellView {
+    const double4_32a* posd;  // {x, y, z, R}  (FP64 form)
+    const float4* posh;   // {x, y, z, R} rounded to FP32
+    const float4* posl;   // {x - xh, y - yh, z - zh, 0} (mixed form)
+    const int* cellid;    // cell hash of each sorted slot
+    const int* cstart;    // first sorted slot of each cell
+    const int* ccount;    // particles in each cell
+};
+
+struct ForceOut {
+    double* fx;
+    double* fy;
+    double* fz;
+    uint32_t* err;
+};
+
+cudaError_t launch_forces_fp64(const ForceSetup& fs, const DevGeom& g, const CellView& cv,
+                               const ForceOut& out, cudaStream_t st);
+cudaError_t launch_forces_mixed(const ForceSetup& fs, const DevGeom& g, const CellView& cv,
+                                const ForceOut& out, cudaStream_t st);
+
+// vGB coefficients and per-step switches for the integrator kernels.
+struct VgbParams {
+    double dt, dt2, dt3, dt_inv, c0;
+    double coeff0, coeff1, coeff2, coeff3;
+    double sig1, sig2, corr, dev, goy2, goy3, hn;
+    int vel_freq;
+    uint32_t seed;
+};
+
+// Device-side step state, advanced by the rebuild's last kernel so a captured
+// CUDA graph replays without host-side argument changes.
+struct StepState {
+    long long step;       // steps taken since upload (0 -> firstStep)
+    int vel_counter;      // brownianIntegrator::velCounter
+    int pad;
+};
+
+struct NoiseView {
+    int mode;             // psim_noise_mode
+    const double* buf;    // injected noise, [step - first][tag][6]
+    long long first;
+    long long n_steps;
+};
+
+// The system-order integrator: gathers the previous state through perm,
+// writes the new state in the current cell order, hashes the new positions
+// and counts them into the next grid.
+struct VgbSystemArgs {
+    int n;
+    const int* perm;            // current slot -> previous-order slot
+    const int* tag;             // original index of each current slot
+    const double* inv_mass;     // 1/m, current order
+    const double* x; const double* y; const double* z;       // previous order
+    const double* x0; const double* y0; const double* z0;
+    const double* mx; const double* my; const double* mz;    // memX/Y/Z
+    const double* fx; const double* fy; const double* fz;    // F, current order
+    const double* gx; const double* gy; const double* gz;    // F0, previous order
+    double* vel;                // 3n, original order (tag-indexed)
+    double* ox; double* oy; double* oz;                      // new pos, current order
+    double* ox0; double* oy0; double* oz0;
+    double* omx; double* omy; double* omz;
+    int* key;                   // new cell hash, current order
+    int* rank;                  // slot inside the new cell (atomic order)
+    int* count;                 // per-cell counts of the next grid (zeroed)
+    uint32_t* err;
+    const StepState* state;
+};
+cudaError_t launch_vgb_system(const VgbSystemArgs& a, const VgbParams& p, const DevGeom& g,
+                              const NoiseView& nz, cudaStream_t st);
+
+// Reference-layout integrator (brownianIntegrator::nextSystem on AoS arrays
+// in original order).  mem/mem_corr: 3n device arrays owned by the integrator.
+struct VgbAosArgs {
+    int n;
+    int first;
+    int vel_step;
+    double* pos; double* pos0; double* vel;
+    const double* frc; const double* frc0;
+    const double* mass;
+    double* mem; double* mem_corr;
+    const double* noise;        // n*6 (injected) or null
+    uint32_t seed;
+    long long philox_step;
+    uint32_t* err;
+};
+cudaError_t launch_vgb_aos(const VgbAosArgs& a, const VgbParams& p, double L, cudaStream_t st);
+
+// Cell hash + atomic count of positions given as three coordinate arrays.
+cudaError_t launch_hash_count(int n, const double* x, const double* y, const double* z,
+                              const DevGeom& g, int* key, int* rank, int* count,
+                              uint32_t* err, cudaStream_t st);
+
+// ---------------------------------------------------------- cells (psim_cells.cu)
+// Exclusive scan of count[ncell] into start[ncell]; scratch needs
+// scan_scratch_ints(ncell) ints.
+size_t scan_scratch_ints(int ncell);
+cudaError_t launch_scan(const int* count, int* start, int ncell, int* scratch, cudaStream_t st);
+
+// tmp[start[key[f]] + rank[f]] = f
+cudaError_t launch_scatter(int n, const int* key, const int* rank, const int* start, int* tmp,
+                           const uint32_t* err, cudaStream_t st);
+
+// Canonical order inside each cell (by original index), the permutation and
+// the sorted-order arrays the force kernel reads.
+struct CanonArgs {
+    int n;
+    const int* tmp;         // atomic-order slot -> previous-order index
+    const int* key;         // cell of each previous-order index
+    const int* start;
+    const int* count;
+    const int* tag_in;      // previous order
+    const double* radius_in;
+    const double* inv_mass_in;
+    const double* x; const double* y; const double* z;   // positions, previous order
+    int* perm;              // new slot -> previous index
+    int* tag_out;
+    double* radius_out;
+    double* inv_mass_out;   // may be null
+    int* cellid;
+    double4_32a* posd;          // may be null
+    float4* posh;
+    float4* posl;           // may be null
+    StepState* state;       // may be null: advanced once per rebuild
+    int advance;            // 1: this rebuild ends a step (advance state)
+    int vel_freq;           // brownianIntegrator::velFreq
+    const uint32_t* err;    // non-zero: a previous kernel failed, skip the work
+};
+cudaError_t launch_canonicalize(const CanonArgs& a, cudaStream_t st);
+
+// Reference layout exports.
+cudaError_t launch_export_cells(int n, int ncell, const int* cellid, const int* tag,
+                                const double4_32a* posd, const int* start, const int* count,
+                                int32_t* hash_index, uint32_t* cse, double* sorted,
+                                cudaStream_t st);
+// Sorted-order SoA force -> original-order AoS (particle_force layout).
+cudaError_t launch_unsort_force(int n, const int* tag, const double* fx, const double* fy,
+                                const double* fz, double* out, cudaStream_t st);
+// Reference layout imports for psim_force_evaluate.
+// Also hashes each position into cellid (EBIT_CELL when outside the grid).
+cudaError_t launch_import_sorted(int n, const double* sorted, const int32_t* hash_index,
+                                 const DevGeom& g, double4_32a* posd, float4* posh, float4* posl,
+                                 int* cellid, int* tag, uint32_t* err, cudaStream_t st);
+// Ranges beyond n set EBIT_INDEX and are treated as empty.
+cudaError_t launch_import_cse(int ncell, int n, const uint32_t* cse, int* start, int* count,
+                              uint32_t* err, cudaStream_t st);
+// AoS xyz -> three arrays, optionally scattered by tag (gather == 0) or
+// gathered (gather == 1: out[i] = in[tag[i]]).
+cudaError_t launch_split_xyz(int n, const double* aos, const int* tag, int gather, double* x,
+                             double* y, double* z, cudaStream_t st);
+// three arrays in storage order -> AoS original order: out[tag[i]] = (x[i], y[i], z[i]);
+// with perm != null the source index is perm[i].
+cudaError_t launch_merge_xyz(int n, const double* x, const double* y, const double* z,
+                             const int* tag, const int* perm, double* aos, cudaStream_t st);
+cudaError_t launch_fill_int_iota(int n, int* v, cudaStream_t st);
+// out[i] = (x[perm[i]], y[perm[i]], z[perm[i]], radius[i])
+cudaError_t launch_gather_posd(int n, const int* perm, const double* x, const double* y,
+                               const double* z, const double* radius, double4_32a* out,
+                               cudaStream_t st);
+cudaError_t launch_occupancy(int ncell, const int* count, int* max_out, cudaStream_t st);
+// Ordered pairs closer than rc (FP32 test on posh) summed into *total.
+cudaError_t launch_pair_count(const DevGeom& g, const CellView& cv, float rc2,
+                              unsigned long long* total, cudaStream_t st);
+// FMA-chain throughput probe: `iters` rounds of 8 independent FMA chains per thread.
+cudaError_t launch_fma_probe(int blocks, int threads, int iters, float* sink, cudaStream_t st);
+
+}  // namespace psim

@@ -1,0 +1,96 @@
+"""Generate tests/golden/*.npz from the reference itself.
+
+The reference (SawyerHopkins/ProteinSim2015) ships no tests, fixtures or
+golden vectors, so these are produced by running its own hot-path code,
+rebuilt from its sources by oracle/build_ref.sh (oracle/_ref), on seeded
+inputs.  Inputs are stored next to the outputs so the fixtures stand alone
+(the GPU machine has no reference tree).
+
+    python tests/golden/make_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import ref  # noqa: E402
+from proteinsim2015_gb300 import init  # noqa: E402
+
+
+def state_small(n, box, seed):
+    pos = init.rsa(n, box, 1.0, seed=seed)
+    return pos.reshape(-1), np.full(n, 0.5)
+
+
+def main():
+    if not ref.available():
+        if not ref.build():
+            sys.exit("reference sources not found; cannot generate golden fixtures")
+    out = {}
+    # ---- case A: AO-type state, L=12, cellSize 3, scale 4 (N=300)
+    n, box, cs, scale = 300, 12, 3, 4
+    pos, rad = state_small(n, box, seed=11)
+    hi, cse, srt = ref.build_cells(n, box, cs, scale, pos, rad)
+    pr = hi.reshape(-1, 2)
+    order = np.lexsort((pr[:, 1], pr[:, 0]))  # the reference's sort is unstable
+    out.update(cellsA_pos=pos, cellsA_radius=rad, cellsA_geom=np.array([n, box, cs, scale]),
+               cellsA_hash_index=pr[order].reshape(-1), cellsA_cse=cse)
+    srt_stable = srt.reshape(-1, 4)[order].reshape(-1)
+    out["cellsA_sorted"] = srt_stable
+    hi_s = pr[order].reshape(-1).astype(np.int32)
+    forces = {
+        "AO": ("AO", {"kT": 1.0, "wellDepth": 4.0, "cutOff": 1.1}),
+        "AOq": ("AO", {"kT": 1.5, "wellDepth": 0.25, "cutOff": 1.2}),
+        "LJ6": ("LJ", {"kT": 1.5, "wellDepth": 1 / 1.5, "cutOff": 2.5, "ljNum": 6,
+                       "yukawaStrength": 0, "debyeLength": 0.5}),
+        "LJ18": ("LJ", {"kT": 1.0, "wellDepth": 3.0, "cutOff": 2.5, "ljNum": 18,
+                        "yukawaStrength": 8.0, "debyeLength": 0.5}),
+        "YUK": ("LJ", {"kT": 1.0, "wellDepth": 1.0, "cutOff": 3.0, "ljNum": 0,
+                       "yukawaStrength": 2183.93, "debyeLength": 0.25}),
+        "CAL": ("Cal", {"cutOff": 1.1}),
+    }
+    for key, (plugin, settings) in forces.items():
+        f = ref.forces(plugin, settings, n, box, cs, scale, srt_stable, hi_s, cse)
+        out["forceA_%s" % key] = f
+        out["forceA_%s_settings" % key] = np.array(repr(settings))
+    # ---- vGB coefficients (known-answer set-up)
+    for g in (1.0, 0.5, 0.01, 0.049, 2.0):
+        c = ref.vgb_coeffs({"gamma": g, "timeStep": 0.001, "kT": 1.0, "nParticles": 1})
+        out["vgb_%g" % g] = np.array([c[k] for k in ref.VGB_KEYS])
+    c = ref.vgb_coeffs({"gamma": 1.0, "timeStep": 0.002, "kT": 1.5, "nParticles": 1})
+    out["vgb_lj"] = np.array([c[k] for k in ref.VGB_KEYS])
+    # ---- trajectories with injected noise (system::run loop body)
+    for tag, plugin, settings, steps, vel_freq in (
+            ("AO", "AO", {"kT": 1.0, "wellDepth": 4.0, "cutOff": 1.1}, 20, 3),
+            ("LJ", "LJ", {"kT": 1.5, "wellDepth": 1 / 1.5, "cutOff": 2.5, "ljNum": 6,
+                          "yukawaStrength": 0, "debyeLength": 0.5}, 10, 0)):
+        rng = np.random.default_rng(5)
+        vel = init.maxwell(n, settings["kT"], seed=7).reshape(-1)
+        noise = rng.standard_normal(steps * n * 6)
+        run_settings = dict(settings, gamma=1.0, nParticles=n, velFreq=vel_freq, mass=1.0,
+                            seed=90210, timeStep=0.001)
+        p = pos.copy()
+        p0, v = np.zeros(3 * n), vel.copy()
+        fr, fr0 = np.zeros(3 * n), np.zeros(3 * n)
+        mass = np.ones(n)
+        hi_t, cse_t, srt_t, lf = ref.run(plugin, run_settings, n, box, cs, scale, steps, noise, p,
+                                         p0, v, fr, fr0, rad, mass)
+        out.update({"traj%s_vel0" % tag: vel, "traj%s_noise" % tag: noise,
+                    "traj%s_meta" % tag: np.array([steps, vel_freq]),
+                    "traj%s_settings" % tag: np.array(repr(run_settings)),
+                    "traj%s_pos" % tag: p, "traj%s_pos0" % tag: p0, "traj%s_vel" % tag: v,
+                    "traj%s_frc" % tag: fr, "traj%s_frc0" % tag: fr0})
+    # ---- the reference's per-particle generator
+    for seed in (90210, 180420, 7):
+        out["rng_%d" % seed] = ref.rng_draws(seed, 256)
+    path = os.path.join(HERE, "reference_hotpath.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path, os.path.getsize(path), "bytes")
+
+
+if __name__ == "__main__":
+    main()

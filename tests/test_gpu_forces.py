@@ -1,0 +1,87 @@
+"""Force pass on the GPU: plain FP64 form against the reference within 1e-12
+(per particle, relative to sum_j |f_ij|); mixed form within 1e-5 (norm)."""
+import numpy as np
+import pytest
+
+from conftest import settings_of
+from gpu_helpers import (FORCE_TOL_FP64, FORCE_TOL_MIXED, lattice_state, oracle_force,
+                         rel_norm, rel_per_particle, rsa_state)
+from oracle import port
+
+pytestmark = pytest.mark.gpu
+
+PLUGIN_OF = {"AO": "AOPotential", "AOq": "AOPotential", "LJ6": "LennardJones",
+             "LJ18": "LennardJones", "YUK": "LennardJones", "CAL": "Calibration"}
+
+
+def params_from_golden(psim, golden, key):
+    s = settings_of(golden, "forceA_%s_settings" % key)
+    text = "".join("%s = %r\n" % kv for kv in s.items())
+    return psim.force_params_from_settings(PLUGIN_OF[key], text)
+
+
+@pytest.mark.parametrize("key", sorted(PLUGIN_OF))
+@pytest.mark.parametrize("precision", [0, 1])
+def test_forces_match_reference_golden(psim, golden, key, precision):
+    n, box, cs, scale = (int(v) for v in golden["cellsA_geom"])
+    g = psim.geometry(n, box, cs, scale)
+    p = params_from_golden(psim, golden, key)
+    f = psim.force_evaluate(p, g, golden["cellsA_sorted"], golden["cellsA_hash_index"],
+                            golden["cellsA_cse"], precision=precision)
+    ref = golden["forceA_%s" % key]
+    _, _, _, _, _, scale_ = oracle_force(p.as_dict(), g, golden["cellsA_pos"],
+                                         golden["cellsA_radius"])
+    if precision == 0:
+        assert rel_per_particle(f, ref, scale_) <= FORCE_TOL_FP64
+    else:
+        assert rel_norm(f, ref) <= FORCE_TOL_MIXED
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_lj_dense_liquid_matches_oracle(psim, precision):
+    # rho = 0.8 LJ (the 2^20 benchmark's density), a jittered FCC block
+    pos, rad, box = lattice_state(8, (4 / 0.8) ** (1 / 3), 0.08, seed=4)
+    n = len(rad)
+    scale = int(box // 2.5)
+    g = psim.geometry(n, box, box / scale, scale)
+    p = psim.make_force("LJ", 2.5, kT=1.5, well_depth=1 / 1.5, lj_num=6, yukawa_strength=0.0)
+    hi, cse, srt, ref, err, sc = oracle_force(p.as_dict(), g, pos, rad)
+    assert err == 0
+    f = psim.force_evaluate(p, g, srt, hi, cse, precision=precision)
+    if precision == 0:
+        assert rel_per_particle(f, ref, sc) <= FORCE_TOL_FP64
+    else:
+        assert rel_norm(f, ref) <= FORCE_TOL_MIXED
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_ao_yukawa_composite_matches_oracle(psim, precision):
+    pos, rad = rsa_state(3000, 26.0, seed=9)
+    n = len(rad)
+    g = psim.geometry(n, 26.0, 26.0 / 8, 8)
+    p = psim.make_force("AO_YUK", 1.1, kT=1.0, well_depth=0.1875, cutoff2=3.0, well_depth2=1.0,
+                        yukawa_strength=2183.93, debye_length=0.25, lj_num=0)
+    hi, cse, srt, ref, err, sc = oracle_force(p.as_dict(), g, pos, rad)
+    assert err == 0
+    f = psim.force_evaluate(p, g, srt, hi, cse, precision=precision)
+    if precision == 0:
+        assert rel_per_particle(f, ref, sc) <= FORCE_TOL_FP64
+    else:
+        assert rel_norm(f, ref) <= FORCE_TOL_MIXED
+
+
+def test_overlap_is_reported_as_7704(psim):
+    g = psim.geometry(2, 12.0, 3.0, 4)
+    pos = np.array([1.0, 1.0, 1.0, 1.5, 1.0, 1.0])
+    hi, cse, srt = psim.cells_build(g, pos, np.full(2, 0.5))
+    for prec in (0, 1):
+        with pytest.raises(psim.PsimError) as e:
+            psim.force_evaluate(psim.make_force("AO", 1.1, well_depth=1.0), g, srt, hi, cse, prec)
+        assert e.value.code == psim.ERR_OVERLAP
+
+
+def test_empty_and_single_particle(psim):
+    g = psim.geometry(1, 12.0, 3.0, 4)
+    hi, cse, srt = psim.cells_build(g, np.array([5.0, 5.0, 5.0]), np.full(1, 0.5))
+    f = psim.force_evaluate(psim.make_force("AO", 1.1, well_depth=1.0), g, srt, hi, cse)
+    assert np.array_equal(f, np.zeros(3))

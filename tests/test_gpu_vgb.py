@@ -1,0 +1,71 @@
+"""brownianIntegrator::nextSystem on the GPU (reference-layout drop-in)
+against the oracle with identical injected noise."""
+import numpy as np
+import pytest
+
+from gpu_helpers import rsa_state
+from oracle import port
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(n=2000, box=20.0, seed=3):
+    pos, rad = rsa_state(n, box, seed)
+    rng = np.random.default_rng(seed)
+    return dict(pos=pos, pos0=pos.copy(), vel=rng.standard_normal(3 * n),
+                frc=rng.standard_normal(3 * n) * 50, frc0=rng.standard_normal(3 * n) * 50,
+                mass=rng.uniform(0.5, 2.0, n), n=n, box=box, rng=rng)
+
+
+@pytest.mark.parametrize("gamma,dt", [(1.0, 0.001), (0.01, 0.001), (5.0, 0.002)])
+def test_next_system_matches_oracle(psim, gamma, dt):
+    s = _setup()
+    n, box = s["n"], s["box"]
+    vel_freq = 1
+    it = psim.Integrator(n, gamma=gamma, dt=dt, kT=1.0, vel_freq=vel_freq)
+    g = port.geom(n, box, box / 5, 5)
+    c = port.vgb_coeffs(gamma, dt, 1.0)
+    gp = {k: s[k].copy() for k in ("pos", "pos0", "vel", "frc", "frc0")}
+    op = {k: s[k].copy() for k in ("pos", "pos0", "vel", "frc", "frc0")}
+    mem, memc = np.zeros(3 * n), np.zeros(3 * n)
+    vc = 0
+    for step in range(6):
+        noise = s["rng"].standard_normal(6 * n)
+        pf = s["rng"].standard_normal(3 * n) * 30
+        it.next_system(step * dt if step else 0.0, box, gp["pos"], gp["pos0"], gp["vel"],
+                       gp["frc"], gp["frc0"], s["mass"], noise=noise, particle_force=pf)
+        port.lib().oracle_push_force(n, port._p(pf), port._p(op["frc"]), port._p(op["frc0"]))
+        first = step == 0
+        vs = (not first) and (vel_freq == 0 or vc == vel_freq)
+        err = port.lib().oracle_vgb_step(port.C.byref(g), port.C.byref(c), dt, int(first), int(vs),
+                                         port._p(noise), port._p(op["pos"]), port._p(op["pos0"]),
+                                         port._p(op["vel"]), port._p(op["frc"]),
+                                         port._p(op["frc0"]), port._p(s["mass"]), port._p(mem),
+                                         port._p(memc))
+        assert err == 0
+        if not first:
+            vc = 0 if vc == vel_freq else vc + 1
+        for k in ("pos", "pos0", "vel", "frc", "frc0"):
+            # same IEEE operations in the same order, no FMA: expected bit-exact
+            assert np.max(np.abs(gp[k] - op[k])) <= 1e-15 * max(1.0, np.max(np.abs(op[k]))), (k, step)
+
+
+def test_out_of_bounds_is_reported_as_7703(psim):
+    n, box = 4, 12.0
+    it = psim.Integrator(n, gamma=1.0, dt=0.001, kT=1.0)
+    pos = np.array([1.0, 1.0, 1.0, 5.0, 5.0, 5.0, 9.0, 9.0, 9.0, 2.0, 8.0, 3.0])
+    z = np.zeros(3 * n)
+    # a force that throws particle 0 beyond one box length: the single +-L wrap
+    # of safeMod cannot bring it back (particle.cpp:67-69)
+    pf = z.copy()
+    pf[0] = -1e11
+    with pytest.raises(psim.PsimError) as e:
+        it.next_system(0.0, box, pos, pos.copy(), z.copy(), z.copy(), z.copy(), np.ones(n),
+                       noise=np.zeros(6 * n), particle_force=pf)
+    assert e.value.code == psim.ERR_PARTICLE_BOUNDS
+
+
+def test_gamma_zero_is_refused(psim):
+    with pytest.raises(psim.PsimError) as e:
+        psim.Integrator(10, gamma=0.0)
+    assert e.value.code == psim.ERR_INPUT
