@@ -125,23 +125,30 @@ def measured_peaks():
 
 def cpu_steps(w, threads):
     """A stepping closure over the oracle restatement on the host cores:
-    run(k) advances the workload k whole steps (noise reused cyclically,
-    which does not change the work)."""
+    run(k) advances the workload k whole steps, with fresh counter-based
+    Gaussians every step."""
     from oracle import port
     port.set_threads(threads)
     g = port.geom(w["n"], w["box"], w["cell_size"], w["scale"])
     f = port.make_force(port.LJ, RC, kT=KT, well_depth=WD, lj_num=LJN, yuk_str=0.0)
     c = port.vgb_coeffs(GAMMA, DT, KT)
     st = port.State(w["pos"], w["radius"], vel=w["vel"])
-    noise = np.random.default_rng(1).standard_normal(w["n"] * 6)
     cells = [None]
 
     def run(k):
-        err, hi, cse, srt, _ = port.run(g, f, c, DT, st, k, noise, vel_freq=1000,
+        err, hi, cse, srt, _ = port.run(g, f, c, DT, st, k, None, vel_freq=1000,
                                         cells=cells[0])
         cells[0] = (hi, cse, srt)
         if err:
-            raise RuntimeError("oracle step failed with %d" % err)
+            msg = "oracle step %d failed with %d" % (st.step, err)
+            try:
+                from scipy.spatial import cKDTree
+                p = np.mod(st.pos.reshape(-1, 3), w["box"])
+                d, _ = cKDTree(p, boxsize=w["box"]).query(p, k=2)
+                msg += "; min pair distance %.6g" % d[:, 1].min()
+            except Exception:
+                pass
+            raise RuntimeError(msg)
     return run
 
 
@@ -158,6 +165,22 @@ def cpu_port_rate(w, budget_s, threads):
         if el >= budget_s or steps >= 1000:
             break
     return w["n"] * steps / el, steps, el
+
+
+def cpu_baseline_child(budget_s):
+    """Body of the child process that times the CPU baseline (it runs apart
+    from the GPU process so neither disturbs the other)."""
+    w = workload()
+    cores = os.cpu_count() or 1
+    try:
+        v, steps, secs = cpu_port_rate(w, budget_s, cores)
+        out = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": "N=%d, %d whole steps (%.1f s) of the same workload" % (
+                   w["n"], steps, secs)}
+    except Exception as e:
+        out = {"value": None, "unit": UNIT, "cores": cores, "kind": "port", "error": str(e)}
+    print(json.dumps(out))
+    return 0
 
 
 def run_reference(args):
@@ -197,28 +220,16 @@ def run_reference(args):
     return 0
 
 
-def cpu_baseline(w, cores, w_gpu_sum=None, w_now=None):
+def cpu_baseline(budget_s=15.0):
     """The oracle restatement on the host cores over a bounded sample (about
-    15 s) of the same workload; failures are reported, with diagnostics of
-    the starting state, instead of ending the run."""
-    try:
-        v, steps, secs = cpu_port_rate(w, 15.0, cores)
-        return {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                "sample": "N=%d, %d whole steps (%.1f s) of the same workload" % (
-                    w["n"], steps, secs)}
-    except Exception as e:  # report, do not hide: the GPU numbers stay valid
-        diag = {"error": str(e), "pos_sum_fresh": float(np.sum(w["pos"]))}
-        if w_gpu_sum is not None:
-            diag["pos_sum_at_start"] = w_gpu_sum
-            diag["pos_sum_after_gpu"] = float(np.sum(w_now["pos"]))
-        try:
-            from scipy.spatial import cKDTree
-            p = np.mod(w["pos"].reshape(-1, 3), w["box"])
-            d, _ = cKDTree(p, boxsize=w["box"]).query(p, k=2)
-            diag["min_pair_distance"] = float(d[:, 1].min())
-        except Exception as e2:
-            diag["kdtree"] = str(e2)
-        return {"value": None, "unit": UNIT, "cores": cores, "kind": "port", "diag": diag}
+    budget_s) of the same workload, timed in a child process."""
+    p = subprocess.run([sys.executable, os.path.abspath(__file__), "--cpu-baseline-json",
+                        str(budget_s)], capture_output=True, text=True, timeout=900)
+    for line in reversed(p.stdout.splitlines()):
+        if line.startswith("{"):
+            return json.loads(line)
+    return {"value": None, "unit": UNIT, "kind": "port",
+            "error": "child failed rc=%d: %s" % (p.returncode, p.stderr[-500:])}
 
 
 def pinned(n):
@@ -269,7 +280,6 @@ def run_gpu(args):
     if psim.device_count() <= dev:
         raise SystemExit("no CUDA device %d" % dev)
     w = workload()
-    pos_sum = float(np.sum(w["pos"]))
     n, box, scale = w["n"], w["box"], w["scale"]
     g = psim.geometry(n, box, box / scale, scale)
     p = psim.make_force("LJ", RC, kT=KT, well_depth=WD, lj_num=LJN, yukawa_strength=0.0)
@@ -329,8 +339,7 @@ def run_gpu(args):
     achieved = flops_launch / (f_ms * 1e-3) / 1e12
     peaks = measured_peaks()
     # ---- CPU baseline: the oracle restatement on the host cores, bounded sample
-    cores = os.cpu_count() or 1
-    cpu = cpu_baseline(workload(), cores, w_gpu_sum=pos_sum, w_now=w)
+    cpu = cpu_baseline(15.0)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps, "higher_is_better": True,
@@ -374,9 +383,13 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-baseline-json", type=float, default=None,
+                    help=argparse.SUPPRESS)
     ap.add_argument("--profile-only", action="store_true",
                     help="time the mixed form and its phases only (short runs under ncu)")
     args = ap.parse_args()
+    if args.cpu_baseline_json is not None:
+        return cpu_baseline_child(args.cpu_baseline_json)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

@@ -194,13 +194,16 @@ class State:
 def run(g, f, c, dt, state, n_steps, noise, vel_freq=1000, cells=None):
     """Advance ``state`` n_steps through the reference hot loop; returns
     (err, hash_index, cell_start_end, sorted, last_force).  ``noise`` holds
-    whole steps of n*6 Gaussians; with fewer steps than n_steps they are
-    reused cyclically.  ``cells`` (hash_index, cse, sorted) continues from a
+    whole steps of n*6 Gaussians (reused cyclically when shorter than
+    n_steps), or None for the oracle's own counter-based generator.  ``cells`` (hash_index, cse, sorted) continues from a
     previous call's cell list instead of rebuilding it."""
     n = g.n
-    noise = np.ascontiguousarray(noise, np.float64).reshape(-1)
-    noise_steps = noise.size // (n * 6) if n else 1
-    assert noise_steps >= 1
+    if noise is None:   # counter-based Gaussians generated inside the oracle
+        noise_steps = 0
+    else:
+        noise = np.ascontiguousarray(noise, np.float64).reshape(-1)
+        noise_steps = noise.size // (n * 6) if n else 1
+        assert noise_steps >= 1
     if cells is None:
         hi, cse, sorted_ = build_cells(g, state.pos, state.radius)
     else:

@@ -474,6 +474,30 @@ int oracle_vgb_step(const oracle_geom* g, const oracle_vgb* c, double dt, int fi
     return bad_all ? ORACLE_ERR_BOUNDS : 0;
 }
 
+/* Six standard normal deviates for (step, particle) from a counter-based
+ * generator (SplitMix64 finaliser, Steele et al. 2014, + Box-Muller); used
+ * when no injected noise is given, e.g. for timing the CPU path. */
+static inline uint64_t mix64(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+static void counter_noise(int step, int n, double* out) {
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; i++) {
+        uint64_t key = ((uint64_t)(uint32_t)step << 32) ^ (uint64_t)(uint32_t)i;
+        for (int k = 0; k < 3; k++) {
+            uint64_t a = mix64(key * 6 + 2 * k), b = mix64(key * 6 + 2 * k + 1);
+            double u1 = ((double)(a >> 11) + 1.0) * (1.0 / 9007199254740992.0);
+            double u2 = (double)(b >> 11) * (1.0 / 9007199254740992.0);
+            double r = sqrt(-2.0 * log(u1));
+            out[6 * (size_t)i + 2 * k] = r * cos(6.283185307179586 * u2);
+            out[6 * (size_t)i + 2 * k + 1] = r * sin(6.283185307179586 * u2);
+        }
+    }
+}
+
 /* system.cpp:170-212, the hot loop without the analysis-only sweep. */
 int oracle_run(const oracle_geom* g, const oracle_force* f, const oracle_vgb* c,
                double dt, int step0, int n_steps, int vel_freq, int* vel_counter,
@@ -482,13 +506,20 @@ int oracle_run(const oracle_geom* g, const oracle_force* f, const oracle_vgb* c,
                double* mem, double* mem_corr, int* hi, uint32_t* cse, double* sorted,
                double* force) {
     const int n = g->n;
+    double* own = noise ? NULL : (double*)malloc(sizeof(double) * 6 * (size_t)(n > 0 ? n : 1));
     for (int t = 0; t < n_steps; t++) {
         int step = step0 + t;
         int e = oracle_forces(g, f, sorted, hi, cse, force);
-        if (e) return e;
+        if (e) { free(own); return e; }
         oracle_push_force(n, force, frc, frc0);
-        const int nt = noise_steps > 0 ? t % noise_steps : t;
-        const double* nz = noise + (size_t)nt * (size_t)n * 6;
+        const double* nz;
+        if (own) {
+            counter_noise(step, n, own);
+            nz = own;
+        } else {
+            const int nt = noise_steps > 0 ? t % noise_steps : t;
+            nz = noise + (size_t)nt * (size_t)n * 6;
+        }
         if (step == 0) {
             e = oracle_vgb_step(g, c, dt, 1, 0, nz, pos, pos0, vel, frc, frc0, mass, mem, mem_corr);
         } else {
@@ -496,9 +527,10 @@ int oracle_run(const oracle_geom* g, const oracle_force* f, const oracle_vgb* c,
             e = oracle_vgb_step(g, c, dt, 0, vs, nz, pos, pos0, vel, frc, frc0, mass, mem, mem_corr);
             *vel_counter = (*vel_counter == vel_freq) ? 0 : *vel_counter + 1;
         }
-        if (e) return e;
+        if (e) { free(own); return e; }
         oracle_build_cells(g, pos, radius, hi, cse, sorted);
     }
+    free(own);
     return 0;
 }
 

@@ -119,7 +119,9 @@ int oracle_vgb_step(const oracle_geom* g, const oracle_vgb* c, double dt,
                     const double* mass, double* mem, double* mem_corr);
 
 /* a15: system::run loop (system.cpp:170-212) for n_steps from step0, with
- * injected noise noise[((t % noise_steps)*n + i)*6 + k] for local step t.  vel_freq as the integrator's
+ * injected noise noise[((t % noise_steps)*n + i)*6 + k] for local step t,
+ * or (noise == NULL) Gaussians from a counter-based generator keyed by
+ * (step, particle).  vel_freq as the integrator's
  * velFreq; *vel_counter carries the integrator's velCounter across calls.
  * Returns 0 or an error code. */
 int oracle_run(const oracle_geom* g, const oracle_force* f, const oracle_vgb* c,

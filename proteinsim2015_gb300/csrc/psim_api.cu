@@ -168,6 +168,13 @@ int make_geom(const psim_geometry* gm, double rc_max, DevGeom* g) {
     g->inv_cs = 1.0 / gm->cell_size;
     g->Lhi = (float)g->L;
     g->Llo = (float)(g->L - (double)g->Lhi);
+    g->inv_csf = (float)g->inv_cs;
+    // FP32 hash error: x rounded (ulp(L)/2) scaled by 1/cs, plus the roundings
+    // of 1/cs and of the product (each ~s 2^-24 cells); 4x that is the guard
+    const double ex = std::ldexp(1.0, std::ilogb(std::max(g->L, 1.0)) - 24) * g->inv_cs +
+                      2.0 * g->s * std::ldexp(1.0, -24);
+    const double guard = 4.0 * ex + 1e-6;
+    g->hash_guard = guard < 0.25 ? (float)guard : 0.5f;  // 0.5: always the FP64 path
     return PSIM_OK;
 }
 
@@ -210,11 +217,12 @@ ForceSetup make_setup(const psim_force_params* p, double L) {
     fs.cal.rc2 = p->cutoff * p->cutoff;
     fs.cal.rc2f = (float)fs.cal.rc2;
     fs.rc_max = max_cutoff(p);
-    // The FP32 prefilter sees positions rounded to FP32 (error <= ulp(L)/2
-    // each, plus the rounding of L and of the difference): bound the error
-    // of a separation by 4 ulp(L) and widen the cutoff by that much.
+    // The FP32 candidate test sees positions rounded to FP32 (ulp(L)/2 each),
+    // L rounded (ulp(L)/2), the imaged home position rounded (ulp(L)) and
+    // the difference rounded: a separation is off by at most ~4.3 ulp(L);
+    // the cutoff is widened by 8 ulp(L).
     double ulpL = std::ldexp(1.0, std::ilogb(std::max(L, 1.0)) - 23);
-    double rpre = fs.rc_max * (1.0 + 1e-6) + 4.0 * ulpL + 1e-6;
+    double rpre = fs.rc_max * (1.0 + 1e-6) + 8.0 * ulpL + 1e-6;
     fs.pre_rc2f = (float)(rpre * rpre * (1.0 + 1e-6));
     return fs;
 }
@@ -554,6 +562,7 @@ int psim_force_evaluate(const psim_force_params* params, const psim_geometry* gm
     PSIM_CUDA(w.tag_out.ensure(4 * n));
     PSIM_CUDA(w.start.ensure(4 * nc));
     PSIM_CUDA(w.count.ensure(4 * nc));
+    PSIM_CUDA(w.scratch.ensure(4 * scan_scratch_ints(g.ncell)));
     PSIM_CUDA(w.fxyz.ensure(24 * n));
     PSIM_CUDA(w.force.ensure(24 * n));
     PSIM_CUDA(w.err.ensure(4));
@@ -567,7 +576,8 @@ int psim_force_evaluate(const psim_force_params* params, const psim_geometry* gm
                                    w.posl.as<float4>(), w.cellid.as<int>(), w.tag_out.as<int>(),
                                    w.err.as<uint32_t>(), st));
     PSIM_CUDA(launch_import_cse(g.ncell, g.n, w.cse.as<uint32_t>(), w.start.as<int>(),
-                                w.count.as<int>(), w.err.as<uint32_t>(), st));
+                                w.count.as<int>(), w.scratch.as<int>(), w.err.as<uint32_t>(),
+                                st));
     // a position outside the grid has no home cell: stop before the force pass
     uint32_t bits = 0;
     PSIM_CUDA(cudaMemcpyAsync(&bits, w.err.p, 4, cudaMemcpyDeviceToHost, st));
@@ -798,7 +808,10 @@ int enqueue_step(psim_system* s, long long t, cudaEvent_t* evs) {
     a.err = s->err.as<uint32_t>();
     a.state = s->state.as<StepState>();
     NoiseView nz{s->cfg.noise_mode, s->noise.as<double>(), s->noise_first, s->noise_steps};
-    PSIM_CUDA(launch_vgb_system(a, s->vp, s->g, nz, st));
+    if (s->cfg.precision == PSIM_PRECISION_FP64)
+        PSIM_CUDA(launch_vgb_system(a, s->vp, s->g, nz, st));
+    else
+        PSIM_CUDA(launch_vgb_system_fast(a, s->vp, s->g, nz, st));
     if (evs) PSIM_CUDA(cudaEventRecord(evs[2], st));
     // rebuild: scan, scatter, canonicalise into the next order
     PSIM_CUDA(launch_scan(s->count[ncb].as<int>(), s->start.as<int>(), s->ncell,

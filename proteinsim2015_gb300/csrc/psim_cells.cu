@@ -269,8 +269,7 @@ cudaError_t launch_import_sorted(int n, const double* sorted, const int32_t* has
 }
 
 __global__ void __launch_bounds__(256)
-import_cse_kernel(int ncell, int n, const uint32_t* cse, int* start, int* count,
-                  uint32_t* err) {
+import_cse_kernel(int ncell, int n, const uint32_t* cse, int* count, uint32_t* err) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= ncell) return;
     const uint32_t s = cse[2 * (size_t)c], e = cse[2 * (size_t)c + 1];
@@ -279,14 +278,28 @@ import_cse_kernel(int ncell, int n, const uint32_t* cse, int* start, int* count,
         atomicOr(err, (uint32_t)EBIT_INDEX);
         empty = true;
     }
-    start[c] = empty ? 0 : (int)s;
     count[c] = empty ? 0 : (int)(e - s);
 }
 
+// Every non-empty cell must start where the counting-sort layout puts it
+// (the layout reorderParticles produces: cells in hash order, back to back).
+__global__ void __launch_bounds__(256)
+check_cse_kernel(int ncell, const uint32_t* cse, const int* start, const int* count,
+                 uint32_t* err) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncell) return;
+    if (count[c] > 0 && cse[2 * (size_t)c] != (uint32_t)start[c])
+        atomicOr(err, (uint32_t)EBIT_INDEX);
+}
+
 cudaError_t launch_import_cse(int ncell, int n, const uint32_t* cse, int* start, int* count,
-                              uint32_t* err, cudaStream_t st) {
+                              int* scratch, uint32_t* err, cudaStream_t st) {
     if (ncell == 0) return cudaSuccess;
-    import_cse_kernel<<<(ncell + 255) / 256, 256, 0, st>>>(ncell, n, cse, start, count, err);
+    const int blocks = (ncell + 255) / 256;
+    import_cse_kernel<<<blocks, 256, 0, st>>>(ncell, n, cse, count, err);
+    cudaError_t e = launch_scan(count, start, ncell, scratch, st);
+    if (e != cudaSuccess) return e;
+    check_cse_kernel<<<blocks, 256, 0, st>>>(ncell, cse, start, count, err);
     return cudaGetLastError();
 }
 

@@ -35,6 +35,8 @@ struct DevGeom {
     double cs;      // cellSize
     double inv_cs;  // 1 / cellSize (fast path of the cell hash)
     float Lhi, Llo; // L as a float pair (Lhi + Llo == L to ~1e-14)
+    float inv_csf;  // 1 / cellSize in FP32 (the FP32 cell hash)
+    float hash_guard; // distance from a cell face (in cells) below which FP64 decides
 };
 
 // floor(x / cs) exactly as the reference computes it (systemHandling.cpp:39-41):
@@ -70,6 +72,19 @@ __device__ __forceinline__ T powi_binary(T base, int e) {  // utilities.cpp:144-
     while (e) {
         if (e & 1) ans *= base;
         e >>= 1;
+        base *= base;
+    }
+    return ans;
+}
+
+// powi_binary with the exponent known at compile time: the same products in
+// the same order (multiplying by the initial 1 is exact), fully unrolled.
+template <int N, typename T>
+__device__ __forceinline__ T powi_fixed(T base) {
+    T ans = T(1);
+#pragma unroll
+    for (int e = N; e; e >>= 1) {
+        if (e & 1) ans *= base;
         base *= base;
     }
     return ans;

@@ -94,6 +94,9 @@ struct VgbSystemArgs {
 };
 cudaError_t launch_vgb_system(const VgbSystemArgs& a, const VgbParams& p, const DevGeom& g,
                               const NoiseView& nz, cudaStream_t st);
+// The same update with FMA contraction (psim_mixed.cu), for the mixed form.
+cudaError_t launch_vgb_system_fast(const VgbSystemArgs& a, const VgbParams& p, const DevGeom& g,
+                                   const NoiseView& nz, cudaStream_t st);
 
 // Reference-layout integrator (brownianIntegrator::nextSystem on AoS arrays
 // in original order).  mem/mem_corr: 3n device arrays owned by the integrator.
@@ -167,9 +170,12 @@ cudaError_t launch_unsort_force(int n, const int* tag, const double* fx, const d
 cudaError_t launch_import_sorted(int n, const double* sorted, const int32_t* hash_index,
                                  const DevGeom& g, double4_32a* posd, float4* posh, float4* posl,
                                  int* cellid, int* tag, uint32_t* err, cudaStream_t st);
-// Ranges beyond n set EBIT_INDEX and are treated as empty.
+// Counts from (start, end) pairs, starts re-derived by a scan (so empty
+// cells keep the back-to-back layout the row walk of the force pass needs);
+// a range beyond n, or a start that disagrees with that layout, sets
+// EBIT_INDEX.  scratch: scan_scratch_ints(ncell) ints.
 cudaError_t launch_import_cse(int ncell, int n, const uint32_t* cse, int* start, int* count,
-                              uint32_t* err, cudaStream_t st);
+                              int* scratch, uint32_t* err, cudaStream_t st);
 // AoS xyz -> three arrays, optionally scattered by tag (gather == 0) or
 // gathered (gather == 1: out[i] = in[tag[i]]).
 cudaError_t launch_split_xyz(int n, const double* aos, const int* tag, int gather, double* x,

@@ -8,16 +8,17 @@
 // with s = 0 or +-L (also a float pair) for a periodic image: the first
 // bracket is exact when the image is applied (Sterbenz), and the rounding of
 // d is then one FP32 rounding of a number of size <= rc, not of the box.
+// The pair loop itself is force_pass_kernel (psim_force.cuh).
 #include <cmath>
 
-#include "psim_kernels.cuh"
+#include "psim_force.cuh"
+#include "psim_vgb.cuh"
 
 namespace psim {
 
 struct ComboPairF {
     AOPair ao;
     LJPair lj;
-    float rc2f;
     __device__ __forceinline__ float fnet32(float r2, float r, float rinv, float size) const {
         float f = 0.0f;
         if (r2 < ao.rc2f) f += ao.fnet32(r2, r, rinv, size);
@@ -33,85 +34,110 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
     s = t;
 }
 
+// One pair (i <- j) in FP32; the drained queue's plain FP32 partial is
+// added to the particle's total with Kahan compensation.
 template <class Pair>
-__global__ void __launch_bounds__(128)
-force_mixed_kernel(Pair pair, float rc2f, DevGeom g, CellView cv, ForceOut out) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= g.n || *out.err) return;
-    const float4 hi = cv.posh[i];
-    const float4 lo = cv.posl[i];
-    const int c = cv.cellid[i];
-    const int cx = c % g.s, cy = (c / g.s) % g.s, cz = c / g.s2;
-    float s0 = 0.f, s1 = 0.f, s2 = 0.f, k0 = 0.f, k1 = 0.f, k2 = 0.f;
-    uint32_t err = 0;
-    for (int dx = -1; dx <= 1; ++dx) {
-        int shx;
-        const int x = wrap_cell(cx + dx, g.s, shx);
-        const float sxh = (float)shx * g.Lhi, sxl = (float)shx * g.Llo;
-        for (int dy = -1; dy <= 1; ++dy) {
-            int shy;
-            const int y = wrap_cell(cy + dy, g.s, shy);
-            const float syh = (float)shy * g.Lhi, syl = (float)shy * g.Llo;
-            for (int dz = -1; dz <= 1; ++dz) {
-                int shz;
-                const int z = wrap_cell(cz + dz, g.s, shz);
-                const float szh = (float)shz * g.Lhi, szl = (float)shz * g.Llo;
-                const int cell = x + g.s * y + g.s2 * z;
-                const int start = cv.cstart[cell];
-                const int end = start + cv.ccount[cell];
-                float p0 = 0.f, p1 = 0.f, p2 = 0.f;
-                for (int j = start; j < end; ++j) {
-                    const float4 hj = __ldg(&cv.posh[j]);
-                    const float4 lj = __ldg(&cv.posl[j]);
-                    const float d0 = ((hj.x + sxh) - hi.x) + ((lj.x + sxl) - lo.x);
-                    const float d1 = ((hj.y + syh) - hi.y) + ((lj.y + syl) - lo.y);
-                    const float d2 = ((hj.z + szh) - hi.z) + ((lj.z + szl) - lo.z);
-                    const float r2 = d0 * d0 + d1 * d1 + d2 * d2;
-                    if (r2 < rc2f && j != i) {
-                        const float rinv = rsqrtf(r2);
-                        const float r = r2 * rinv;
-                        const float size = hi.w + hj.w;
-                        if (r < 0.8f * size) err |= EBIT_OVERLAP;
-                        const float f = pair.fnet32(r2, r, rinv, size) * rinv;
-                        p0 += f * d0;
-                        p1 += f * d1;
-                        p2 += f * d2;
-                    }
-                }
-                kahan_add(s0, k0, p0);
-                kahan_add(s1, k1, p1);
-                kahan_add(s2, k2, p2);
-            }
+struct MixedBody {
+    Pair pf;
+    float rc2f;
+    struct Home {
+        float4 lo;
+    };
+    struct Acc {
+        float s0, s1, s2, k0, k1, k2, p0, p1, p2;
+    };
+    __device__ __forceinline__ void init(Acc& a) const {
+        a.s0 = a.s1 = a.s2 = a.k0 = a.k1 = a.k2 = a.p0 = a.p1 = a.p2 = 0.f;
+    }
+    __device__ __forceinline__ void load_home(const CellView& cv, int i, Home& h) const {
+        h.lo = cv.posl[i];
+    }
+    __device__ __forceinline__ void eval(const DevGeom& g, const CellView& cv, const Home& h,
+                                         const float4& hi, uint32_t e, Acc& a,
+                                         uint32_t& err) const {
+        const int j = (int)(e & kIndexMask);
+        const float4 hj = __ldg(&cv.posh[j]);
+        const float4 lj = __ldg(&cv.posl[j]);
+        float d0, d1, d2;
+        if ((e >> 27) == kNoImage) {  // the common case: no periodic image
+            d0 = (hj.x - hi.x) + (lj.x - h.lo.x);
+            d1 = (hj.y - hi.y) + (lj.y - h.lo.y);
+            d2 = (hj.z - hi.z) + (lj.z - h.lo.z);
+        } else {
+            int sx, sy, sz;
+            decode_image(e, sx, sy, sz);
+            d0 = ((hj.x + (float)sx * g.Lhi) - hi.x) + ((lj.x + (float)sx * g.Llo) - h.lo.x);
+            d1 = ((hj.y + (float)sy * g.Lhi) - hi.y) + ((lj.y + (float)sy * g.Llo) - h.lo.y);
+            d2 = ((hj.z + (float)sz * g.Lhi) - hi.z) + ((lj.z + (float)sz * g.Llo) - h.lo.z);
+        }
+        const float r2 = d0 * d0 + d1 * d1 + d2 * d2;
+        if (r2 < rc2f) {
+            const float rinv = rsqrtf(r2);
+            const float r = r2 * rinv;
+            const float size = hi.w + hj.w;
+            if (r < 0.8f * size) err |= EBIT_OVERLAP;
+            const float f = pf.fnet32(r2, r, rinv, size) * rinv;
+            a.p0 += f * d0;
+            a.p1 += f * d1;
+            a.p2 += f * d2;
         }
     }
-    out.fx[i] = (double)s0 - (double)k0;
-    out.fy[i] = (double)s1 - (double)k1;
-    out.fz[i] = (double)s2 - (double)k2;
-    if (err) atomicOr(out.err, err);
-}
+    __device__ __forceinline__ void fold(Acc& a) const {
+        kahan_add(a.s0, a.k0, a.p0);
+        kahan_add(a.s1, a.k1, a.p1);
+        kahan_add(a.s2, a.k2, a.p2);
+        a.p0 = a.p1 = a.p2 = 0.f;
+    }
+    __device__ __forceinline__ void store(const ForceOut& out, int i, const Acc& a) const {
+        out.fx[i] = (double)a.s0 - (double)a.k0;
+        out.fy[i] = (double)a.s1 - (double)a.k1;
+        out.fz[i] = (double)a.s2 - (double)a.k2;
+    }
+};
 
 template <class Pair>
 static cudaError_t run_mixed(const Pair& p, float rc2f, const DevGeom& g, const CellView& cv,
-                             const ForceOut& out, cudaStream_t st) {
-    if (g.n == 0) return cudaSuccess;
-    const int bs = 128;
-    force_mixed_kernel<Pair><<<(g.n + bs - 1) / bs, bs, 0, st>>>(p, rc2f, g, cv, out);
-    return cudaGetLastError();
+                             const ForceOut& out, float pre, cudaStream_t st) {
+    return launch_force_pass(MixedBody<Pair>{p, rc2f}, g, cv, out, pre, st);
+}
+
+template <int N>
+static cudaError_t run_lj_mixed(const LJPair& lj, const DevGeom& g, const CellView& cv,
+                                const ForceOut& out, float pre, cudaStream_t st) {
+    LJFixed<N> p;
+    static_cast<LJPair&>(p) = lj;
+    return run_mixed(p, lj.rc2f, g, cv, out, pre, st);
 }
 
 cudaError_t launch_forces_mixed(const ForceSetup& fs, const DevGeom& g, const CellView& cv,
                                 const ForceOut& out, cudaStream_t st) {
+    const float pre = fs.pre_rc2f;
     switch (fs.kind) {
-    case 1: return run_mixed(fs.ao, fs.ao.rc2f, g, cv, out, st);
-    case 2: return run_mixed(fs.lj, fs.lj.rc2f, g, cv, out, st);
-    case 3: return run_mixed(fs.cal, fs.cal.rc2f, g, cv, out, st);
+    case 1: return run_mixed(fs.ao, fs.ao.rc2f, g, cv, out, pre, st);
+    case 2:
+        switch (fs.lj.n) {
+        case 0: return run_lj_mixed<0>(fs.lj, g, cv, out, pre, st);
+        case 6: return run_lj_mixed<6>(fs.lj, g, cv, out, pre, st);
+        case 12: return run_lj_mixed<12>(fs.lj, g, cv, out, pre, st);
+        case 18: return run_lj_mixed<18>(fs.lj, g, cv, out, pre, st);
+        default: return run_mixed(fs.lj, fs.lj.rc2f, g, cv, out, pre, st);
+        }
+    case 3: return run_mixed(fs.cal, fs.cal.rc2f, g, cv, out, pre, st);
     case 4: {
-        float rc2f = fs.ao.rc2f > fs.lj.rc2f ? fs.ao.rc2f : fs.lj.rc2f;
-        ComboPairF cp{fs.ao, fs.lj, rc2f};
-        return run_mixed(cp, rc2f, g, cv, out, st);
+        const float rc2f = fs.ao.rc2f > fs.lj.rc2f ? fs.ao.rc2f : fs.lj.rc2f;
+        return run_mixed(ComboPairF{fs.ao, fs.lj}, rc2f, g, cv, out, pre, st);
     }
     }
     return cudaErrorInvalidValue;
+}
+
+// The update of the mixed form: the same FP64 arithmetic as psim_exact.cu's
+// instance, with a*b+c contracted into FMA by this translation unit.
+cudaError_t launch_vgb_system_fast(const VgbSystemArgs& a, const VgbParams& p, const DevGeom& g,
+                                   const NoiseView& nz, cudaStream_t st) {
+    if (a.n == 0) return cudaSuccess;
+    vgb_system_kernel<VgbFast><<<(a.n + 255) / 256, 256, 0, st>>>(a, p, g, nz);
+    return cudaGetLastError();
 }
 
 }  // namespace psim

@@ -1,0 +1,252 @@
+// psim_vgb.cuh -- the van Gunsteren-Berendsen update (brownianIntegrator.cpp:
+// 181-356) with the periodic wrap (particle.cpp:61-99, utilities.cpp:26-50)
+// and the cell hash of the next rebuild (systemHandling.cpp:33-48).
+//
+// Included by two translation units: psim_exact.cu (built with --fmad=false:
+// the plain form, every product and sum rounded separately in the reference's
+// order) and psim_mixed.cu (FMA contraction allowed: the update of the mixed
+// form, still FP64).  The Tag template argument keeps the two instances apart.
+//
+// GB300 issues FP64 arithmetic at 1/64 of the FP32 rate, so only the update's
+// own arithmetic is FP64: sign and range tests of the wrap read the IEEE bit
+// patterns as integers (same order as the floating-point comparison for the
+// values involved), the wrap's additions sit behind warp-uniform branches
+// (almost no particle crosses the box in one step), and the cell hash is
+// computed in FP32 unless the position lies within a guard band of a cell
+// face (a few times the FP32 error of the hash), where the FP64 division of
+// the reference decides.
+#pragma once
+
+#include "psim_kernels.cuh"
+
+namespace psim {
+
+struct VgbExact {};
+struct VgbFast {};
+
+// v < 0 for a non-NaN double: sign bit set and not -0.0
+__device__ __forceinline__ bool neg_d(double v) {
+    const long long b = __double_as_longlong(v);
+    return b < 0 && b != (long long)0x8000000000000000ull;
+}
+// v >= base for v >= +0 and base > 0 (a positive NaN counts as >= base)
+__device__ __forceinline__ bool ge_pos_d(double v, double base) {
+    return __double_as_longlong(v) >= __double_as_longlong(base);
+}
+// |d| > h for h > 0
+__device__ __forceinline__ bool abs_gt_d(double d, double h) {
+    return (__double_as_longlong(d) & 0x7fffffffffffffffll) > __double_as_longlong(h);
+}
+
+// One particle of nextSystem (see the file comment).  x/x0: current position
+// and previous position; mx: memX/Y/Z in, new memX/Y/Z out; F/F0: pushed
+// forces; v: velocity in/out; xi: 6 Gaussians in draw order.  Writes the
+// wrapped new position xn and the re-imaged previous position x0n.
+__device__ __forceinline__ void vgb_particle(const VgbParams& p, double L, double half_L,
+                                             bool first, bool vel_step, const double x[3],
+                                             const double x0[3], double mx[3], double mc[3],
+                                             const double F[3], const double F0[3], double v[3],
+                                             const double xi[6], double m, double xn[3],
+                                             double x0n[3], uint32_t& err) {
+    double nw[3];
+    if (first) {  // firstStep, brownianIntegrator.cpp:191-223 (G&B eq. 2.26)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            mc[k] = 0.0;
+            mx[k] = xi[k];
+            nw[k] = x[k] + (v[k] * p.coeff1 * p.dt) + (F[k] * p.coeff3 * p.dt * p.dt * m)
+                    + (p.sig1 * mx[k]);
+        }
+    } else {      // normalStep, brownianIntegrator.cpp:225-296
+        const double c1 = m * p.dt2 * p.coeff1;
+        const double c2 = m * p.dt2 * p.coeff2;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            mc[k] = p.sig2 * ((p.corr * mx[k]) + (p.dev * xi[k]));
+            mx[k] = xi[3 + k];
+            double t = (p.c0 * x[k]);
+            t -= (p.coeff0 * x0[k]);
+            t += (c1 * F[k]);
+            t += (c2 * (F[k] - F0[k]));
+            t += (p.sig1 * mx[k]) + (p.coeff0 * mc[k]);
+            nw[k] = t;
+        }
+    }
+    // safeMod (one +-L), then safeMod0 re-images the old position next to the
+    // new one (particle::setX/Y/Z, particle.cpp:61-92)
+    bool lo[3], hi[3];
+    bool any = false;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        lo[k] = neg_d(nw[k]);
+        hi[k] = !lo[k] && ge_pos_d(nw[k], L);
+        any |= lo[k] | hi[k];
+        xn[k] = nw[k];
+    }
+    if (__any_sync(__activemask(), any)) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            if (lo[k]) xn[k] = nw[k] + L;
+            else if (hi[k]) xn[k] = nw[k] - L;
+        }
+    }
+    bool far[3];
+    any = false;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        far[k] = abs_gt_d(xn[k] - x[k], half_L);
+        any |= far[k];
+        x0n[k] = x[k];
+    }
+    if (__any_sync(__activemask(), any)) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+            if (far[k]) x0n[k] = (xn[k] - x[k] < 0) ? x[k] - L : x[k] + L;
+    }
+    if (vel_step) {  // velocityStep, brownianIntegrator.cpp:298-356
+        const double g2 = m * p.dt2 * p.goy2;
+        const double g3 = m * p.dt3 * p.goy3;
+        const double g4 = p.hn * p.dt_inv;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const double d0 = x[k] - x0[k];
+            double vv = (xn[k] - x0n[k]) + d0;  // the new position's wrap and re-image
+            vv += (g2 * F[k]);
+            vv -= (g3 * (F[k] - F0[k]));
+            vv += (mc[k] - p.sig1 * mx[k]);
+            vv *= g4;
+            v[k] = vv;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        // the reference exits with 7703 when the wrapped value is outside
+        // [0, L) (particle.cpp:67-69); a NaN coordinate is flagged too
+        const bool inside = !neg_d(xn[k]) && !ge_pos_d(xn[k], L) && (xn[k] == xn[k]);
+        if (!inside) err |= EBIT_BOUNDS;
+    }
+}
+
+// floor(x / cs) as the reference computes it (systemHandling.cpp:39-41).
+__device__ __forceinline__ int cell_coord_fast(double x, const DevGeom& g) {
+    const float q = __double2float_rn(x) * g.inv_csf;
+    const float f = floorf(q);
+    const float fr = q - f;
+    if (fr > g.hash_guard && fr < 1.0f - g.hash_guard) return (int)f;
+    return cell_coord(x, g);
+}
+
+__device__ __forceinline__ int hash_pos(const double xn[3], const DevGeom& g, uint32_t& err) {
+    int c[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        int q = cell_coord_fast(xn[k], g);
+        if (q < 0 || q >= g.s) {
+            err |= EBIT_CELL;
+            q = q < 0 ? 0 : g.s - 1;
+        }
+        c[k] = q;
+    }
+    return c[0] + g.s * c[1] + g.s2 * c[2];  // systemHandling.cpp:43
+}
+
+__device__ __forceinline__ void load_noise(const NoiseView& nz, uint32_t seed, int n, int tag,
+                                           long long step, double xi[6], uint32_t& err) {
+    if (nz.mode == 1) {
+        const long long idx = step - nz.first;
+        if (idx < 0 || idx >= nz.n_steps) {
+            err |= EBIT_NOISE;
+#pragma unroll
+            for (int k = 0; k < 6; ++k) xi[k] = 0.0;
+            return;
+        }
+        const double* b = nz.buf + ((size_t)idx * (size_t)n + (size_t)tag) * 6;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) xi[k] = b[k];
+    } else {
+        philox_gaussians6(seed, (uint32_t)tag, (uint32_t)step, xi);
+    }
+}
+
+// The system-order update: gathers the previous state through perm, writes
+// the new state in the current cell order, and hashes + counts the new
+// positions into the next grid.
+template <class Tag>
+__global__ void __launch_bounds__(256)
+vgb_system_kernel(VgbSystemArgs a, VgbParams p, DevGeom g, NoiseView nz) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= a.n || *a.err) return;
+    const long long step = a.state->step;
+    const int vc = a.state->vel_counter;
+    const bool first = (step == 0);
+    const bool vel_step = !first && (p.vel_freq == 0 || vc == p.vel_freq);
+    const int o = a.perm[f];
+    const int tag = a.tag[f];
+    const double m = a.inv_mass[f];
+    uint32_t err = 0;
+    const double x[3] = {a.x[o], a.y[o], a.z[o]};
+    const double x0[3] = {a.x0[o], a.y0[o], a.z0[o]};
+    double mx[3] = {a.mx[o], a.my[o], a.mz[o]};
+    const double F[3] = {a.fx[f], a.fy[f], a.fz[f]};
+    const double F0[3] = {a.gx[o], a.gy[o], a.gz[o]};
+    double v[3] = {0.0, 0.0, 0.0};
+    if (first || vel_step) {
+        v[0] = a.vel[3 * (size_t)tag];
+        v[1] = a.vel[3 * (size_t)tag + 1];
+        v[2] = a.vel[3 * (size_t)tag + 2];
+    }
+    double xi[6];
+    load_noise(nz, p.seed, a.n, tag, step, xi, err);
+    double mc[3], xn[3], x0n[3];
+    vgb_particle(p, g.L, g.half, first, vel_step, x, x0, mx, mc, F, F0, v, xi, m, xn, x0n, err);
+    a.ox[f] = xn[0]; a.oy[f] = xn[1]; a.oz[f] = xn[2];
+    a.ox0[f] = x0n[0]; a.oy0[f] = x0n[1]; a.oz0[f] = x0n[2];
+    a.omx[f] = mx[0]; a.omy[f] = mx[1]; a.omz[f] = mx[2];
+    if (vel_step) {
+        a.vel[3 * (size_t)tag] = v[0];
+        a.vel[3 * (size_t)tag + 1] = v[1];
+        a.vel[3 * (size_t)tag + 2] = v[2];
+    }
+    const int key = hash_pos(xn, g, err);
+    a.key[f] = key;
+    a.rank[f] = atomicAdd(&a.count[key], 1);
+    if (err) atomicOr(a.err, err);
+}
+
+// nextSystem on the reference's own AoS arrays in original order.
+template <class Tag>
+__global__ void __launch_bounds__(256) vgb_aos_kernel(VgbAosArgs a, VgbParams p, double L) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    uint32_t err = 0;
+    double x[3], x0[3], mx[3], F[3], F0[3], v[3], xi[6], mc[3], xn[3], x0n[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        x[k] = a.pos[3 * (size_t)i + k];
+        x0[k] = a.pos0[3 * (size_t)i + k];
+        mx[k] = a.mem[3 * (size_t)i + k];
+        F[k] = a.frc[3 * (size_t)i + k];
+        F0[k] = a.frc0[3 * (size_t)i + k];
+        v[k] = a.vel[3 * (size_t)i + k];
+    }
+    if (a.noise) {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) xi[k] = a.noise[6 * (size_t)i + k];
+    } else {
+        philox_gaussians6(a.seed, (uint32_t)i, (uint32_t)a.philox_step, xi);
+    }
+    const double m = 1.0 / a.mass[i];
+    vgb_particle(p, L, L / 2, a.first != 0, a.vel_step != 0, x, x0, mx, mc, F, F0, v, xi, m, xn,
+                 x0n, err);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        a.pos[3 * (size_t)i + k] = xn[k];
+        a.pos0[3 * (size_t)i + k] = x0n[k];
+        a.mem[3 * (size_t)i + k] = mx[k];
+        a.mem_corr[3 * (size_t)i + k] = mc[k];
+        if (a.vel_step) a.vel[3 * (size_t)i + k] = v[k];
+    }
+    if (err) atomicOr(a.err, err);
+}
+
+}  // namespace psim

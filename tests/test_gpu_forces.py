@@ -85,3 +85,41 @@ def test_empty_and_single_particle(psim):
     hi, cse, srt = psim.cells_build(g, np.array([5.0, 5.0, 5.0]), np.full(1, 0.5))
     f = psim.force_evaluate(psim.make_force("AO", 1.1, well_depth=1.0), g, srt, hi, cse)
     assert np.array_equal(f, np.zeros(3))
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_sparse_grid_with_empty_cells(psim, precision):
+    # 0.5 particles per cell: most rows cross empty cells, whose sentinel
+    # start must not break the contiguous row walk
+    n, box, scale = 500, 30.0, 10
+    pos, rad = rsa_state(n, box, seed=12)
+    g = psim.geometry(n, box, box / scale, scale)
+    p = psim.make_force("AO", 1.1, kT=1.0, well_depth=2.0)
+    hi, cse, srt, ref, err, sc = oracle_force(p.as_dict(), g, pos, rad)
+    assert err == 0 and np.sum(cse == 0xFFFFFFFF) > 0
+    f = psim.force_evaluate(p, g, srt, hi, cse, precision=precision)
+    if precision == 0:
+        assert rel_per_particle(f, ref, sc) <= FORCE_TOL_FP64
+    else:
+        assert rel_norm(f, ref) <= FORCE_TOL_MIXED
+
+
+def test_malformed_cell_list_is_refused(psim):
+    n, box, scale = 300, 12.0, 4
+    pos, rad = rsa_state(n, box, seed=13)
+    g = psim.geometry(n, box, box / scale, scale)
+    hi, cse, srt = psim.cells_build(g, pos, rad)
+    p = psim.make_force("AO", 1.1, well_depth=1.0)
+    bad_tag = hi.copy()
+    bad_tag[1] = n + 5                        # an original index beyond n
+    bad_end = cse.copy()
+    k = int(np.flatnonzero(cse[0::2] != 0xFFFFFFFF)[0])
+    bad_end[2 * k + 1] = n + 100              # a cell range beyond the list
+    bad_start = cse.copy()
+    nz = np.flatnonzero(cse[0::2] != 0xFFFFFFFF)
+    bad_start[2 * nz[3]] += 1                 # a start off the counting-sort layout
+    bad_start[2 * nz[3] + 1] += 1
+    for h, c in ((bad_tag, cse), (hi, bad_end), (hi, bad_start)):
+        with pytest.raises(psim.PsimError) as e:
+            psim.force_evaluate(p, g, srt, h, c)
+        assert e.value.code == psim.ERR_INPUT
