@@ -35,27 +35,33 @@ struct ComboPair {  // AO + LJ(n) summed; each part inside its own cutoff
 // pbcDist's |dx| > L/2.0 for r^2 (utilities.cpp:79-104) and unitVectorAdv's
 // |dx| > int(L)/2 for the unit vector (utilities.cpp:114-142), the overlap
 // check (AOPotential.cpp:83-88) and, for AO, the NaN check (:105-109).
-// Partial sums are folded into the total when a queue drains, as the
-// reference folds each cell's partial (AOPotential.cpp:165-167).
+// Each row's partial sum is folded into the total, as the reference folds
+// each cell's partial (AOPotential.cpp:165-167).
 template <class Pair>
 struct F64Body {
     Pair pf;
+    using Aux = double4_32a;  // the FP64 neighbour positions {x, y, z, R}
     struct Home {
         double4_32a p;
     };
+    using Shifted = Home;     // the FP64 form takes raw differences
     struct Acc {
         double n0, n1, n2, c0, c1, c2;
     };
+    __device__ __forceinline__ const Aux* aux(const CellView& cv) const { return cv.posd; }
     __device__ __forceinline__ void init(Acc& a) const {
         a.n0 = a.n1 = a.n2 = a.c0 = a.c1 = a.c2 = 0.0;
     }
     __device__ __forceinline__ void load_home(const CellView& cv, int i, Home& h) const {
         h.p = cv.posd[i];
     }
-    __device__ __forceinline__ void eval(const DevGeom& g, const CellView& cv, const Home& h,
-                                         const float4&, uint32_t e, Acc& a, uint32_t& err) const {
-        const int j = (int)(e & kIndexMask);
-        const double4_32a pj = cv.posd[j];
+    __device__ __forceinline__ void shift(const Home& h, const float4&, int, int, int,
+                                          const DevGeom&, Shifted& o) const {
+        o = h;
+    }
+    __device__ __forceinline__ void eval(const float4&, const double4_32a& pj, const Home& h,
+                                         Acc& a, uint32_t& err) const {
+        const DevGeom& g = geom;
         double d0 = pj.x - h.p.x, d1 = pj.y - h.p.y, d2 = pj.z - h.p.z;
         double a0 = fabs(d0), a1 = fabs(d1), a2 = fabs(d2);
         if (a0 > g.half) a0 -= g.L;
@@ -88,12 +94,13 @@ struct F64Body {
         out.fy[i] = a.n1;
         out.fz[i] = a.n2;
     }
+    DevGeom geom;
 };
 
 template <class Pair>
 static cudaError_t run_fp64(const Pair& p, const DevGeom& g, const CellView& cv,
                             const ForceOut& out, float pre, cudaStream_t st) {
-    return launch_force_pass(F64Body<Pair>{p}, g, cv, out, pre, st);
+    return launch_force_pass(F64Body<Pair>{p, g}, g, cv, out, pre, st);
 }
 
 template <int N>

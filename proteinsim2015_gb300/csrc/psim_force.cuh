@@ -6,56 +6,63 @@
 // ~15% of those candidates are inside the cutoff, so a thread-per-particle
 // loop that evaluates the pair force under a branch runs the pair body in
 // almost every iteration with a few lanes active.  Here each warp owns 32
-// consecutive sorted particles and works in two phases:
+// consecutive sorted particles and walks the 27 cells as 9 rows of 3
+// x-adjacent cells: in the sorted list a row is one contiguous run (the x-wrap
+// at the box edge adds a second, one-cell run).  For each row:
 //
-//   A. candidate test: the 27 cells are walked as 9 rows of 3 x-adjacent
-//      cells, each row a contiguous run of the sorted particle list (two runs
-//      when the row wraps around the box).  Each lane tests its own row with
-//      an FP32 distance on the rounded positions (a margin covers their
-//      rounding) and appends in-range candidates (index + periodic image) to
-//      its own queue in shared memory.  Loop bounds are warp-uniform (the
-//      longest run of the warp), so there is no divergent control flow.
-//   B. pair forces: when a queue fills (and at the end) every lane drains its
-//      own queue with the plugin's pair body; lanes stay busy because each
-//      holds ~a queue's worth of pairs, and each lane sums only its own
-//      particle's force, so no atomics or reductions are needed.
+//   stage  the union of the 32 lanes' runs (~5 cells, ~70 particles) is
+//          copied into shared memory with coalesced 16-byte loads;
+//   A      each lane tests its own run from shared memory with an FP32
+//          distance on the rounded positions (a margin covers their rounding)
+//          and appends in-range candidates to its own queue -- branch-free:
+//          every candidate is written to the next free slot and only an
+//          in-range one advances the count; loop bounds are warp-uniform;
+//   B      every lane drains its own queue with the plugin's pair body, so
+//          each lane sums only its own particle's force (no atomics).
+//
+// The row's periodic image is folded into a per-lane shifted home position,
+// so neither phase handles images per pair.  Runs that wrap around the box
+// in x, and unions too long for the stage, are read from global memory.
 //
 // Body supplies the precision-specific parts (psim_exact.cu: FP64 plain form
 // with the reference's image rules; psim_mixed.cu: FP32 pairs with Kahan
 // sums).
 #pragma once
 
+#include <climits>
+
 #include "psim_kernels.cuh"
 
 namespace psim {
 
-constexpr int kForceWarps = 4;              // warps per block
-constexpr int kQueue = 48;                  // drain when a lane holds this many
-constexpr int kUnroll = 4;                  // candidates tested between drains
-constexpr int kQueueCap = kQueue + kUnroll; // slots per lane
-constexpr uint32_t kIndexMask = (1u << 27) - 1u;  // queue entry: j | image << 27
-constexpr uint32_t kNoImage = 13u;                // (0, 0, 0)
-
-// n < 2^27 particles so a queue entry packs the index with the image code
-// ((sx+1) + 3(sy+1) + 9(sz+1), 0..26).
-__device__ __forceinline__ void decode_image(uint32_t e, int& sx, int& sy, int& sz) {
-    const int code = (int)(e >> 27);
-    sx = code % 3 - 1;
-    sy = (code / 3) % 3 - 1;
-    sz = code / 9 - 1;
-}
+constexpr int kForceWarps = 4;                // warps per block
+constexpr int kStage = 96;                    // staged particles per warp and row
+constexpr int kQueue = 20;                    // drain when a lane holds this many
+constexpr int kUnroll = 4;                    // candidates tested between drain checks
+constexpr int kQueueCap = kQueue + kUnroll;   // slots per lane
+// A lane reads its run at stage[rel + t] for t < (longest run of the warp,
+// rounded up to kUnroll); rel + len <= union length <= kStage, so reads stay
+// below 2 kStage + kUnroll.  Slots past the union hold stale data that the
+// t < len test masks.
+constexpr int kStagePad = 2 * kStage + kUnroll;
 
 template <class Body>
 __global__ void __launch_bounds__(kForceWarps * 32)
 force_pass_kernel(Body body, DevGeom g, CellView cv, ForceOut out, float pre_rc2) {
-    __shared__ uint32_t queue[kForceWarps][kQueueCap][32];
+    using Aux = typename Body::Aux;
+    __shared__ float4 s_hi[kForceWarps][kStagePad];
+    __shared__ Aux s_aux[kForceWarps][kStage];
+    __shared__ uint32_t s_q[kForceWarps][kQueueCap][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     // an error latched by an earlier kernel stops the pass; read once and
     // broadcast so every lane of the warp takes the same path
     const bool failed = __shfl_sync(0xffffffffu, (lane == 0) ? (*out.err != 0) : false, 0);
     const bool active = (i < g.n) && !failed;
-    uint32_t (*q)[32] = queue[w];
+    float4* st_hi = s_hi[w];
+    Aux* st_aux = s_aux[w];
+    uint32_t (*q)[32] = s_q[w];
+    const Aux* g_aux = body.aux(cv);
 
     float4 hi = make_float4(0.f, 0.f, 0.f, 0.f);
     int cx = 0, cy = 0, cz = 0;
@@ -72,16 +79,7 @@ force_pass_kernel(Body body, DevGeom g, CellView cv, ForceOut out, float pre_rc2
     }
     uint32_t err = 0;
     int cnt = 0;
-
-    auto drain = [&]() {
-        const int kmax = __reduce_max_sync(0xffffffffu, cnt);
-        for (int k = 0; k < kmax; ++k) {
-            if (k < cnt) body.eval(g, cv, home, hi, q[k][lane], acc, err);
-        }
-        body.fold(acc);
-        cnt = 0;
-        __syncwarp();
-    };
+    const int jlast = g.n - 1;
 
     for (int row = 0; row < 9; ++row) {
         const int dy = row / 3 - 1, dz = row % 3 - 1;
@@ -110,32 +108,80 @@ force_pass_kernel(Body body, DevGeom g, CellView cv, ForceOut out, float pre_rc2
             const int lmax = __reduce_max_sync(0xffffffffu, len);
             if (lmax == 0) continue;
             // the image is applied to the home position: d = x_j - (x_i - s L)
+            typename Body::Shifted hs;
+            body.shift(home, hi, sx, sy, sz, g, hs);
             const float hx = hi.x - (float)sx * g.Lhi;
             const float hy = hi.y - (float)sy * g.Lhi;
             const float hz = hi.z - (float)sz * g.Lhi;
-            const uint32_t img = (uint32_t)((sx + 1) + 3 * (sy + 1) + 9 * (sz + 1)) << 27;
-            // Branch-free test: the load index is clamped into the list (the
-            // tail of a shorter run reads a valid particle and is masked out),
-            // every candidate is written to the next free slot and only an
-            // in-range one advances the counter.
-            const int jlast = g.n - 1;
-            for (int t0 = 0; t0 < lmax; t0 += kUnroll) {
-#pragma unroll
-                for (int u = 0; u < kUnroll; ++u) {
-                    const int t = t0 + u;
-                    const int j = a + t;
-                    const float4 hj = __ldg(&cv.posh[min(j, jlast)]);
-                    const float ex = hj.x - hx, ey = hj.y - hy, ez = hj.z - hz;
-                    const float r2 = ex * ex + ey * ey + ez * ez;
-                    const bool in = (t < len) & (r2 < pre_rc2) & (j != i);
-                    q[cnt][lane] = (uint32_t)j | img;
-                    cnt += in ? 1 : 0;
+            const int u0 = __reduce_min_sync(0xffffffffu, len > 0 ? a : INT_MAX);
+            const int u1 = __reduce_max_sync(0xffffffffu, len > 0 ? a + len : 0);
+            const int ulen = u1 - u0;
+            if (part == 0 && ulen <= kStage) {
+                for (int k = lane; k < ulen; k += 32) {
+                    st_hi[k] = cv.posh[u0 + k];
+                    st_aux[k] = g_aux[u0 + k];
                 }
-                if (__any_sync(0xffffffffu, cnt >= kQueue)) drain();
+                __syncwarp();
+                const int rel = len > 0 ? a - u0 : 0;
+                // candidate t of this lane is stage[rel + t]; it is the home
+                // particle itself when rel + t == i - u0
+                const int dself = (i >= u0 && i < u1) ? rel - (i - u0) : INT_MIN / 2;
+                const float4* sp = st_hi + rel;
+                uint32_t* qp = &q[0][lane];
+                uint32_t* const qlim = &q[kQueue][lane];
+                for (int t0 = 0; t0 < lmax; t0 += kUnroll, sp += kUnroll) {
+                    const int rem = len - t0;      // candidate u is in the run iff u < rem
+                    const int ds = dself + t0;     // candidate u is the home iff ds + u == 0
+#pragma unroll
+                    for (int u = 0; u < kUnroll; ++u) {
+                        const float4 hj = sp[u];
+                        const float ex = hj.x - hx, ey = hj.y - hy, ez = hj.z - hz;
+                        const float r2 = ex * ex + ey * ey + ez * ez;
+                        const bool in = (u < rem) & (r2 < pre_rc2) & (ds + u != 0);
+                        *qp = (uint32_t)(rel + t0 + u);
+                        qp += in ? 32 : 0;
+                    }
+                    if (__any_sync(0xffffffffu, qp >= qlim) || t0 + kUnroll >= lmax) {
+                        const int n_in = (int)(qp - &q[0][lane]) >> 5;
+                        const int kmax = __reduce_max_sync(0xffffffffu, n_in);
+                        for (int k = 0; k < kmax; ++k) {
+                            if (k < n_in) {
+                                const uint32_t sidx = q[k][lane];
+                                body.eval(st_hi[sidx], st_aux[sidx], hs, acc, err);
+                            }
+                        }
+                        qp = &q[0][lane];
+                    }
+                }
+                __syncwarp();  // the stage is rewritten by the next row
+            } else {
+                for (int t0 = 0; t0 < lmax; t0 += kUnroll) {
+#pragma unroll
+                    for (int u = 0; u < kUnroll; ++u) {
+                        const int t = t0 + u;
+                        const int j = min(a + t, jlast);
+                        const float4 hj = __ldg(&cv.posh[j]);
+                        const float ex = hj.x - hx, ey = hj.y - hy, ez = hj.z - hz;
+                        const float r2 = ex * ex + ey * ey + ez * ez;
+                        const bool in = (t < len) & (r2 < pre_rc2) & (j != i);
+                        q[cnt][lane] = (uint32_t)j;
+                        cnt += in ? 1 : 0;
+                    }
+                    if (__any_sync(0xffffffffu, cnt >= kQueue) || t0 + kUnroll >= lmax) {
+                        const int kmax = __reduce_max_sync(0xffffffffu, cnt);
+                        for (int k = 0; k < kmax; ++k) {
+                            if (k < cnt) {
+                                const uint32_t j2 = q[k][lane];
+                                body.eval(__ldg(&cv.posh[j2]), g_aux[j2], hs, acc, err);
+                            }
+                        }
+                        cnt = 0;
+                    }
+                }
             }
+            body.fold(acc);
         }
     }
-    drain();
     if (active) body.store(out, i, acc);
     if (err) atomicOr(out.err, err);
 }
@@ -144,7 +190,6 @@ template <class Body>
 cudaError_t launch_force_pass(const Body& body, const DevGeom& g, const CellView& cv,
                               const ForceOut& out, float pre_rc2, cudaStream_t st) {
     if (g.n == 0) return cudaSuccess;
-    if (g.n >= (1 << 27)) return cudaErrorInvalidValue;
     const int threads = kForceWarps * 32;
     force_pass_kernel<Body><<<(g.n + threads - 1) / threads, threads, 0, st>>>(body, g, cv, out,
                                                                               pre_rc2);

@@ -3,11 +3,12 @@
 // Pair forces are computed in FP32 and summed in FP32 with Kahan-compensated
 // per-particle totals; the update, wrap and coefficients stay FP64 (in
 // psim_exact.cu).  Positions are carried as FP32 pairs (hi + lo == the FP64
-// position to ~1e-14), so a pair separation is
-//     d = ((x_j,hi + s_hi) - x_i,hi) + ((x_j,lo + s_lo) - x_i,lo)
-// with s = 0 or +-L (also a float pair) for a periodic image: the first
-// bracket is exact when the image is applied (Sterbenz), and the rounding of
-// d is then one FP32 rounding of a number of size <= rc, not of the box.
+// position to ~1e-14).  For a row of cells the home position minus the
+// row's periodic image (0 or +-L, L itself a float pair) is formed exactly
+// as a float pair (h, l) by TwoSum, and a pair separation is
+//     d = (x_j,hi - h) + (x_j,lo - l)
+// where the first difference is exact for nearby values (Sterbenz), so d
+// carries one FP32 rounding of a number of size <= rc, not of the box.
 // The pair loop itself is force_pass_kernel (psim_force.cuh).
 #include <cmath>
 
@@ -34,47 +35,58 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
     s = t;
 }
 
-// One pair (i <- j) in FP32; the drained queue's plain FP32 partial is
-// added to the particle's total with Kahan compensation.
+// Knuth's TwoSum: s + e == a + b exactly.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// One pair (i <- j) in FP32; each row's plain FP32 partial is added to the
+// particle's total with Kahan compensation.
 template <class Pair>
 struct MixedBody {
     Pair pf;
     float rc2f;
+    using Aux = float4;  // the low parts of the neighbour positions
     struct Home {
         float4 lo;
+    };
+    struct Shifted {     // home position minus the row's image, as a float pair
+        float4 h;        // xyz: high part, w: radius
+        float lx, ly, lz;
     };
     struct Acc {
         float s0, s1, s2, k0, k1, k2, p0, p1, p2;
     };
+    __device__ __forceinline__ const Aux* aux(const CellView& cv) const { return cv.posl; }
     __device__ __forceinline__ void init(Acc& a) const {
         a.s0 = a.s1 = a.s2 = a.k0 = a.k1 = a.k2 = a.p0 = a.p1 = a.p2 = 0.f;
     }
     __device__ __forceinline__ void load_home(const CellView& cv, int i, Home& h) const {
         h.lo = cv.posl[i];
     }
-    __device__ __forceinline__ void eval(const DevGeom& g, const CellView& cv, const Home& h,
-                                         const float4& hi, uint32_t e, Acc& a,
-                                         uint32_t& err) const {
-        const int j = (int)(e & kIndexMask);
-        const float4 hj = __ldg(&cv.posh[j]);
-        const float4 lj = __ldg(&cv.posl[j]);
-        float d0, d1, d2;
-        if ((e >> 27) == kNoImage) {  // the common case: no periodic image
-            d0 = (hj.x - hi.x) + (lj.x - h.lo.x);
-            d1 = (hj.y - hi.y) + (lj.y - h.lo.y);
-            d2 = (hj.z - hi.z) + (lj.z - h.lo.z);
-        } else {
-            int sx, sy, sz;
-            decode_image(e, sx, sy, sz);
-            d0 = ((hj.x + (float)sx * g.Lhi) - hi.x) + ((lj.x + (float)sx * g.Llo) - h.lo.x);
-            d1 = ((hj.y + (float)sy * g.Lhi) - hi.y) + ((lj.y + (float)sy * g.Llo) - h.lo.y);
-            d2 = ((hj.z + (float)sz * g.Lhi) - hi.z) + ((lj.z + (float)sz * g.Llo) - h.lo.z);
-        }
+    __device__ __forceinline__ void shift(const Home& h, const float4& hi, int sx, int sy, int sz,
+                                          const DevGeom& g, Shifted& o) const {
+        float ex, ey, ez;
+        two_sum(hi.x, -(float)sx * g.Lhi, o.h.x, ex);
+        two_sum(hi.y, -(float)sy * g.Lhi, o.h.y, ey);
+        two_sum(hi.z, -(float)sz * g.Lhi, o.h.z, ez);
+        o.h.w = hi.w;
+        o.lx = (ex + h.lo.x) - (float)sx * g.Llo;
+        o.ly = (ey + h.lo.y) - (float)sy * g.Llo;
+        o.lz = (ez + h.lo.z) - (float)sz * g.Llo;
+    }
+    __device__ __forceinline__ void eval(const float4& hj, const float4& lj, const Shifted& hs,
+                                         Acc& a, uint32_t& err) const {
+        const float d0 = (hj.x - hs.h.x) + (lj.x - hs.lx);
+        const float d1 = (hj.y - hs.h.y) + (lj.y - hs.ly);
+        const float d2 = (hj.z - hs.h.z) + (lj.z - hs.lz);
         const float r2 = d0 * d0 + d1 * d1 + d2 * d2;
         if (r2 < rc2f) {
             const float rinv = rsqrtf(r2);
             const float r = r2 * rinv;
-            const float size = hi.w + hj.w;
+            const float size = hs.h.w + hj.w;
             if (r < 0.8f * size) err |= EBIT_OVERLAP;
             const float f = pf.fnet32(r2, r, rinv, size) * rinv;
             a.p0 += f * d0;
