@@ -86,6 +86,8 @@ def build(verbose=False, force=False):
 
 
 PLUGINS = ["AOPotential", "LennardJones", "Calibration"]
+# the names the reference's own settings.cfg files use for the same plugins
+ALIASES = {"AO": "AOPotential", "LJ": "LennardJones", "Cal": "Calibration"}
 
 
 def build_plugins():
@@ -106,6 +108,10 @@ def build_plugins():
         if r.returncode != 0:
             raise RuntimeError("plugin build failed for %s:\n%s" % (name, r.stderr))
         os.replace(out + ".tmp", out)
+    for alias, name in ALIASES.items():
+        link = os.path.join(HERE, "plugins", alias + ".so")
+        if not os.path.lexists(link):
+            os.symlink(name + ".so", link)
 
 
 if __name__ == "__main__":
