@@ -154,6 +154,24 @@ int psim_cells_build(const psim_geometry* geom, const double* pos, const double*
                      int32_t* particle_hash_index, uint32_t* cell_start_end,
                      double* sorted_particles);
 
+/* The cell-list build of psim_cells_build for callers that cannot allocate
+ * device memory (hosts that own all device memory through their own pool and
+ * forbid cudaMalloc/cudaFree in their step loop, or that cannot afford an
+ * allocation's latency).  No counterpart in the reference, which has no
+ * device code.  All buffers are the caller's device buffers, in the same
+ * layouts as psim_cells_build: d_pos (3n), d_radius (n) in; d_hash_index
+ * (2n), d_cell_start_end (2*s^3), d_sorted (4n, 32-byte aligned) out.  Work
+ * is queued on `stream` (a cudaStream_t; NULL = default stream) and the call
+ * waits for it.  The scratch is one static 32 MiB device array held by every
+ * GPU that loads the library until exit; the first call on a device looks it
+ * up (make that call before any stream capture); calls that overlap on the
+ * GPU share and race on it.  Problems needing more scratch than the array
+ * (about 76 bytes per particle plus 8 per cell) return PSIM_ERR_INPUT.
+ * Allocates no device memory. */
+int psim_cells_build_noalloc(const psim_geometry* geom, const double* d_pos,
+                             const double* d_radius, int32_t* d_hash_index,
+                             uint32_t* d_cell_start_end, double* d_sorted, void* stream);
+
 /* defaultForceManager::getAcceleration (defaultForceManager.cpp:55-65) with
  * the plugin's getAcceleration/iterCells (e.g. AOPotential.cpp:61-175) on
  * a cell list in the reference layout.  Writes particle_force (3n, original

@@ -108,6 +108,7 @@ def lib():
             "psim_force_params_from_settings": ([C.c_char_p, C.c_char_p, C.POINTER(ForceParams)], C.c_int),
             "psim_ao_coefficients": ([C.c_double] * 3 + [C.POINTER(C.c_double)] * 2, C.c_int),
             "psim_cells_build": ([C.POINTER(Geometry), P, P, P, P, P], C.c_int),
+            "psim_cells_build_noalloc": ([C.POINTER(Geometry), P, P, P, P, P, P], C.c_int),
             "psim_force_evaluate": ([C.POINTER(ForceParams), C.POINTER(Geometry), C.c_int32, P, P, P, P], C.c_int),
             "psim_vgb_coefficients": ([C.c_double] * 3 + [C.POINTER(VgbCoeffs)], C.c_int),
             "psim_integrator_create": ([C.POINTER(IntegratorConfig), C.c_int32], P),

@@ -6,6 +6,7 @@ Translation units are compiled in parallel with one -gencode each:
   psim_mixed.cu  FP32 pair math (contraction allowed)
   psim_cells.cu  integer counting sort and layout conversions
   psim_api.cu    host side of the C ABI
+  psim_noalloc.cu  the cell-list build on a static device scratch array
 The CUDA runtime is linked statically, so the library needs only the driver.
 Output goes next to this file (git-ignored) and is what the package loads.
 """
@@ -25,6 +26,7 @@ SOURCES = {
     "psim_mixed.cu": [],
     "psim_cells.cu": [],
     "psim_api.cu": [],
+    "psim_noalloc.cu": [],
 }
 HEADERS = ["psim_device.cuh", "psim_kernels.cuh"]
 

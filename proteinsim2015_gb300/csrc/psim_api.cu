@@ -386,6 +386,10 @@ extern "C" {
 
 int psim_abi_version(void) { return 1; }
 
+// Lets other translation units of this library report through
+// psim_last_error_string (not part of the public header).
+void psim_internal_set_error(const char* msg) { g_last_error = msg ? msg : ""; }
+
 const char* psim_last_error_string(void) { return g_last_error.c_str(); }
 
 int psim_device_count(void) {
