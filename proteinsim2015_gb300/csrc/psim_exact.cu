@@ -12,6 +12,7 @@
 #include <cmath>
 
 #include "psim_force.cuh"
+#include "psim_force_cell.cuh"
 #include "psim_vgb.cuh"
 
 namespace psim {
@@ -89,6 +90,32 @@ struct F64Body {
         a.n2 += a.c2;
         a.c0 = a.c1 = a.c2 = 0.0;
     }
+    // the FP64 form takes raw differences; only the FP32 test copy is imaged
+    __device__ __forceinline__ void image(float4& h, double4_32a&, int sx, int sy, int sz,
+                                          const DevGeom& g) const {
+        h.x += (float)sx * g.Lhi;
+        h.y += (float)sy * g.Lhi;
+        h.z += (float)sz * g.Lhi;
+    }
+    __device__ __forceinline__ void partial(const Acc& a, double* red, int tid,
+                                            int stride) const {
+        red[0 * stride + tid] = a.n0;
+        red[1 * stride + tid] = a.n1;
+        red[2 * stride + tid] = a.n2;
+    }
+    __device__ __forceinline__ void reduce_store(const ForceOut& out, int i, const double* red,
+                                                 int stride, int h, int nh, int k) const {
+        double t0 = 0.0, t1 = 0.0, t2 = 0.0;
+        for (int q = 0; q < k; ++q) {
+            const int t = q * nh + h;
+            t0 += red[0 * stride + t];
+            t1 += red[1 * stride + t];
+            t2 += red[2 * stride + t];
+        }
+        out.fx[i] = t0;
+        out.fy[i] = t1;
+        out.fz[i] = t2;
+    }
     __device__ __forceinline__ void store(const ForceOut& out, int i, const Acc& a) const {
         out.fx[i] = a.n0;
         out.fy[i] = a.n1;
@@ -99,34 +126,36 @@ struct F64Body {
 
 template <class Pair>
 static cudaError_t run_fp64(const Pair& p, const DevGeom& g, const CellView& cv,
-                            const ForceOut& out, float pre, cudaStream_t st) {
+                            const ForceOut& out, float pre, cudaStream_t st, int tile) {
+    if (tile) return launch_force_cells(F64Body<Pair>{p, g}, g, cv, out, pre, st);
     return launch_force_pass(F64Body<Pair>{p, g}, g, cv, out, pre, st);
 }
 
 template <int N>
 static cudaError_t run_lj_fp64(const LJPair& lj, const DevGeom& g, const CellView& cv,
-                               const ForceOut& out, float pre, cudaStream_t st) {
+                               const ForceOut& out, float pre, cudaStream_t st, int tile) {
     LJFixed<N> p;
     static_cast<LJPair&>(p) = lj;
-    return run_fp64(p, g, cv, out, pre, st);
+    return run_fp64(p, g, cv, out, pre, st, tile);
 }
 
 cudaError_t launch_forces_fp64(const ForceSetup& fs, const DevGeom& g, const CellView& cv,
                                const ForceOut& out, cudaStream_t st) {
+    const int t = fs.tile;
     switch (fs.kind) {
-    case 1: return run_fp64(fs.ao, g, cv, out, fs.pre_rc2f, st);
+    case 1: return run_fp64(fs.ao, g, cv, out, fs.pre_rc2f, st, t);
     case 2:
         switch (fs.lj.n) {
-        case 0: return run_lj_fp64<0>(fs.lj, g, cv, out, fs.pre_rc2f, st);
-        case 6: return run_lj_fp64<6>(fs.lj, g, cv, out, fs.pre_rc2f, st);
-        case 12: return run_lj_fp64<12>(fs.lj, g, cv, out, fs.pre_rc2f, st);
-        case 18: return run_lj_fp64<18>(fs.lj, g, cv, out, fs.pre_rc2f, st);
-        default: return run_fp64(fs.lj, g, cv, out, fs.pre_rc2f, st);
+        case 0: return run_lj_fp64<0>(fs.lj, g, cv, out, fs.pre_rc2f, st, t);
+        case 6: return run_lj_fp64<6>(fs.lj, g, cv, out, fs.pre_rc2f, st, t);
+        case 12: return run_lj_fp64<12>(fs.lj, g, cv, out, fs.pre_rc2f, st, t);
+        case 18: return run_lj_fp64<18>(fs.lj, g, cv, out, fs.pre_rc2f, st, t);
+        default: return run_fp64(fs.lj, g, cv, out, fs.pre_rc2f, st, t);
         }
-    case 3: return run_fp64(fs.cal, g, cv, out, fs.pre_rc2f, st);
+    case 3: return run_fp64(fs.cal, g, cv, out, fs.pre_rc2f, st, t);
     case 4: {
         ComboPair cp{fs.ao, fs.lj, fs.ao.rc2 > fs.lj.rc2 ? fs.ao.rc2 : fs.lj.rc2};
-        return run_fp64(cp, g, cv, out, fs.pre_rc2f, st);
+        return run_fp64(cp, g, cv, out, fs.pre_rc2f, st, t);
     }
     }
     return cudaErrorInvalidValue;

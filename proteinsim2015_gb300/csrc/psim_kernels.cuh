@@ -21,6 +21,7 @@ struct ForceSetup {
     CalPair cal;
     double rc_max;     // largest cutoff: cell_size must be >= rc_max
     float pre_rc2f;    // conservative FP32 prefilter bound on r^2 (FP64 form)
+    int tile;          // 0: a warp per 32 consecutive particles; 1: a block per home cell
 };
 
 // Positions and cell ranges in sorted (cell) order, as the force kernels read them.

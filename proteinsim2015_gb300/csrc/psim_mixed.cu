@@ -13,6 +13,7 @@
 #include <cmath>
 
 #include "psim_force.cuh"
+#include "psim_force_cell.cuh"
 #include "psim_vgb.cuh"
 
 namespace psim {
@@ -100,6 +101,47 @@ struct MixedBody {
         kahan_add(a.s2, a.k2, a.p2);
         a.p0 = a.p1 = a.p2 = 0.f;
     }
+    // a staged neighbour with its periodic image s L applied, exactly as a
+    // float pair: (h + l) + s (Lhi + Llo)
+    __device__ __forceinline__ void image(float4& h, float4& l, int sx, int sy, int sz,
+                                          const DevGeom& g) const {
+        float ex, ey, ez;
+        two_sum(h.x, (float)sx * g.Lhi, h.x, ex);
+        two_sum(h.y, (float)sy * g.Lhi, h.y, ey);
+        two_sum(h.z, (float)sz * g.Lhi, h.z, ez);
+        l.x = (l.x + ex) + (float)sx * g.Llo;
+        l.y = (l.y + ey) + (float)sy * g.Llo;
+        l.z = (l.z + ez) + (float)sz * g.Llo;
+    }
+    // per-lane partial sums for the cross-lane reduction: 6 floats per lane
+    __device__ __forceinline__ void partial(const Acc& a, double* red, int tid,
+                                            int stride) const {
+        float* f = reinterpret_cast<float*>(red);
+        f[0 * stride + tid] = a.s0;
+        f[1 * stride + tid] = a.s1;
+        f[2 * stride + tid] = a.s2;
+        f[3 * stride + tid] = a.k0;
+        f[4 * stride + tid] = a.k1;
+        f[5 * stride + tid] = a.k2;
+    }
+    // the k lanes of home h (slots h, h + nh, ...), Kahan-summed in lane order
+    __device__ __forceinline__ void reduce_store(const ForceOut& out, int i, const double* red,
+                                                 int stride, int h, int nh, int k) const {
+        const float* f = reinterpret_cast<const float*>(red);
+        float S0 = 0.f, S1 = 0.f, S2 = 0.f, C0 = 0.f, C1 = 0.f, C2 = 0.f;
+        for (int q = 0; q < k; ++q) {
+            const int t = q * nh + h;
+            kahan_add(S0, C0, f[0 * stride + t]);
+            kahan_add(S1, C1, f[1 * stride + t]);
+            kahan_add(S2, C2, f[2 * stride + t]);
+            kahan_add(S0, C0, -f[3 * stride + t]);
+            kahan_add(S1, C1, -f[4 * stride + t]);
+            kahan_add(S2, C2, -f[5 * stride + t]);
+        }
+        out.fx[i] = (double)S0 - (double)C0;
+        out.fy[i] = (double)S1 - (double)C1;
+        out.fz[i] = (double)S2 - (double)C2;
+    }
     __device__ __forceinline__ void store(const ForceOut& out, int i, const Acc& a) const {
         out.fx[i] = (double)a.s0 - (double)a.k0;
         out.fy[i] = (double)a.s1 - (double)a.k1;
@@ -109,35 +151,37 @@ struct MixedBody {
 
 template <class Pair>
 static cudaError_t run_mixed(const Pair& p, float rc2f, const DevGeom& g, const CellView& cv,
-                             const ForceOut& out, float pre, cudaStream_t st) {
+                             const ForceOut& out, float pre, cudaStream_t st, int tile) {
+    if (tile) return launch_force_cells(MixedBody<Pair>{p, rc2f}, g, cv, out, pre, st);
     return launch_force_pass(MixedBody<Pair>{p, rc2f}, g, cv, out, pre, st);
 }
 
 template <int N>
 static cudaError_t run_lj_mixed(const LJPair& lj, const DevGeom& g, const CellView& cv,
-                                const ForceOut& out, float pre, cudaStream_t st) {
+                                const ForceOut& out, float pre, cudaStream_t st, int tile) {
     LJFixed<N> p;
     static_cast<LJPair&>(p) = lj;
-    return run_mixed(p, lj.rc2f, g, cv, out, pre, st);
+    return run_mixed(p, lj.rc2f, g, cv, out, pre, st, tile);
 }
 
 cudaError_t launch_forces_mixed(const ForceSetup& fs, const DevGeom& g, const CellView& cv,
                                 const ForceOut& out, cudaStream_t st) {
     const float pre = fs.pre_rc2f;
+    const int t = fs.tile;
     switch (fs.kind) {
-    case 1: return run_mixed(fs.ao, fs.ao.rc2f, g, cv, out, pre, st);
+    case 1: return run_mixed(fs.ao, fs.ao.rc2f, g, cv, out, pre, st, t);
     case 2:
         switch (fs.lj.n) {
-        case 0: return run_lj_mixed<0>(fs.lj, g, cv, out, pre, st);
-        case 6: return run_lj_mixed<6>(fs.lj, g, cv, out, pre, st);
-        case 12: return run_lj_mixed<12>(fs.lj, g, cv, out, pre, st);
-        case 18: return run_lj_mixed<18>(fs.lj, g, cv, out, pre, st);
-        default: return run_mixed(fs.lj, fs.lj.rc2f, g, cv, out, pre, st);
+        case 0: return run_lj_mixed<0>(fs.lj, g, cv, out, pre, st, t);
+        case 6: return run_lj_mixed<6>(fs.lj, g, cv, out, pre, st, t);
+        case 12: return run_lj_mixed<12>(fs.lj, g, cv, out, pre, st, t);
+        case 18: return run_lj_mixed<18>(fs.lj, g, cv, out, pre, st, t);
+        default: return run_mixed(fs.lj, fs.lj.rc2f, g, cv, out, pre, st, t);
         }
-    case 3: return run_mixed(fs.cal, fs.cal.rc2f, g, cv, out, pre, st);
+    case 3: return run_mixed(fs.cal, fs.cal.rc2f, g, cv, out, pre, st, t);
     case 4: {
         const float rc2f = fs.ao.rc2f > fs.lj.rc2f ? fs.ao.rc2f : fs.lj.rc2f;
-        return run_mixed(ComboPairF{fs.ao, fs.lj}, rc2f, g, cv, out, pre, st);
+        return run_mixed(ComboPairF{fs.ao, fs.lj}, rc2f, g, cv, out, pre, st, t);
     }
     }
     return cudaErrorInvalidValue;

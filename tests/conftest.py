@@ -37,3 +37,10 @@ def psim():
     import proteinsim2015_gb300 as psim
     psim.lib()
     return psim
+
+
+@pytest.fixture(params=["rows", "cells"])
+def force_pass(request, monkeypatch):
+    """Both force-pass layouts: a warp per 32 sorted particles, a block per cell."""
+    monkeypatch.setenv("PSIM_FORCE_PASS", request.param)
+    return request.param

@@ -9,7 +9,6 @@ from gpu_helpers import (FORCE_TOL_FP64, FORCE_TOL_MIXED, lattice_state, oracle_
 from oracle import port
 
 pytestmark = pytest.mark.gpu
-
 PLUGIN_OF = {"AO": "AOPotential", "AOq": "AOPotential", "LJ6": "LennardJones",
              "LJ18": "LennardJones", "YUK": "LennardJones", "CAL": "Calibration"}
 
@@ -22,7 +21,7 @@ def params_from_golden(psim, golden, key):
 
 @pytest.mark.parametrize("key", sorted(PLUGIN_OF))
 @pytest.mark.parametrize("precision", [0, 1])
-def test_forces_match_reference_golden(psim, golden, key, precision):
+def test_forces_match_reference_golden(psim, golden, key, precision, force_pass):
     n, box, cs, scale = (int(v) for v in golden["cellsA_geom"])
     g = psim.geometry(n, box, cs, scale)
     p = params_from_golden(psim, golden, key)
@@ -38,7 +37,7 @@ def test_forces_match_reference_golden(psim, golden, key, precision):
 
 
 @pytest.mark.parametrize("precision", [0, 1])
-def test_lj_dense_liquid_matches_oracle(psim, precision):
+def test_lj_dense_liquid_matches_oracle(psim, precision, force_pass):
     # rho = 0.8 LJ (the 2^20 benchmark's density), a jittered FCC block
     pos, rad, box = lattice_state(8, (4 / 0.8) ** (1 / 3), 0.08, seed=4)
     n = len(rad)
@@ -55,7 +54,7 @@ def test_lj_dense_liquid_matches_oracle(psim, precision):
 
 
 @pytest.mark.parametrize("precision", [0, 1])
-def test_ao_yukawa_composite_matches_oracle(psim, precision):
+def test_ao_yukawa_composite_matches_oracle(psim, precision, force_pass):
     pos, rad = rsa_state(3000, 26.0, seed=9)
     n = len(rad)
     g = psim.geometry(n, 26.0, 26.0 / 8, 8)
@@ -88,7 +87,7 @@ def test_empty_and_single_particle(psim):
 
 
 @pytest.mark.parametrize("precision", [0, 1])
-def test_sparse_grid_with_empty_cells(psim, precision):
+def test_sparse_grid_with_empty_cells(psim, precision, force_pass):
     # 0.5 particles per cell: most rows cross empty cells, whose sentinel
     # start must not break the contiguous row walk
     n, box, scale = 500, 30.0, 10

@@ -18,7 +18,7 @@ def make_system(psim, n, box, scale, force, precision=0, noise_mode=1, gamma=1.0
 
 
 @pytest.mark.parametrize("tag", ["AO", "LJ"])
-def test_trajectory_matches_reference_golden(psim, golden, tag):
+def test_trajectory_matches_reference_golden(psim, golden, tag, force_pass):
     n, box, cs, scale = (int(v) for v in golden["cellsA_geom"])
     s = settings_of(golden, "traj%s_settings" % tag)
     steps, vel_freq = (int(v) for v in golden["traj%s_meta" % tag])
@@ -40,7 +40,7 @@ def test_trajectory_matches_reference_golden(psim, golden, tag):
         assert np.max(np.abs(out[k] - ref)) <= 1e-9 * np.max(np.abs(ref)), k
 
 
-def test_100_steps_match_oracle_fp64(psim):
+def test_100_steps_match_oracle_fp64(psim, force_pass):
     n, box, scale = 4000, 21.0, 7            # the reference-constructible AO box
     pos, rad = rsa_state(n, box, seed=21)
     rng = np.random.default_rng(8)
