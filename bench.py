@@ -32,7 +32,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "particle-steps/s, 1 GB300: FP32-mixed vs FP64 plain at <=1e-5 rel force err"
+METRIC = "particle-steps/s, 1 GB300: FP32-mixed vs FP64 plain at \u22641e-5 rel force err"
 UNIT = "particle-steps/s"
 KT, WD, RC, LJN, DT, GAMMA = 1.5, 1.0 / 1.5, 2.5, 6, 0.002, 1.0
 FLOPS_PER_PAIR_LJ = 30   # algorithmic FLOPs per in-range ordered pair (FMA = 2)
@@ -113,6 +113,24 @@ class ClockSampler:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
                 "samples": len(sm)}
+
+
+# the dominant kernel of the mixed step and the ncu summary that gives its
+# DRAM traffic per launch (a line "dram_bytes_per_launch: B")
+FORCE_KERNEL = "force_pass_kernel<MixedBody<LJFixed<6>>>"
+FORCE_PROFILE = os.path.join(ROOT, "profiles", "force_pass_lj_rho0.8_n2e20.txt")
+
+
+def profiled_traffic(path):
+    """DRAM bytes per launch (read + write) from a committed ncu summary, or None."""
+    try:
+        with open(path) as fh:
+            for line in fh:
+                if line.startswith("dram_bytes_per_launch:"):
+                    return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
 
 
 def measured_peaks():
@@ -361,8 +379,9 @@ def run_gpu(args):
                 "path": "force_evaluate -> next_system -> cells_build on pinned host arrays"},
         "gpu_launches": args.steps * s.launches_per_step(),
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak,
-                     "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": None,
-                     "kernel": "force_mixed_kernel<LJPair>",
+                     "unit": "TFLOP/s", "frac": achieved / fp32_peak,
+                     "traffic": profiled_traffic(FORCE_PROFILE),
+                     "kernel": FORCE_KERNEL,
                      "algorithmic": "%d FLOP/pair x %.2f pairs/particle x N per launch" % (
                          FLOPS_PER_PAIR_LJ, pairs),
                      "peak_source": "measured FP32 FMA probe (MEASURED_PEAKS.json has no FP32 figure)",
@@ -380,7 +399,7 @@ def run_gpu(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--steps", type=int, default=5000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-baseline-json", type=float, default=None,
