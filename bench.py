@@ -37,6 +37,9 @@ UNIT = "particle-steps/s"
 KT, WD, RC, LJN, DT, GAMMA = 1.5, 1.0 / 1.5, 2.5, 6, 0.002, 1.0
 FLOPS_PER_PAIR_LJ = 30   # algorithmic FLOPs per in-range ordered pair (FMA = 2)
 FLOPS_VGB = 60           # algorithmic FP64 FLOPs per particle of the vGB update
+# Verlet pair-list skin of the mixed form; the cell grid is the finest with
+# cellSize >= rc + skin, so the list can be built from the 27-cell walk
+SKIN = 0.4
 
 
 def workload(cells=64):
@@ -45,7 +48,7 @@ def workload(cells=64):
     box = cells * a
     pos = init.fcc(cells, a).reshape(-1)
     n = pos.size // 3
-    scale = int(math.floor(box / RC))
+    scale = int(math.floor(box / (RC + SKIN)))
     vel = init.maxwell(n, KT, seed=90210).reshape(-1)
     return dict(n=n, box=box, scale=scale, cell_size=box / scale, pos=pos, vel=vel,
                 radius=np.full(n, 0.5), cells=cells)
@@ -303,7 +306,7 @@ def run_gpu(args):
     p = psim.make_force("LJ", RC, kT=KT, well_depth=WD, lj_num=LJN, yukawa_strength=0.0)
     seed = 90210 + 7919 * rank   # independent replicas per rank
     s = psim.System(g, p, gamma=GAMMA, dt=DT, kT=KT, vel_freq=1000, seed=seed,
-                    precision=psim.PRECISION_MIXED, device=dev)
+                    precision=psim.PRECISION_MIXED, device=dev, skin=args.skin)
     s.upload(w["pos"], w["radius"], vel=w["vel"])
     s.step(max(args.warmup, 3))          # W >= 3 untimed warm-up steps (melting the lattice)
     if dist:
@@ -325,7 +328,8 @@ def run_gpu(args):
     if args.profile_only:
         print(json.dumps({"profile_only": True, "value": value, "unit": UNIT,
                           "ms_per_step": ms / args.steps, "phases_ms": prof,
-                          "pairs_per_particle": pairs}))
+                          "pairs_per_particle": pairs, "skin": args.skin,
+                          "cell_scale": scale, "list_builds": s.list_builds()}))
         s.close()
         return 0
     state = s.download()
@@ -404,6 +408,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-baseline-json", type=float, default=None,
                     help=argparse.SUPPRESS)
+    ap.add_argument("--skin", type=float, default=SKIN,
+                    help="pair-list skin of the mixed form (0: walk the 27 cells every step)")
     ap.add_argument("--profile-only", action="store_true",
                     help="time the mixed form and its phases only (short runs under ncu)")
     args = ap.parse_args()

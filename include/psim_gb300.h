@@ -217,6 +217,12 @@ typedef struct {
     int32_t precision;   /* psim_precision */
     int32_t noise_mode;  /* psim_noise_mode */
     int32_t device;      /* CUDA device ordinal */
+    /* Verlet pair-list skin (mixed form only; 0: the force pass walks the
+     * 27 cells every step).  With skin > 0 the pairs within cutOff + skin are
+     * listed from the cell walk and reused until a particle has moved skin/2;
+     * each step's force is the same set of pair terms.  Needs
+     * cellSize >= cutOff + skin. */
+    double skin;
 } psim_system_config;
 
 /* Creates the system and its device buffers (the role of system::system,
@@ -266,6 +272,10 @@ int psim_system_snapshot_wait(psim_system* sys);
 
 /* Step counter (0 = next step is firstStep) and velocity counter. */
 int psim_system_get_step(psim_system* sys, int64_t* step, int32_t* vel_counter);
+
+/* Pair-list rebuilds since the upload (0 without a skin; the list the upload
+ * builds is not counted). */
+int psim_system_list_builds(psim_system* sys, int32_t* builds);
 
 /* The CUDA stream all step kernels are launched on (cudaStream_t). */
 void* psim_system_stream(psim_system* sys);

@@ -87,7 +87,8 @@ class IntegratorConfig(C.Structure):
 
 class SystemConfig(C.Structure):
     _fields_ = [("geom", Geometry), ("integ", IntegratorConfig), ("force", ForceParams),
-                ("precision", C.c_int32), ("noise_mode", C.c_int32), ("device", C.c_int32)]
+                ("precision", C.c_int32), ("noise_mode", C.c_int32), ("device", C.c_int32),
+                ("skin", C.c_double)]
 
 
 _lib = None
@@ -127,6 +128,7 @@ def lib():
             "psim_system_snapshot_wait": ([P], C.c_int),
             "psim_system_get_step": ([P, C.POINTER(C.c_int64), C.POINTER(C.c_int32)], C.c_int),
             "psim_system_stream": ([P], P),
+            "psim_system_list_builds": ([P, C.POINTER(C.c_int32)], C.c_int),
             "psim_system_profile": ([P, C.c_int32, P], C.c_int),
             "psim_system_launches_per_step": ([P], C.c_int),
             "psim_system_cell_occupancy": ([P, C.POINTER(C.c_int32), C.POINTER(C.c_double)], C.c_int),
@@ -331,16 +333,30 @@ class Integrator:
             pass
 
 
+def auto_skin(geom, force, preferred=0.4, smallest=0.1):
+    """A pair-list skin the cell size allows: min(preferred, cellSize - cutOff),
+    or 0 (no list) when that is below `smallest`."""
+    room = geom.cell_size - force.max_cutoff()
+    skin = min(preferred, room * (1.0 - 1e-9))
+    return skin if skin >= smallest else 0.0
+
+
 class System:
     """The device-resident hot loop of system::run (system.cpp:187-206)."""
 
     def __init__(self, geom, force, gamma=1.0, dt=0.001, kT=1.0, vel_freq=1000, seed=90210,
-                 precision=PRECISION_MIXED, noise_mode=NOISE_PHILOX, device=0):
+                 precision=PRECISION_MIXED, noise_mode=NOISE_PHILOX, device=0, skin=0.0):
+        """skin: Verlet pair-list skin of the mixed form (0: walk the 27 cells
+        every step; "auto": the largest of 0.4 and cellSize - cutOff that the
+        cell size allows, if at least 0.1)."""
+        if skin == "auto":
+            skin = auto_skin(geom, force) if precision == PRECISION_MIXED else 0.0
         self.cfg = SystemConfig(geom=geom,
                                 integ=IntegratorConfig(gamma=gamma, dt=dt, kT=kT,
                                                        vel_freq=vel_freq, seed=seed),
                                 force=force, precision=precision, noise_mode=noise_mode,
-                                device=device)
+                                device=device, skin=float(skin))
+        self.skin = float(skin)
         self.n = geom.n_particles
         self.ncell = geom.cell_scale ** 3
         self._h = lib().psim_system_create(C.byref(self.cfg))
@@ -395,6 +411,11 @@ class System:
         s, v = C.c_int64(), C.c_int32()
         _check(lib().psim_system_get_step(self._h, C.byref(s), C.byref(v)))
         return s.value, v.value
+
+    def list_builds(self):
+        b = C.c_int32()
+        _check(lib().psim_system_list_builds(self._h, C.byref(b)))
+        return b.value
 
     def stream(self):
         return lib().psim_system_stream(self._h)

@@ -48,7 +48,7 @@ int code_from_bits(uint32_t bits) {
     if (bits & EBIT_NAN) return PSIM_ERR_NAN_FORCE;
     if (bits & EBIT_BOUNDS) return PSIM_ERR_PARTICLE_BOUNDS;
     if (bits & EBIT_CELL) return PSIM_ERR_CELL_BOUNDS;
-    if (bits & (EBIT_NOISE | EBIT_INDEX)) return PSIM_ERR_INPUT;
+    if (bits & (EBIT_NOISE | EBIT_INDEX | EBIT_LIST)) return PSIM_ERR_INPUT;
     return PSIM_OK;
 }
 
@@ -59,6 +59,9 @@ const char* bits_text(uint32_t bits) {
     if (bits & EBIT_CELL) return "particle hashed outside the cell grid";
     if (bits & EBIT_NOISE) return "injected noise does not cover the step";
     if (bits & EBIT_INDEX) return "an index or cell range in the input is out of bounds";
+    if (bits & EBIT_LIST)
+        return "pair list full: a particle has more neighbours within cutOff + skin than the "
+               "list holds (lower the skin)";
     return "";
 }
 
@@ -188,6 +191,16 @@ void ao_coeffs(double kT, double wd, double rc, double* c1, double* c2) {  // AO
     *c2 = -3.0 * a1 * a3;
 }
 
+// The FP32 candidate test sees positions rounded to FP32 (ulp(L)/2 each),
+// L rounded (ulp(L)/2), the imaged home position rounded (ulp(L)) and the
+// difference rounded: a separation is off by at most ~4.3 ulp(L), so the
+// test's radius is widened by 8 ulp(L).
+float prefilter_r2(double r, double L) {
+    double ulpL = std::ldexp(1.0, std::ilogb(std::max(L, 1.0)) - 23);
+    double rpre = r * (1.0 + 1e-6) + 8.0 * ulpL + 1e-6;
+    return (float)(rpre * rpre * (1.0 + 1e-6));
+}
+
 ForceSetup make_setup(const psim_force_params* p, double L) {
     ForceSetup fs{};
     fs.kind = p->kind;
@@ -218,13 +231,7 @@ ForceSetup make_setup(const psim_force_params* p, double L) {
     fs.cal.rc2 = p->cutoff * p->cutoff;
     fs.cal.rc2f = (float)fs.cal.rc2;
     fs.rc_max = max_cutoff(p);
-    // The FP32 candidate test sees positions rounded to FP32 (ulp(L)/2 each),
-    // L rounded (ulp(L)/2), the imaged home position rounded (ulp(L)) and
-    // the difference rounded: a separation is off by at most ~4.3 ulp(L);
-    // the cutoff is widened by 8 ulp(L).
-    double ulpL = std::ldexp(1.0, std::ilogb(std::max(L, 1.0)) - 23);
-    double rpre = fs.rc_max * (1.0 + 1e-6) + 8.0 * ulpL + 1e-6;
-    fs.pre_rc2f = (float)(rpre * rpre * (1.0 + 1e-6));
+    fs.pre_rc2f = prefilter_r2(fs.rc_max, L);
     return fs;
 }
 
@@ -399,7 +406,7 @@ int ws_begin(Workspace& w) {
 
 extern "C" {
 
-int psim_abi_version(void) { return 1; }
+int psim_abi_version(void) { return 2; }
 
 // Lets other translation units of this library report through
 // psim_last_error_string (not part of the public header).
@@ -764,6 +771,14 @@ struct psim_system {
     bool snap_pending = false;
     cudaGraphExec_t graph[6] = {};
     uint32_t latched = 0;
+    // Verlet pair list of the mixed form (list_on): list slot of each storage
+    // slot (ping-pong with the order), positions at the build, entries,
+    // counts, and the two step-parity rebuild flags
+    bool list_on = false;
+    double skin = 0.0;
+    int lcap = 0;
+    float lpre = 0.f, ldisp2 = 0.f;
+    DevBuf lslot[2], lbuild, list, lcount, lflag;
 };
 
 namespace {
@@ -788,22 +803,38 @@ Phase phase_of(long long t) {
 
 double* d3(DevBuf& b, int n, int k) { return b.as<double>() + (size_t)k * n; }
 
+// The pair-list build on the cell order just made (count buffer cb), run
+// only when *gate != 0.
+cudaError_t enqueue_list_build(psim_system* s, int cb, const int* gate) {
+    CellView cv{nullptr, s->posh.as<float4>(), s->posl.as<float4>(), s->cellid.as<int>(),
+                s->start.as<int>(), s->count[cb].as<int>()};
+    ListBuild lb{s->list.as<uint32_t>(), s->lcount.as<int>(), s->n, s->lcap, s->lpre, gate};
+    return launch_list_build(s->g, cv, lb, s->err.as<uint32_t>(), s->st);
+}
+
 int enqueue_step(psim_system* s, long long t, cudaEvent_t* evs) {
     const Phase ph = phase_of(t);
     const int n = s->n;
     cudaStream_t st = s->st;
     const int sb = ph.sb, nsb = 1 - ph.sb, ob = ph.ob, nob = 1 - ph.ob, cb = ph.cb, ncb = 1 - ph.cb;
     const int pb = ph.pb, npb = 1 - ph.pb;
+    // the rebuild flag of this step's parity (pair list only)
+    int* lflag = s->list_on ? s->lflag.as<int>() + (t & 1) : nullptr;
     if (evs) PSIM_CUDA(cudaEventRecord(evs[0], st));
-    // forces on the current cell order
+    // forces on the current cell order, or through the pair list
     CellView cv{s->posd.as<double4_32a>(), s->posh.as<float4>(), s->posl.as<float4>(),
                 s->cellid.as<int>(), s->start.as<int>(), s->count[cb].as<int>()};
     ForceOut fo{d3(s->frc[ph.fcur], n, 0), d3(s->frc[ph.fcur], n, 1), d3(s->frc[ph.fcur], n, 2),
-                s->err.as<uint32_t>()};
-    if (s->cfg.precision == PSIM_PRECISION_FP64)
+                s->err.as<uint32_t>(), nullptr};
+    if (s->cfg.precision == PSIM_PRECISION_FP64) {
         PSIM_CUDA(launch_forces_fp64(s->fs, s->g, cv, fo, st));
-    else
+    } else if (s->list_on) {
+        PairList pl{s->lslot[ob].as<int>(), s->posh.as<float4>(), s->posl.as<float4>(),
+                    s->lcount.as<int>(), s->list.as<uint32_t>(), n};
+        PSIM_CUDA(launch_forces_list(s->fs, s->g, pl, fo, st));
+    } else {
         PSIM_CUDA(launch_forces_mixed(s->fs, s->g, cv, fo, st));
+    }
     if (evs) PSIM_CUDA(cudaEventRecord(evs[1], st));
     // integrator: pushParticleForce + nextSystem, hash + count into the next grid
     PSIM_CUDA(cudaMemsetAsync(s->count[ncb].p, 0, 4 * (size_t)s->ncell, st));
@@ -827,6 +858,15 @@ int enqueue_step(psim_system* s, long long t, cudaEvent_t* evs) {
     a.count = s->count[ncb].as<int>();
     a.err = s->err.as<uint32_t>();
     a.state = s->state.as<StepState>();
+    if (s->list_on) {
+        a.lslot = s->lslot[ob].as<int>();
+        a.lbuild = s->lbuild.as<float4>();
+        a.lposh = s->posh.as<float4>();
+        a.lposl = s->posl.as<float4>();
+        a.lflag_set = lflag;
+        a.lflag_clear = s->lflag.as<int>() + (1 - (t & 1));
+        a.ldisp2 = s->ldisp2;
+    }
     NoiseView nz{s->cfg.noise_mode, s->noise.as<double>(), s->noise_first, s->noise_steps};
     if (s->cfg.precision == PSIM_PRECISION_FP64)
         PSIM_CUDA(launch_vgb_system(a, s->vp, s->g, nz, st));
@@ -860,7 +900,14 @@ int enqueue_step(psim_system* s, long long t, cudaEvent_t* evs) {
     ca.advance = 1;
     ca.vel_freq = s->vp.vel_freq;
     ca.err = s->err.as<uint32_t>();
+    if (s->list_on) {
+        ca.rebuild = lflag;
+        ca.lslot_in = s->lslot[ob].as<int>();
+        ca.lslot_out = s->lslot[nob].as<int>();
+        ca.lbuild = s->lbuild.as<float4>();
+    }
     PSIM_CUDA(launch_canonicalize(ca, st));
+    if (s->list_on) PSIM_CUDA(enqueue_list_build(s, ncb, lflag));
     if (evs) PSIM_CUDA(cudaEventRecord(evs[3], st));
     return PSIM_OK;
 }
@@ -926,6 +973,24 @@ psim_system* psim_system_create(const psim_system_config* cfg) {
     if (make_geom(&cfg->geom, max_cutoff(&cfg->force), &g)) return nullptr;
     VgbParams vp;
     if (make_vgb_params(&cfg->integ, &vp)) return nullptr;
+    const double rc = max_cutoff(&cfg->force);
+    const double skin = cfg->skin;
+    const bool list_on = skin > 0.0 && cfg->precision == PSIM_PRECISION_MIXED;
+    if (!(skin >= 0.0) || (skin > 0.0 && cfg->precision != PSIM_PRECISION_MIXED)) {
+        fail(PSIM_ERR_INPUT, "a pair-list skin needs the mixed precision form (skin %g)", skin);
+        return nullptr;
+    }
+    if (list_on && g.cs < rc + skin) {
+        // the list is built from the 27-cell walk, which sees every pair
+        // within cellSize only
+        fail(PSIM_ERR_INPUT, "pair-list skin %g needs cellSize >= cutOff + skin (%g < %g)", skin,
+             g.cs, rc + skin);
+        return nullptr;
+    }
+    if (list_on && g.n > (int)kListIdxMask) {
+        fail(PSIM_ERR_INPUT, "the pair list indexes at most %u particles", kListIdxMask);
+        return nullptr;
+    }
     if (ensure_device()) return nullptr;
     int ndev = 0;
     cudaGetDeviceCount(&ndev);
@@ -943,6 +1008,20 @@ psim_system* psim_system_create(const psim_system_config* cfg) {
     s->fs.tile = choose_tile(g);
     s->n = g.n;
     s->ncell = g.ncell;
+    if (list_on) {
+        // room for 1.5x the mean number of neighbours within rc + skin, + 32
+        const double rl = rc + skin;
+        const double mean = 4.0 / 3.0 * M_PI * rl * rl * rl * g.n / (g.L * g.L * g.L);
+        s->list_on = true;
+        s->skin = skin;
+        s->lcap = ((int)(1.5 * mean) + 32 + 31) / 32 * 32;
+        s->lpre = prefilter_r2(rl, g.L);
+        // the rebuild test compares FP32 roundings of the positions (each off
+        // by ulp(L)/2): half the skin, less that error
+        const double ulpL = std::ldexp(1.0, std::ilogb(std::max(g.L, 1.0)) - 23);
+        const double dmax = 0.5 * skin * (1.0 - 1e-3) - 4.0 * ulpL;
+        s->ldisp2 = dmax > 0.0 ? (float)(dmax * dmax) : 0.f;
+    }
     const size_t n = (size_t)g.n, nc = (size_t)g.ncell;
     bool ok = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) == cudaSuccess &&
               cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking) == cudaSuccess &&
@@ -958,11 +1037,22 @@ psim_system* psim_system_create(const psim_system_config* cfg) {
     for (int k = 0; k < 3 && ok; ++k) ok = !s->frc[k].ensure(24 * n);
     ok = ok && !s->cellid.ensure(4 * n) && !s->key.ensure(4 * n) && !s->rank.ensure(4 * n) &&
          !s->tmp.ensure(4 * n) && !s->start.ensure(4 * nc) &&
-         !s->scratch.ensure(4 * scan_scratch_ints(g.ncell)) && !s->posh.ensure(16 * n) &&
+         !s->scratch.ensure(4 * scan_scratch_ints(g.ncell)) &&
+         !s->posh.ensure(16 * (n + (list_on ? 1 : 0))) &&
          !s->vel.ensure(24 * n) && !s->err.ensure(4) && !s->state.ensure(sizeof(StepState)) &&
          !s->occ.ensure(4);
     if (ok && cfg->precision == PSIM_PRECISION_FP64) ok = !s->posd.ensure(32 * n);
-    if (ok && cfg->precision == PSIM_PRECISION_MIXED) ok = !s->posl.ensure(16 * n);
+    if (ok && cfg->precision == PSIM_PRECISION_MIXED)
+        ok = !s->posl.ensure(16 * (n + (list_on ? 1 : 0)));
+    if (ok && list_on) {
+        ok = !s->lslot[0].ensure(4 * n) && !s->lslot[1].ensure(4 * n) && !s->lbuild.ensure(16 * n) &&
+             !s->list.ensure(4 * n * (size_t)s->lcap) && !s->lcount.ensure(4 * n) &&
+             !s->lflag.ensure(8) && cudaMemset(s->lflag.p, 0, 8) == cudaSuccess;
+        // the ghost slot n that pads the lists: far from every particle
+        const float4 gh = make_float4(1e18f, 1e18f, 1e18f, 0.f), gl = make_float4(0.f, 0.f, 0.f, 0.f);
+        ok = ok && cudaMemcpy(s->posh.as<float4>() + n, &gh, 16, cudaMemcpyHostToDevice) == cudaSuccess &&
+             cudaMemcpy(s->posl.as<float4>() + n, &gl, 16, cudaMemcpyHostToDevice) == cudaSuccess;
+    }
     if (ok) ok = cudaMemset(s->err.p, 0, 4) == cudaSuccess &&
                  cudaMemset(s->state.p, 0, sizeof(StepState)) == cudaSuccess;
     if (!ok) {
@@ -981,7 +1071,8 @@ void psim_system_destroy(psim_system* s) {
     drop_graphs(s);
     DevBuf* arrs[] = {&s->cellid, &s->key, &s->rank, &s->tmp, &s->start, &s->scratch, &s->posd,
                       &s->posh, &s->posl, &s->vel, &s->err, &s->state, &s->occ, &s->noise,
-                      &s->snap};
+                      &s->snap, &s->lslot[0], &s->lslot[1], &s->lbuild, &s->list, &s->lcount,
+                      &s->lflag};
     for (DevBuf* b : arrs) b->release();
     for (int k = 0; k < 2; ++k) {
         s->pos[k].release(); s->pos0[k].release(); s->mem[k].release(); s->tag[k].release();
@@ -1068,7 +1159,21 @@ int psim_system_upload(psim_system* s, const double* pos, const double* pos0, co
     ca.posd = s->cfg.precision == PSIM_PRECISION_FP64 ? s->posd.as<double4_32a>() : nullptr;
     ca.posh = s->posh.as<float4>();
     ca.posl = s->cfg.precision == PSIM_PRECISION_MIXED ? s->posl.as<float4>() : nullptr;
+    if (s->list_on) {
+        // the first list, on the first cell order: flag 0 raised for the
+        // build, lowered for step 0 (whose integrator raises it when needed)
+        const int one = 1;
+        PSIM_CUDA(cudaMemsetAsync(s->lflag.p, 0, 8, st));
+        PSIM_CUDA(cudaMemcpyAsync(s->lflag.p, &one, 4, cudaMemcpyHostToDevice, st));
+        ca.rebuild = s->lflag.as<int>();
+        ca.lslot_out = s->lslot[ob].as<int>();
+        ca.lbuild = s->lbuild.as<float4>();
+    }
     PSIM_CUDA(launch_canonicalize(ca, st));
+    if (s->list_on) {
+        PSIM_CUDA(enqueue_list_build(s, ph.cb, s->lflag.as<int>()));
+        PSIM_CUDA(cudaMemsetAsync(s->lflag.p, 0, 8, st));
+    }
     uint32_t bits = 0;
     PSIM_CUDA(cudaMemcpyAsync(&bits, s->err.p, 4, cudaMemcpyDeviceToHost, st));
     PSIM_CUDA(cudaStreamSynchronize(st));
@@ -1246,6 +1351,16 @@ int psim_system_get_step(psim_system* s, int64_t* step, int32_t* vel_counter) {
     return PSIM_OK;
 }
 
+int psim_system_list_builds(psim_system* s, int32_t* builds) {
+    if (!s || !builds) return fail(PSIM_ERR_INPUT, "NULL argument");
+    DeviceGuard dg(s->device);
+    PSIM_CUDA(cudaStreamSynchronize(s->st));
+    StepState ss{};
+    PSIM_CUDA(cudaMemcpy(&ss, s->state.p, sizeof ss, cudaMemcpyDeviceToHost));
+    *builds = ss.list_builds;
+    return PSIM_OK;
+}
+
 void* psim_system_stream(psim_system* s) { return s ? (void*)s->st : nullptr; }
 
 int psim_system_profile(psim_system* s, int32_t n_steps, double* out_ms) {
@@ -1269,8 +1384,9 @@ int psim_system_profile(psim_system* s, int32_t n_steps, double* out_ms) {
 }
 
 int psim_system_launches_per_step(psim_system* s) {
-    (void)s;
-    return 7;  // force, vGB, scan x3, scatter, canonicalise (+1 memset node)
+    // force, vGB, scan x3, scatter, canonicalise (+1 memset node); the
+    // pair-list build (which returns at once unless the list is due)
+    return (s && s->list_on) ? 8 : 7;
 }
 
 int psim_system_cell_occupancy(psim_system* s, int32_t* max_occ, double* mean_occ) {
@@ -1321,11 +1437,17 @@ int psim_system_pair_count(psim_system* s, double cutoff, double* mean_pairs) {
     int rc = settle(s);
     if (rc) return rc;
     const Phase ph = phase_of(s->total);
-    ScopedBuf tot;
+    ScopedBuf tot, ph4;
     PSIM_CUDA(tot.ensure(8));
+    PSIM_CUDA(ph4.ensure(16 * (size_t)s->n));
     PSIM_CUDA(cudaMemsetAsync(tot.p, 0, 8, s->st));
-    CellView cv{s->posd.as<double4_32a>(), s->posh.as<float4>(), s->posl.as<float4>(),
-                s->cellid.as<int>(), s->start.as<int>(), s->count[ph.cb].as<int>()};
+    // sorted positions gathered from the FP64 state (with a pair list the
+    // float copies are in list order)
+    PSIM_CUDA(launch_gather_posh(s->n, s->perm[ph.pb].as<int>(), d3(s->pos[ph.sb], s->n, 0),
+                                 d3(s->pos[ph.sb], s->n, 1), d3(s->pos[ph.sb], s->n, 2),
+                                 s->radius[ph.ob].as<double>(), ph4.as<float4>(), s->st));
+    CellView cv{nullptr, ph4.as<float4>(), nullptr, s->cellid.as<int>(), s->start.as<int>(),
+                s->count[ph.cb].as<int>()};
     PSIM_CUDA(launch_pair_count(s->g, cv, (float)(cutoff * cutoff), tot.as<unsigned long long>(),
                                 s->st));
     unsigned long long h = 0;

@@ -143,13 +143,22 @@ __global__ void __launch_bounds__(256) canonicalize_kernel(CanonArgs a, int vel_
         const double R = a.radius_in[f];
         a.radius_out[g] = R;
         if (a.inv_mass_out) a.inv_mass_out[g] = a.inv_mass_in[f];
-        const double x = a.x[f], y = a.y[f], z = a.z[f];
-        if (a.posd) a.posd[g] = make_double4_32a(x, y, z, R);
-        const float hx = (float)x, hy = (float)y, hz = (float)z;
-        a.posh[g] = make_float4(hx, hy, hz, (float)R);
-        if (a.posl)
-            a.posl[g] = make_float4((float)(x - (double)hx), (float)(y - (double)hy),
-                                    (float)(z - (double)hz), 0.0f);
+        // with a pair list, the sorted positions are written only when the
+        // list is rebuilt on this order (they are the list's positions)
+        const bool pos_out = !a.rebuild || *a.rebuild != 0;
+        if (a.lslot_out) a.lslot_out[g] = (pos_out || !a.lslot_in) ? g : a.lslot_in[f];
+        if (pos_out) {
+            const double x = a.x[f], y = a.y[f], z = a.z[f];
+            if (a.posd) a.posd[g] = make_double4_32a(x, y, z, R);
+            const float hx = (float)x, hy = (float)y, hz = (float)z;
+            const float4 h = make_float4(hx, hy, hz, (float)R);
+            a.posh[g] = h;
+            if (a.lbuild) a.lbuild[g] = h;
+            // .w carries the slot, which the pair-list build reads
+            if (a.posl)
+                a.posl[g] = make_float4((float)(x - (double)hx), (float)(y - (double)hy),
+                                        (float)(z - (double)hz), __int_as_float(g));
+        }
     }
     if (a.state && a.advance && p == 0) {
         // end of a step: brownianIntegrator's velCounter bookkeeping
@@ -157,6 +166,7 @@ __global__ void __launch_bounds__(256) canonicalize_kernel(CanonArgs a, int vel_
         StepState s = *a.state;
         if (s.step > 0) s.vel_counter = (s.vel_counter == vel_freq) ? 0 : s.vel_counter + 1;
         s.step += 1;
+        if (a.rebuild && *a.rebuild) s.list_builds += 1;
         *a.state = s;
     }
 }
@@ -348,6 +358,23 @@ __global__ void __launch_bounds__(256) iota_kernel(int n, int* v) {
 cudaError_t launch_fill_int_iota(int n, int* v, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
     iota_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, v);
+    return cudaGetLastError();
+}
+
+__global__ void __launch_bounds__(256)
+gather_posh_kernel(int n, const int* perm, const double* x, const double* y, const double* z,
+                   const double* radius, float4* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int o = perm[i];
+    out[i] = make_float4((float)x[o], (float)y[o], (float)z[o], (float)radius[i]);
+}
+
+cudaError_t launch_gather_posh(int n, const int* perm, const double* x, const double* y,
+                               const double* z, const double* radius, float4* out,
+                               cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    gather_posh_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, perm, x, y, z, radius, out);
     return cudaGetLastError();
 }
 

@@ -21,6 +21,7 @@ enum : uint32_t {
     EBIT_CELL = 8u,       // 7702 particle hashed outside the grid
     EBIT_NOISE = 16u,     // 7706 injected noise buffer does not cover the step
     EBIT_INDEX = 32u,     // 7706 a caller-supplied index or cell range is out of bounds
+    EBIT_LIST = 64u,      // 7706 a pair list is full (more neighbours within rc + skin than it holds)
 };
 
 // ----------------------------------------------------------------- geometry

@@ -55,10 +55,12 @@ force_pass_kernel(Body body, DevGeom g, CellView cv, ForceOut out, float pre_rc2
     __shared__ uint32_t s_q[kForceWarps][kQueueCap][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    // an error latched by an earlier kernel stops the pass; read once and
-    // broadcast so every lane of the warp takes the same path
-    const bool failed = __shfl_sync(0xffffffffu, (lane == 0) ? (*out.err != 0) : false, 0);
-    const bool active = (i < g.n) && !failed;
+    // an error latched by an earlier kernel (or a closed gate) stops the
+    // pass; read once and broadcast so every lane takes the same path
+    const bool failed = __shfl_sync(
+        0xffffffffu, (lane == 0) ? (*out.err != 0 || (out.gate && *out.gate == 0)) : false, 0);
+    if (failed) return;  // warp-uniform; the kernel synchronises warps only
+    const bool active = i < g.n;
     float4* st_hi = s_hi[w];
     Aux* st_aux = s_aux[w];
     uint32_t (*q)[32] = s_q[w];

@@ -1,0 +1,149 @@
+// psim_force_list.cuh -- the mixed form's force pass through a Verlet pair list.
+//
+// The plugin force on particle i is the sum over the particles j of its 27
+// neighbour cells with |x_j - x_i| < rc (AOPotential.cpp:61-175,
+// LJPotential.cpp:64-182).  Every such j lies within rc + skin of i's position
+// at any earlier time at which neither particle had yet moved skin/2 -- so a
+// list of the pairs within rc + skin, built from the cell list at one step,
+// holds every pair the cell walk would find for as long as no particle has
+// moved more than skin/2 since.  The list is rebuilt on the step after one
+// has.  The force of each step is then the same set of pair terms, read from
+// ~(rc+skin)^3/(27 cs^3) as many candidates as the cell walk tests.
+//
+//   build  the warp kernel of psim_force.cuh with a body that appends, rather
+//          than evaluates, the candidates within rc + skin (plus the rounding
+//          margin of its FP32 test): entry = neighbour slot | image code.
+//          It runs on the step's own cell list, so list order is the cell
+//          order of the build step, and it needs cellSize >= rc + skin.
+//   force  a thread per particle walks its list in FP32 with the plugin's pair
+//          body and Kahan-compensated sums (MixedBody, psim_mixed.cu).
+//
+// Positions in list order are kept as exact float pairs and *unwrapped*: the
+// integrator writes each particle's new position as the image nearest its
+// build position, so a pair's periodic image found at the build stays right
+// for the life of the list (the box is larger than 2 (rc + skin)).
+#pragma once
+
+#include "psim_force.cuh"
+
+namespace psim {
+
+// image code of a list entry: 2 bits per axis (0: none, 1: +L, 3: -L) of the
+// shift applied to the home particle, as in the warp kernel's rows
+__device__ __forceinline__ uint32_t image_code(int sx, int sy, int sz) {
+    return ((uint32_t)(sx & 3) | ((uint32_t)(sy & 3) << 2) | ((uint32_t)(sz & 3) << 4))
+           << kListIdxBits;
+}
+__device__ __forceinline__ int image_axis(uint32_t code, int axis) {
+    return (int)(code << (30 - 2 * axis)) >> 30;  // sign-extend the 2-bit field
+}
+
+// Appends the candidates the warp kernel selects to the home particle's list,
+// then pads the list to a multiple of kListFold with the ghost slot (a
+// far-away dummy particle), so the force pass reads whole batches.  The
+// neighbour's slot travels in the .w lane of its low-part float4.
+struct ListBody {
+    uint32_t* list;
+    int* count;
+    int stride;
+    int cap;    // a multiple of kListFold
+    int ghost;  // the ghost slot (n)
+    using Aux = float4;
+    struct Home {
+        int i;
+    };
+    struct Shifted {
+        int i;
+        uint32_t code;
+    };
+    struct Acc {
+        int n;
+    };
+    __device__ __forceinline__ const Aux* aux(const CellView& cv) const { return cv.posl; }
+    __device__ __forceinline__ void init(Acc& a) const { a.n = 0; }
+    __device__ __forceinline__ void load_home(const CellView&, int i, Home& h) const { h.i = i; }
+    __device__ __forceinline__ void shift(const Home& h, const float4&, int sx, int sy, int sz,
+                                          const DevGeom&, Shifted& o) const {
+        o.i = h.i;
+        o.code = image_code(sx, sy, sz);
+    }
+    __device__ __forceinline__ void eval(const float4&, const float4& lj, const Shifted& hs,
+                                         Acc& a, uint32_t&) const {
+        if (a.n < cap) list[(size_t)a.n * stride + hs.i] = __float_as_uint(lj.w) | hs.code;
+        a.n++;
+    }
+    __device__ __forceinline__ void fold(Acc&) const {}
+    __device__ __forceinline__ void store(const ForceOut& out, int i, const Acc& a) const {
+        if (a.n > cap) {
+            atomicOr(out.err, EBIT_LIST);
+            count[i] = cap;
+            return;
+        }
+        const int padded = (a.n + kListFold - 1) / kListFold * kListFold;
+        for (int k = a.n; k < padded; ++k) list[(size_t)k * stride + i] = (uint32_t)ghost;
+        count[i] = padded;
+    }
+};
+
+// A thread per particle (current storage order f): its list slot, its list,
+// its neighbours' list-order positions; the force is stored at f.  Lists are
+// padded to whole batches, so each batch's loads are issued together
+// before any of its pair terms.
+template <class Body>
+__global__ void __launch_bounds__(128)
+force_list_kernel(Body body, DevGeom g, PairList pl, ForceOut out) {
+    constexpr int kBatch = 4;
+    static_assert(kListFold % kBatch == 0, "batches tile a fold");
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= g.n || *out.err) return;
+    const int s = pl.lslot[f];
+    const float4 hh = pl.posh[s];
+    CellView cv{};
+    cv.posl = pl.posl;
+    typename Body::Home home;
+    body.load_home(cv, s, home);
+    typename Body::Shifted hs0;
+    body.shift(home, hh, 0, 0, 0, g, hs0);
+    typename Body::Acc acc;
+    body.init(acc);
+    uint32_t err = 0;
+    const int cnt = pl.count[s];   // a multiple of kListFold
+    const uint32_t* lp = pl.list + s;
+    for (int k0 = 0; k0 < cnt; k0 += kListFold) {
+#pragma unroll
+        for (int b = 0; b < kListFold; b += kBatch) {
+            uint32_t e[kBatch];
+            float4 nh[kBatch], nl[kBatch];
+#pragma unroll
+            for (int u = 0; u < kBatch; ++u) e[u] = __ldg(lp + (size_t)(k0 + b + u) * pl.stride);
+#pragma unroll
+            for (int u = 0; u < kBatch; ++u) {
+                const int j = (int)(e[u] & kListIdxMask);
+                nh[u] = pl.posh[j];
+                nl[u] = pl.posl[j];
+            }
+#pragma unroll
+            for (int u = 0; u < kBatch; ++u) {
+                const uint32_t code = e[u] >> kListIdxBits;
+                typename Body::Shifted hs = hs0;
+                if (code != 0)  // a pair across the box edge (rare: a branch)
+                    body.shift(home, hh, image_axis(code, 0), image_axis(code, 1),
+                               image_axis(code, 2), g, hs);
+                body.eval_masked(nh[u], nl[u], hs, acc, err);
+            }
+        }
+        body.fold(acc);
+    }
+    body.store(out, f, acc);
+    if (err) atomicOr(out.err, err);
+}
+
+template <class Body>
+cudaError_t launch_force_list(const Body& body, const DevGeom& g, const PairList& pl,
+                              const ForceOut& out, cudaStream_t st) {
+    if (g.n == 0) return cudaSuccess;
+    force_list_kernel<Body><<<(g.n + 127) / 128, 128, 0, st>>>(body, g, pl, out);
+    return cudaGetLastError();
+}
+
+}  // namespace psim

@@ -2,7 +2,8 @@
 // and the kernel translation units:
 //   psim_exact.cu  FP64 kernels built without FMA contraction (the plain
 //                  force form, the vGB update, the cell hash)
-//   psim_mixed.cu  the FP32-pair / Kahan-sum force form
+//   psim_mixed.cu  the FP32-pair / Kahan-sum force form, from the cell list or
+//                  from a Verlet pair list
 //   psim_cells.cu  counting sort, scan, reorder, layout conversions
 #pragma once
 
@@ -28,7 +29,7 @@ struct ForceSetup {
 struct CellView {
     const double4_32a* posd;  // {x, y, z, R}  (FP64 form)
     const float4* posh;   // {x, y, z, R} rounded to FP32
-    const float4* posl;   // {x - xh, y - yh, z - zh, 0} (mixed form)
+    const float4* posl;   // {x - xh, y - yh, z - zh, slot bits} (mixed form)
     const int* cellid;    // cell hash of each sorted slot
     const int* cstart;    // first sorted slot of each cell
     const int* ccount;    // particles in each cell
@@ -39,12 +40,42 @@ struct ForceOut {
     double* fy;
     double* fz;
     uint32_t* err;
+    const int* gate;   // may be null; else the pass runs only when *gate != 0
 };
 
 cudaError_t launch_forces_fp64(const ForceSetup& fs, const DevGeom& g, const CellView& cv,
                                const ForceOut& out, cudaStream_t st);
 cudaError_t launch_forces_mixed(const ForceSetup& fs, const DevGeom& g, const CellView& cv,
                                 const ForceOut& out, cudaStream_t st);
+
+// Verlet pair list of the mixed form (psim_force_list.cuh).  Entries are a
+// neighbour's list slot in the low kListIdxBits bits and the periodic image
+// of the pair above them; the list of slot s is list[k * stride + s].
+constexpr int kListIdxBits = 26;
+constexpr uint32_t kListIdxMask = (1u << kListIdxBits) - 1u;
+constexpr int kListFold = 8;   // pair terms per Kahan fold
+struct PairList {
+    const int* lslot;      // list slot of each current storage slot
+    const float4* posh;    // list order, unwrapped: {x, y, z, R} rounded to FP32
+    const float4* posl;    // list order: low parts
+    const int* count;      // entries of each list slot
+    const uint32_t* list;
+    int stride;
+};
+cudaError_t launch_forces_list(const ForceSetup& fs, const DevGeom& g, const PairList& pl,
+                               const ForceOut& out, cudaStream_t st);
+// Builds the list from the cell list of cv (list order = cell order) when
+// *gate != 0; pre_r2: FP32 bound on r^2 for (rc + skin) with the rounding margin.
+struct ListBuild {
+    uint32_t* list;
+    int* count;
+    int stride;
+    int cap;
+    float pre_r2;
+    const int* gate;
+};
+cudaError_t launch_list_build(const DevGeom& g, const CellView& cv, const ListBuild& lb,
+                              uint32_t* err, cudaStream_t st);
 
 // vGB coefficients and per-step switches for the integrator kernels.
 struct VgbParams {
@@ -60,7 +91,7 @@ struct VgbParams {
 struct StepState {
     long long step;       // steps taken since upload (0 -> firstStep)
     int vel_counter;      // brownianIntegrator::velCounter
-    int pad;
+    int list_builds;      // pair-list rebuilds while stepping
 };
 
 struct NoiseView {
@@ -92,6 +123,18 @@ struct VgbSystemArgs {
     int* count;                 // per-cell counts of the next grid (zeroed)
     uint32_t* err;
     const StepState* state;
+    // mixed form with a pair list (lslot null: none).  The new position is
+    // also written in list order as the image nearest the list-build position
+    // (an exact float pair), and *lflag_set is raised when it lies more than
+    // sqrt(ldisp2) from that position; *lflag_clear (the other step parity's
+    // flag) is cleared.
+    const int* lslot;
+    const float4* lbuild;       // list order: positions at the build, .w radius
+    float4* lposh;
+    float4* lposl;
+    int* lflag_set;
+    int* lflag_clear;
+    float ldisp2;
 };
 cudaError_t launch_vgb_system(const VgbSystemArgs& a, const VgbParams& p, const DevGeom& g,
                               const NoiseView& nz, cudaStream_t st);
@@ -155,6 +198,14 @@ struct CanonArgs {
     int advance;            // 1: this rebuild ends a step (advance state)
     int vel_freq;           // brownianIntegrator::velFreq
     const uint32_t* err;    // non-zero: a previous kernel failed, skip the work
+    // pair-list bookkeeping (null: none).  lslot is carried with the particles;
+    // when *rebuild != 0 the list is rebuilt on the new order, so lslot becomes
+    // the identity and posh/posl/lbuild are written -- otherwise posh/posl
+    // hold the list-order positions and are left alone.
+    const int* rebuild;
+    const int* lslot_in;
+    int* lslot_out;
+    float4* lbuild;
 };
 cudaError_t launch_canonicalize(const CanonArgs& a, cudaStream_t st);
 
@@ -187,6 +238,10 @@ cudaError_t launch_merge_xyz(int n, const double* x, const double* y, const doub
                              const int* tag, const int* perm, double* aos, cudaStream_t st);
 cudaError_t launch_fill_int_iota(int n, int* v, cudaStream_t st);
 // out[i] = (x[perm[i]], y[perm[i]], z[perm[i]], radius[i])
+// Sorted-order float4 {x, y, z, R} from storage-order FP64 positions.
+cudaError_t launch_gather_posh(int n, const int* perm, const double* x, const double* y,
+                               const double* z, const double* radius, float4* out,
+                               cudaStream_t st);
 cudaError_t launch_gather_posd(int n, const int* perm, const double* x, const double* y,
                                const double* z, const double* radius, double4_32a* out,
                                cudaStream_t st);

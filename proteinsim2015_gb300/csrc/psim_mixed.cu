@@ -14,6 +14,7 @@
 
 #include "psim_force.cuh"
 #include "psim_force_cell.cuh"
+#include "psim_force_list.cuh"
 #include "psim_vgb.cuh"
 
 namespace psim {
@@ -95,6 +96,27 @@ struct MixedBody {
             a.p2 += f * d2;
         }
     }
+    // eval without a branch on the cutoff (the pair-list pass, where most
+    // candidates are in range): out-of-range terms are computed at r^2 = 1
+    // and dropped
+    __device__ __forceinline__ void eval_masked(const float4& hj, const float4& lj,
+                                                const Shifted& hs, Acc& a, uint32_t& err) const {
+        const float d0 = (hj.x - hs.h.x) + (lj.x - hs.lx);
+        const float d1 = (hj.y - hs.h.y) + (lj.y - hs.ly);
+        const float d2 = (hj.z - hs.h.z) + (lj.z - hs.lz);
+        const float r2 = d0 * d0 + d1 * d1 + d2 * d2;
+        const bool in = r2 < rc2f;
+        const float r2s = in ? r2 : 1.0f;
+        const float rinv = rsqrtf(r2s);
+        const float r = r2s * rinv;
+        const float size = hs.h.w + hj.w;
+        if (in && r < 0.8f * size) err |= EBIT_OVERLAP;
+        const float fr = pf.fnet32(r2s, r, rinv, size) * rinv;
+        const float f = in ? fr : 0.0f;
+        a.p0 += f * d0;
+        a.p1 += f * d1;
+        a.p2 += f * d2;
+    }
     __device__ __forceinline__ void fold(Acc& a) const {
         kahan_add(a.s0, a.k0, a.p0);
         kahan_add(a.s1, a.k1, a.p1);
@@ -149,42 +171,55 @@ struct MixedBody {
     }
 };
 
-template <class Pair>
-static cudaError_t run_mixed(const Pair& p, float rc2f, const DevGeom& g, const CellView& cv,
-                             const ForceOut& out, float pre, cudaStream_t st, int tile) {
-    if (tile) return launch_force_cells(MixedBody<Pair>{p, rc2f}, g, cv, out, pre, st);
-    return launch_force_pass(MixedBody<Pair>{p, rc2f}, g, cv, out, pre, st);
-}
-
-template <int N>
-static cudaError_t run_lj_mixed(const LJPair& lj, const DevGeom& g, const CellView& cv,
-                                const ForceOut& out, float pre, cudaStream_t st, int tile) {
-    LJFixed<N> p;
-    static_cast<LJPair&>(p) = lj;
-    return run_mixed(p, lj.rc2f, g, cv, out, pre, st, tile);
+// The plugin's pair functor (LennardJones with its exponent fixed at compile
+// time for the common ljNum values) handed to run(pair, rc2f).
+template <class Run>
+static cudaError_t with_pair(const ForceSetup& fs, Run&& run) {
+    switch (fs.kind) {
+    case 1: return run(fs.ao, fs.ao.rc2f);
+    case 2: {
+        auto fixed = [&](auto p) {
+            static_cast<LJPair&>(p) = fs.lj;
+            return run(p, fs.lj.rc2f);
+        };
+        switch (fs.lj.n) {
+        case 0: return fixed(LJFixed<0>{});
+        case 6: return fixed(LJFixed<6>{});
+        case 12: return fixed(LJFixed<12>{});
+        case 18: return fixed(LJFixed<18>{});
+        default: return run(fs.lj, fs.lj.rc2f);
+        }
+    }
+    case 3: return run(fs.cal, fs.cal.rc2f);
+    case 4: {
+        const float rc2f = fs.ao.rc2f > fs.lj.rc2f ? fs.ao.rc2f : fs.lj.rc2f;
+        return run(ComboPairF{fs.ao, fs.lj}, rc2f);
+    }
+    }
+    return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_forces_mixed(const ForceSetup& fs, const DevGeom& g, const CellView& cv,
                                 const ForceOut& out, cudaStream_t st) {
-    const float pre = fs.pre_rc2f;
-    const int t = fs.tile;
-    switch (fs.kind) {
-    case 1: return run_mixed(fs.ao, fs.ao.rc2f, g, cv, out, pre, st, t);
-    case 2:
-        switch (fs.lj.n) {
-        case 0: return run_lj_mixed<0>(fs.lj, g, cv, out, pre, st, t);
-        case 6: return run_lj_mixed<6>(fs.lj, g, cv, out, pre, st, t);
-        case 12: return run_lj_mixed<12>(fs.lj, g, cv, out, pre, st, t);
-        case 18: return run_lj_mixed<18>(fs.lj, g, cv, out, pre, st, t);
-        default: return run_mixed(fs.lj, fs.lj.rc2f, g, cv, out, pre, st, t);
-        }
-    case 3: return run_mixed(fs.cal, fs.cal.rc2f, g, cv, out, pre, st, t);
-    case 4: {
-        const float rc2f = fs.ao.rc2f > fs.lj.rc2f ? fs.ao.rc2f : fs.lj.rc2f;
-        return run_mixed(ComboPairF{fs.ao, fs.lj}, rc2f, g, cv, out, pre, st, t);
-    }
-    }
-    return cudaErrorInvalidValue;
+    return with_pair(fs, [&](auto p, float rc2f) {
+        const MixedBody<decltype(p)> body{p, rc2f};
+        if (fs.tile) return launch_force_cells(body, g, cv, out, fs.pre_rc2f, st);
+        return launch_force_pass(body, g, cv, out, fs.pre_rc2f, st);
+    });
+}
+
+cudaError_t launch_forces_list(const ForceSetup& fs, const DevGeom& g, const PairList& pl,
+                               const ForceOut& out, cudaStream_t st) {
+    return with_pair(fs, [&](auto p, float rc2f) {
+        return launch_force_list(MixedBody<decltype(p)>{p, rc2f}, g, pl, out, st);
+    });
+}
+
+cudaError_t launch_list_build(const DevGeom& g, const CellView& cv, const ListBuild& lb,
+                              uint32_t* err, cudaStream_t st) {
+    const ListBody body{lb.list, lb.count, lb.stride, lb.cap, g.n};
+    const ForceOut out{nullptr, nullptr, nullptr, err, lb.gate};
+    return launch_force_pass(body, g, cv, out, lb.pre_r2, st);
 }
 
 // The update of the mixed form: the same FP64 arithmetic as psim_exact.cu's

@@ -171,6 +171,38 @@ __device__ __forceinline__ void load_noise(const NoiseView& nz, uint32_t seed, i
 // The system-order update: gathers the previous state through perm, writes
 // the new state in the current cell order, and hashes + counts the new
 // positions into the next grid.
+// The new position in pair-list order: the periodic image nearest the
+// position at the list build (|x - build| < L/2 picks it), as an exact float
+// pair; raises the rebuild flag when it has moved more than sqrt(ldisp2).
+__device__ __forceinline__ void list_position(const VgbSystemArgs& a, int f, const double xn[3],
+                                              const DevGeom& g) {
+    const int s = a.lslot[f];
+    const float4 b = a.lbuild[s];
+    const float bb[3] = {b.x, b.y, b.z};
+    const float halff = 0.5f * g.Lhi;
+    float h[3], l[3], d2 = 0.f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        double u = xn[k];
+        float hk = (float)u;
+        const float dk = hk - bb[k];
+        if (dk > halff) {
+            u -= g.L;
+            hk = (float)u;
+        } else if (dk < -halff) {
+            u += g.L;
+            hk = (float)u;
+        }
+        h[k] = hk;
+        l[k] = (float)(u - (double)hk);
+        const float e = hk - bb[k];
+        d2 += e * e;
+    }
+    a.lposh[s] = make_float4(h[0], h[1], h[2], b.w);
+    a.lposl[s] = make_float4(l[0], l[1], l[2], 0.f);
+    if (d2 > a.ldisp2) *a.lflag_set = 1;
+}
+
 template <class Tag>
 __global__ void __launch_bounds__(256)
 vgb_system_kernel(VgbSystemArgs a, VgbParams p, DevGeom g, NoiseView nz) {
@@ -207,6 +239,8 @@ vgb_system_kernel(VgbSystemArgs a, VgbParams p, DevGeom g, NoiseView nz) {
         a.vel[3 * (size_t)tag + 1] = v[1];
         a.vel[3 * (size_t)tag + 2] = v[2];
     }
+    if (a.lslot) list_position(a, f, xn, g);
+    if (f == 0 && a.lflag_clear) *a.lflag_clear = 0;
     const int key = hash_pos(xn, g, err);
     a.key[f] = key;
     a.rank[f] = atomicAdd(&a.count[key], 1);

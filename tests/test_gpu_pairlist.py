@@ -1,0 +1,133 @@
+"""The mixed form's Verlet pair list: the same pair terms as the 27-cell walk
+every step, so a run with a skin follows the run without one up to FP32
+summation order, across list rebuilds and periodic wraps."""
+import numpy as np
+import pytest
+
+from gpu_helpers import lattice_state, rel_norm, rsa_state
+
+pytestmark = pytest.mark.gpu
+
+DT, KT = 0.002, 1.5
+
+
+def run(psim, g, force, pos, rad, vel, noise, steps, skin, precision=1):
+    s = psim.System(g, force, gamma=1.0, dt=DT, kT=KT, vel_freq=1000, seed=7,
+                    precision=precision, noise_mode=psim.NOISE_INJECTED, skin=skin)
+    s.upload(pos, rad, vel=vel)
+    s.set_noise(noise, steps)
+    s.step(steps)
+    out = s.download()
+    out["builds"] = s.list_builds()
+    hi, cse, srt = s.download_cells()
+    out["hi"], out["cse"] = hi, cse
+    s.close()
+    return out
+
+
+def lj_liquid(psim):
+    # rho = 0.8 LJ, 2048 particles in a 13.7 box: 4^3 cells of 3.42 leave room
+    # for a 0.9 skin; a quarter of the particles sit in boundary cells
+    pos, rad, box = lattice_state(8, (4 / 0.8) ** (1 / 3), 0.08, seed=40)
+    n = len(rad)
+    g = psim.geometry(n, box, box / 4, 4)
+    p = psim.make_force("LJ", 2.5, kT=KT, well_depth=1 / KT, lj_num=6, yukawa_strength=0.0)
+    return g, p, pos, rad
+
+
+def ao_colloids(psim):
+    n, box, scale = 4000, 21.0, 7
+    pos, rad = rsa_state(n, box, seed=41)
+    return psim.geometry(n, box, box / scale, scale), psim.make_force("AO", 1.1, kT=1.0,
+                                                                        well_depth=0.25), pos, rad
+
+
+def ao_yukawa(psim):
+    n, box, scale = 3000, 26.0, 6
+    pos, rad = rsa_state(n, box, seed=42)
+    p = psim.make_force("AO_YUK", 1.1, kT=1.0, well_depth=0.1875, cutoff2=3.0, well_depth2=1.0,
+                        yukawa_strength=2183.93, debye_length=0.25, lj_num=0)
+    return psim.geometry(n, box, box / scale, scale), p, pos, rad
+
+
+SYSTEMS = {"lj_liquid": lj_liquid, "ao": ao_colloids, "ao_yukawa": ao_yukawa}
+
+
+@pytest.mark.parametrize("name", sorted(SYSTEMS))
+@pytest.mark.parametrize("skin", [0.1, 0.4])
+def test_pairlist_run_follows_cell_walk(psim, name, skin):
+    g, p, pos, rad = SYSTEMS[name](psim)
+    n = g.n_particles
+    rng = np.random.default_rng(43)
+    vel = rng.standard_normal(3 * n) * np.sqrt(KT)
+    steps = 60
+    noise = rng.standard_normal(steps * n * 6)
+    ref = run(psim, g, p, pos, rad, vel, noise, steps, 0.0)
+    got = run(psim, g, p, pos, rad, vel, noise, steps, skin)
+    assert ref["builds"] == 0
+    assert got["builds"] >= 1                      # the list was rebuilt on the way
+    # a missing or doubled pair term would show as an O(1) relative force error;
+    # the FP32 summation order alone moves the steep AO core's forces ~1e-7
+    assert rel_norm(got["frc"], ref["frc"]) < 1e-5
+    d = got["pos"] - ref["pos"]
+    d -= g.box_size * np.round(d / g.box_size)
+    assert np.max(np.abs(d)) < 1e-6
+    assert rel_norm(got["vel"], ref["vel"]) < 1e-5
+    # the reference's cell list is still rebuilt every step
+    assert np.array_equal(got["hi"], ref["hi"]) and np.array_equal(got["cse"], ref["cse"])
+
+
+def test_pairlist_run_tracks_fp64(psim):
+    g, p, pos, rad = lj_liquid(psim)
+    n = g.n_particles
+    rng = np.random.default_rng(44)
+    vel = rng.standard_normal(3 * n) * np.sqrt(KT)
+    steps = 40
+    noise = rng.standard_normal(steps * n * 6)
+    ref = run(psim, g, p, pos, rad, vel, noise, steps, 0.0, precision=0)
+    got = run(psim, g, p, pos, rad, vel, noise, steps, 0.3)
+    assert rel_norm(got["frc"], ref["frc"]) < 1e-5
+    d = got["pos"] - ref["pos"]
+    d -= g.box_size * np.round(d / g.box_size)
+    assert np.max(np.abs(d)) < 1e-6
+
+
+def test_pairlist_is_deterministic(psim):
+    g, p, pos, rad = ao_colloids(psim)
+    outs = []
+    for _ in range(2):
+        s = psim.System(g, p, gamma=1.0, dt=0.001, kT=1.0, precision=psim.PRECISION_MIXED,
+                        noise_mode=psim.NOISE_PHILOX, skin=0.2)
+        s.upload(pos, rad)
+        for k in (1, 5, 7, 30):
+            s.step(k)
+        outs.append(s.download())
+        s.close()
+    for k in outs[0]:
+        assert np.array_equal(outs[0][k], outs[1][k])
+
+
+def test_pairlist_overlap_is_7704(psim):
+    n, box, scale = 500, 12.0, 4
+    pos, rad = rsa_state(n, box, seed=45)
+    pos = pos.reshape(-1, 3)
+    pos[1] = pos[0] + np.array([0.3, 0.0, 0.0])
+    pos = np.mod(pos, box).reshape(-1)
+    g = psim.geometry(n, box, box / scale, scale)
+    s = psim.System(g, psim.make_force("AO", 1.1, well_depth=0.5), precision=psim.PRECISION_MIXED,
+                    noise_mode=psim.NOISE_PHILOX, skin=0.4)
+    s.upload(pos, rad)
+    with pytest.raises(psim.PsimError) as e:
+        s.step(3)
+    assert e.value.code == psim.ERR_OVERLAP
+
+
+def test_pairlist_skin_is_checked(psim):
+    g, p, pos, rad = lj_liquid(psim)
+    with pytest.raises(psim.PsimError) as e:     # cellSize 3.42 < 2.5 + 1.0
+        psim.System(g, p, precision=psim.PRECISION_MIXED, skin=1.0)
+    assert e.value.code == psim.ERR_INPUT
+    with pytest.raises(psim.PsimError) as e:     # the plain FP64 form walks the cells
+        psim.System(g, p, precision=psim.PRECISION_FP64, skin=0.3)
+    assert e.value.code == psim.ERR_INPUT
+    assert psim.auto_skin(g, p) == pytest.approx(0.4)
