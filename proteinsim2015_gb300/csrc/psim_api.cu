@@ -778,7 +778,7 @@ struct psim_system {
     double skin = 0.0;
     int lcap = 0;
     float lpre = 0.f, ldisp2 = 0.f;
-    DevBuf lslot[2], lbuild, list, lcount, lflag;
+    DevBuf lslot[2], lbuild, lpos, list, lcount, lflag;
 };
 
 namespace {
@@ -829,8 +829,8 @@ int enqueue_step(psim_system* s, long long t, cudaEvent_t* evs) {
     if (s->cfg.precision == PSIM_PRECISION_FP64) {
         PSIM_CUDA(launch_forces_fp64(s->fs, s->g, cv, fo, st));
     } else if (s->list_on) {
-        PairList pl{s->lslot[ob].as<int>(), s->posh.as<float4>(), s->posl.as<float4>(),
-                    s->lcount.as<int>(), s->list.as<uint32_t>(), n};
+        PairList pl{s->lslot[ob].as<int>(), s->lpos.as<float4>(), s->lcount.as<int>(),
+                    s->list.as<uint32_t>(), n};
         PSIM_CUDA(launch_forces_list(s->fs, s->g, pl, fo, st));
     } else {
         PSIM_CUDA(launch_forces_mixed(s->fs, s->g, cv, fo, st));
@@ -861,8 +861,7 @@ int enqueue_step(psim_system* s, long long t, cudaEvent_t* evs) {
     if (s->list_on) {
         a.lslot = s->lslot[ob].as<int>();
         a.lbuild = s->lbuild.as<float4>();
-        a.lposh = s->posh.as<float4>();
-        a.lposl = s->posl.as<float4>();
+        a.lpos = s->lpos.as<float4>();
         a.lflag_set = lflag;
         a.lflag_clear = s->lflag.as<int>() + (1 - (t & 1));
         a.ldisp2 = s->ldisp2;
@@ -905,6 +904,7 @@ int enqueue_step(psim_system* s, long long t, cudaEvent_t* evs) {
         ca.lslot_in = s->lslot[ob].as<int>();
         ca.lslot_out = s->lslot[nob].as<int>();
         ca.lbuild = s->lbuild.as<float4>();
+        ca.lpos = s->lpos.as<float4>();
     }
     PSIM_CUDA(launch_canonicalize(ca, st));
     if (s->list_on) PSIM_CUDA(enqueue_list_build(s, ncb, lflag));
@@ -1038,20 +1038,21 @@ psim_system* psim_system_create(const psim_system_config* cfg) {
     ok = ok && !s->cellid.ensure(4 * n) && !s->key.ensure(4 * n) && !s->rank.ensure(4 * n) &&
          !s->tmp.ensure(4 * n) && !s->start.ensure(4 * nc) &&
          !s->scratch.ensure(4 * scan_scratch_ints(g.ncell)) &&
-         !s->posh.ensure(16 * (n + (list_on ? 1 : 0))) &&
+         !s->posh.ensure(16 * n) &&
          !s->vel.ensure(24 * n) && !s->err.ensure(4) && !s->state.ensure(sizeof(StepState)) &&
          !s->occ.ensure(4);
     if (ok && cfg->precision == PSIM_PRECISION_FP64) ok = !s->posd.ensure(32 * n);
     if (ok && cfg->precision == PSIM_PRECISION_MIXED)
-        ok = !s->posl.ensure(16 * (n + (list_on ? 1 : 0)));
+        ok = !s->posl.ensure(16 * n);
     if (ok && list_on) {
         ok = !s->lslot[0].ensure(4 * n) && !s->lslot[1].ensure(4 * n) && !s->lbuild.ensure(16 * n) &&
-             !s->list.ensure(4 * n * (size_t)s->lcap) && !s->lcount.ensure(4 * n) &&
-             !s->lflag.ensure(8) && cudaMemset(s->lflag.p, 0, 8) == cudaSuccess;
+             !s->lpos.ensure(32 * (n + 1)) && !s->list.ensure(4 * n * (size_t)s->lcap) &&
+             !s->lcount.ensure(4 * n) && !s->lflag.ensure(8) &&
+             cudaMemset(s->lflag.p, 0, 8) == cudaSuccess;
         // the ghost slot n that pads the lists: far from every particle
-        const float4 gh = make_float4(1e18f, 1e18f, 1e18f, 0.f), gl = make_float4(0.f, 0.f, 0.f, 0.f);
-        ok = ok && cudaMemcpy(s->posh.as<float4>() + n, &gh, 16, cudaMemcpyHostToDevice) == cudaSuccess &&
-             cudaMemcpy(s->posl.as<float4>() + n, &gl, 16, cudaMemcpyHostToDevice) == cudaSuccess;
+        const float4 ghost[2] = {make_float4(1e18f, 1e18f, 1e18f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f)};
+        ok = ok && cudaMemcpy(s->lpos.as<float4>() + 2 * n, ghost, 32, cudaMemcpyHostToDevice) ==
+                       cudaSuccess;
     }
     if (ok) ok = cudaMemset(s->err.p, 0, 4) == cudaSuccess &&
                  cudaMemset(s->state.p, 0, sizeof(StepState)) == cudaSuccess;
@@ -1071,8 +1072,8 @@ void psim_system_destroy(psim_system* s) {
     drop_graphs(s);
     DevBuf* arrs[] = {&s->cellid, &s->key, &s->rank, &s->tmp, &s->start, &s->scratch, &s->posd,
                       &s->posh, &s->posl, &s->vel, &s->err, &s->state, &s->occ, &s->noise,
-                      &s->snap, &s->lslot[0], &s->lslot[1], &s->lbuild, &s->list, &s->lcount,
-                      &s->lflag};
+                      &s->snap, &s->lslot[0], &s->lslot[1], &s->lbuild, &s->lpos, &s->list,
+                      &s->lcount, &s->lflag};
     for (DevBuf* b : arrs) b->release();
     for (int k = 0; k < 2; ++k) {
         s->pos[k].release(); s->pos0[k].release(); s->mem[k].release(); s->tag[k].release();
@@ -1168,6 +1169,7 @@ int psim_system_upload(psim_system* s, const double* pos, const double* pos0, co
         ca.rebuild = s->lflag.as<int>();
         ca.lslot_out = s->lslot[ob].as<int>();
         ca.lbuild = s->lbuild.as<float4>();
+        ca.lpos = s->lpos.as<float4>();
     }
     PSIM_CUDA(launch_canonicalize(ca, st));
     if (s->list_on) {

@@ -150,14 +150,19 @@ __global__ void __launch_bounds__(256) canonicalize_kernel(CanonArgs a, int vel_
         if (pos_out) {
             const double x = a.x[f], y = a.y[f], z = a.z[f];
             if (a.posd) a.posd[g] = make_double4_32a(x, y, z, R);
-            const float hx = (float)x, hy = (float)y, hz = (float)z;
-            const float4 h = make_float4(hx, hy, hz, (float)R);
+            float4 h, l;
+            split_f64(x, h.x, l.x);
+            split_f64(y, h.y, l.y);
+            split_f64(z, h.z, l.z);
+            h.w = (float)R;
+            l.w = __int_as_float(g);  // the slot, which the pair-list build reads
             a.posh[g] = h;
+            if (a.posl) a.posl[g] = l;
             if (a.lbuild) a.lbuild[g] = h;
-            // .w carries the slot, which the pair-list build reads
-            if (a.posl)
-                a.posl[g] = make_float4((float)(x - (double)hx), (float)(y - (double)hy),
-                                        (float)(z - (double)hz), __int_as_float(g));
+            if (a.lpos) {
+                a.lpos[2 * (size_t)g] = h;
+                a.lpos[2 * (size_t)g + 1] = l;
+            }
         }
     }
     if (a.state && a.advance && p == 0) {
@@ -243,11 +248,14 @@ import_sorted_kernel(int n, const double* sorted, const int32_t* hi, DevGeom g, 
     const double x = sorted[4 * (size_t)i], y = sorted[4 * (size_t)i + 1];
     const double z = sorted[4 * (size_t)i + 2], R = sorted[4 * (size_t)i + 3];
     posd[i] = make_double4_32a(x, y, z, R);
-    const float hx = (float)x, hy = (float)y, hz = (float)z;
-    posh[i] = make_float4(hx, hy, hz, (float)R);
-    if (posl)
-        posl[i] = make_float4((float)(x - (double)hx), (float)(y - (double)hy),
-                              (float)(z - (double)hz), 0.0f);
+    float4 h, l;
+    split_f64(x, h.x, l.x);
+    split_f64(y, h.y, l.y);
+    split_f64(z, h.z, l.z);
+    h.w = (float)R;
+    l.w = __int_as_float(i);
+    posh[i] = h;
+    if (posl) posl[i] = l;
     int t = hi[2 * (size_t)i + 1];
     if (t < 0 || t >= n) {  // an original index outside [0, n): refuse, stay in bounds
         atomicOr(err, (uint32_t)EBIT_INDEX);

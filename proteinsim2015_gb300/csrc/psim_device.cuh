@@ -51,6 +51,26 @@ __device__ __forceinline__ int cell_coord(double x, const DevGeom& g) {
     return (int)floor(x / g.cs);
 }
 
+// x = hi + lo: hi is x with its significand cut to FP32's 24 bits (toward
+// zero), lo the remainder rounded to FP32 (|hi + lo - x| <= 2^-47 |x|).  Built
+// from the bits of x with integer and FP32 operations only: on GB300 the FP64
+// unit, which also performs double<->float conversions, runs at 1/64 of the
+// FP32 rate.  Positions outside [2^-74, 2^127) in magnitude are not used
+// here: below 2^-126 hi = 0, below 2^-74 lo = 0.
+__device__ __forceinline__ void split_f64(double x, float& hi, float& lo) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const uint32_t top = (uint32_t)(b >> 32);
+    const uint32_t sign = top & 0x80000000u;
+    const int e = (int)((top >> 20) & 0x7FFu);               // biased FP64 exponent
+    const uint32_t m23 = (uint32_t)(b >> 29) & 0x7FFFFFu;    // the significand's top 23 bits
+    const uint32_t rem = (uint32_t)b & 0x1FFFFFFFu;          // the 29 bits below them
+    hi = (e > 896 && e < 1151) ? __uint_as_float(sign | ((uint32_t)(e - 896) << 23) | m23) : 0.f;
+    // rem is an integer in units of 2^(e - 1075)
+    const float unit = (e > 948) ? __uint_as_float((uint32_t)(e - 948) << 23) : 0.f;
+    const float r = __uint2float_rn(rem) * unit;
+    lo = sign ? -r : r;
+}
+
 // Neighbour cell index wrapped into [0, s) as the reference does
 // ((c % s) + s when negative, AOPotential.cpp:154-160), and the periodic
 // image it implies (-1, 0 or +1 boxes).

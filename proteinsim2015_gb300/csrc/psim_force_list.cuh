@@ -97,11 +97,13 @@ force_list_kernel(Body body, DevGeom g, PairList pl, ForceOut out) {
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= g.n || *out.err) return;
     const int s = pl.lslot[f];
-    const float4 hh = pl.posh[s];
+    const float4 hh = pl.pos[2 * (size_t)s];
+    // the body reads the home's low part as cv.posl[i]: point it at the
+    // records' second halves, indexed in float4 units
     CellView cv{};
-    cv.posl = pl.posl;
+    cv.posl = pl.pos + 1;
     typename Body::Home home;
-    body.load_home(cv, s, home);
+    body.load_home(cv, 2 * s, home);
     typename Body::Shifted hs0;
     body.shift(home, hh, 0, 0, 0, g, hs0);
     typename Body::Acc acc;
@@ -119,8 +121,8 @@ force_list_kernel(Body body, DevGeom g, PairList pl, ForceOut out) {
 #pragma unroll
             for (int u = 0; u < kBatch; ++u) {
                 const int j = (int)(e[u] & kListIdxMask);
-                nh[u] = pl.posh[j];
-                nl[u] = pl.posl[j];
+                nh[u] = pl.pos[2 * (size_t)j];       // one 32-byte sector per neighbour
+                nl[u] = pl.pos[2 * (size_t)j + 1];
             }
 #pragma unroll
             for (int u = 0; u < kBatch; ++u) {

@@ -56,8 +56,9 @@ constexpr uint32_t kListIdxMask = (1u << kListIdxBits) - 1u;
 constexpr int kListFold = 8;   // pair terms per Kahan fold
 struct PairList {
     const int* lslot;      // list slot of each current storage slot
-    const float4* posh;    // list order, unwrapped: {x, y, z, R} rounded to FP32
-    const float4* posl;    // list order: low parts
+    // list order, unwrapped, one 32-byte record per slot (+ the ghost slot n):
+    // pos[2 s] = {x, y, z, R} high parts, pos[2 s + 1] = low parts
+    const float4* pos;
     const int* count;      // entries of each list slot
     const uint32_t* list;
     int stride;
@@ -130,8 +131,7 @@ struct VgbSystemArgs {
     // flag) is cleared.
     const int* lslot;
     const float4* lbuild;       // list order: positions at the build, .w radius
-    float4* lposh;
-    float4* lposl;
+    float4* lpos;               // PairList::pos
     int* lflag_set;
     int* lflag_clear;
     float ldisp2;
@@ -206,6 +206,7 @@ struct CanonArgs {
     const int* lslot_in;
     int* lslot_out;
     float4* lbuild;
+    float4* lpos;           // PairList::pos, written with posh/posl
 };
 cudaError_t launch_canonicalize(const CanonArgs& a, cudaStream_t st);
 

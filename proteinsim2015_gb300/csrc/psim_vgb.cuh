@@ -183,23 +183,15 @@ __device__ __forceinline__ void list_position(const VgbSystemArgs& a, int f, con
     float h[3], l[3], d2 = 0.f;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        double u = xn[k];
-        float hk = (float)u;
-        const float dk = hk - bb[k];
-        if (dk > halff) {
-            u -= g.L;
-            hk = (float)u;
-        } else if (dk < -halff) {
-            u += g.L;
-            hk = (float)u;
-        }
-        h[k] = hk;
-        l[k] = (float)(u - (double)hk);
-        const float e = hk - bb[k];
+        split_f64(xn[k], h[k], l[k]);
+        const float dk = h[k] - bb[k];
+        if (dk > halff || dk < -halff)  // wrapped since the build: the other image
+            split_f64(dk > 0.f ? xn[k] - g.L : xn[k] + g.L, h[k], l[k]);
+        const float e = h[k] - bb[k];
         d2 += e * e;
     }
-    a.lposh[s] = make_float4(h[0], h[1], h[2], b.w);
-    a.lposl[s] = make_float4(l[0], l[1], l[2], 0.f);
+    a.lpos[2 * (size_t)s] = make_float4(h[0], h[1], h[2], b.w);
+    a.lpos[2 * (size_t)s + 1] = make_float4(l[0], l[1], l[2], 0.f);
     if (d2 > a.ldisp2) *a.lflag_set = 1;
 }
 
