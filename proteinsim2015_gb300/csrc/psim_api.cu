@@ -776,9 +776,9 @@ struct psim_system {
     // counts, and the two step-parity rebuild flags
     bool list_on = false;
     double skin = 0.0;
-    int lcap = 0;
-    float lpre = 0.f, ldisp2 = 0.f;
-    DevBuf lslot[2], lbuild, lpos, list, lcount, lflag;
+    int lcap = 0, hcap = 0;
+    float lpre = 0.f, ldisp2 = 0.f, hr = 0.f;
+    DevBuf lslot[2], lbuild, lpos, list, lcount, lflag, lhalo, lhcount;
 };
 
 namespace {
@@ -803,12 +803,27 @@ Phase phase_of(long long t) {
 
 double* d3(DevBuf& b, int n, int k) { return b.as<double>() + (size_t)k * n; }
 
+// The list-order records the canonicalisation writes when the list is
+// rebuilt: positions, build positions and halo images.
+void set_halo_args(psim_system* s, CanonArgs& ca) {
+    ca.lbuild = s->lbuild.as<float4>();
+    ca.lpos = s->lpos.as<float4>();
+    ca.lhalo = s->lhalo.as<int>();
+    ca.lhcount = s->lhcount.as<int>();
+    ca.hcap = s->hcap;
+    ca.hr = s->hr;
+    ca.Lf = (float)s->g.L;
+    ca.Lhi = s->g.Lhi;
+    ca.Llo = s->g.Llo;
+}
+
 // The pair-list build on the cell order just made (count buffer cb), run
 // only when *gate != 0.
 cudaError_t enqueue_list_build(psim_system* s, int cb, const int* gate) {
     CellView cv{nullptr, s->posh.as<float4>(), s->posl.as<float4>(), s->cellid.as<int>(),
                 s->start.as<int>(), s->count[cb].as<int>()};
-    ListBuild lb{s->list.as<uint32_t>(), s->lcount.as<int>(), s->n, s->lcap, s->lpre, gate};
+    ListBuild lb{s->list.as<uint32_t>(), s->lcount.as<int>(), s->n, s->lcap, s->lpre, gate,
+                 s->lhalo.as<int>()};
     return launch_list_build(s->g, cv, lb, s->err.as<uint32_t>(), s->st);
 }
 
@@ -865,6 +880,8 @@ int enqueue_step(psim_system* s, long long t, cudaEvent_t* evs) {
         a.lflag_set = lflag;
         a.lflag_clear = s->lflag.as<int>() + (1 - (t & 1));
         a.ldisp2 = s->ldisp2;
+        a.lhalo = s->lhalo.as<int>();
+        a.lhcount = s->lhcount.as<int>();
     }
     NoiseView nz{s->cfg.noise_mode, s->noise.as<double>(), s->noise_first, s->noise_steps};
     if (s->cfg.precision == PSIM_PRECISION_FP64)
@@ -903,8 +920,7 @@ int enqueue_step(psim_system* s, long long t, cudaEvent_t* evs) {
         ca.rebuild = lflag;
         ca.lslot_in = s->lslot[ob].as<int>();
         ca.lslot_out = s->lslot[nob].as<int>();
-        ca.lbuild = s->lbuild.as<float4>();
-        ca.lpos = s->lpos.as<float4>();
+        set_halo_args(s, ca);
     }
     PSIM_CUDA(launch_canonicalize(ca, st));
     if (s->list_on) PSIM_CUDA(enqueue_list_build(s, ncb, lflag));
@@ -987,8 +1003,8 @@ psim_system* psim_system_create(const psim_system_config* cfg) {
              g.cs, rc + skin);
         return nullptr;
     }
-    if (list_on && g.n > (int)kListIdxMask) {
-        fail(PSIM_ERR_INPUT, "the pair list indexes at most %u particles", kListIdxMask);
+    if (list_on && g.n > (1 << 28)) {
+        fail(PSIM_ERR_INPUT, "the pair list indexes at most 2^28 particles");
         return nullptr;
     }
     if (ensure_device()) return nullptr;
@@ -1021,6 +1037,12 @@ psim_system* psim_system_create(const psim_system_config* cfg) {
         const double ulpL = std::ldexp(1.0, std::ilogb(std::max(g.L, 1.0)) - 23);
         const double dmax = 0.5 * skin * (1.0 - 1e-3) - 4.0 * ulpL;
         s->ldisp2 = dmax > 0.0 ? (float)(dmax * dmax) : 0.f;
+        // halo images for the particles within hr of a face: beyond the list
+        // test's radius, so every pair the build finds across an edge has one
+        s->hr = (float)(std::sqrt((double)s->lpre) + 1e-3 * rl + 16.0 * ulpL);
+        const double p = 2.0 * s->hr / g.L;   // a particle's chance of an image per axis
+        const double expect = g.n * ((1.0 + p) * (1.0 + p) * (1.0 + p) - 1.0);
+        s->hcap = (int)std::min(std::min(7.0 * g.n, 1.3 * expect + 1024.0), (double)kHaloBaseMax);
     }
     const size_t n = (size_t)g.n, nc = (size_t)g.ncell;
     bool ok = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) == cudaSuccess &&
@@ -1046,9 +1068,11 @@ psim_system* psim_system_create(const psim_system_config* cfg) {
         ok = !s->posl.ensure(16 * n);
     if (ok && list_on) {
         ok = !s->lslot[0].ensure(4 * n) && !s->lslot[1].ensure(4 * n) && !s->lbuild.ensure(16 * n) &&
-             !s->lpos.ensure(32 * (n + 1)) && !s->list.ensure(4 * n * (size_t)s->lcap) &&
-             !s->lcount.ensure(4 * n) && !s->lflag.ensure(8) &&
-             cudaMemset(s->lflag.p, 0, 8) == cudaSuccess;
+             !s->lpos.ensure(32 * (n + 1 + (size_t)s->hcap)) &&
+             !s->list.ensure(4 * n * (size_t)s->lcap) && !s->lcount.ensure(4 * n) &&
+             !s->lflag.ensure(8) && !s->lhalo.ensure(4 * n) && !s->lhcount.ensure(4) &&
+             cudaMemset(s->lflag.p, 0, 8) == cudaSuccess &&
+             cudaMemset(s->lhcount.p, 0, 4) == cudaSuccess;
         // the ghost slot n that pads the lists: far from every particle
         const float4 ghost[2] = {make_float4(1e18f, 1e18f, 1e18f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f)};
         ok = ok && cudaMemcpy(s->lpos.as<float4>() + 2 * n, ghost, 32, cudaMemcpyHostToDevice) ==
@@ -1073,7 +1097,7 @@ void psim_system_destroy(psim_system* s) {
     DevBuf* arrs[] = {&s->cellid, &s->key, &s->rank, &s->tmp, &s->start, &s->scratch, &s->posd,
                       &s->posh, &s->posl, &s->vel, &s->err, &s->state, &s->occ, &s->noise,
                       &s->snap, &s->lslot[0], &s->lslot[1], &s->lbuild, &s->lpos, &s->list,
-                      &s->lcount, &s->lflag};
+                      &s->lcount, &s->lflag, &s->lhalo, &s->lhcount};
     for (DevBuf* b : arrs) b->release();
     for (int k = 0; k < 2; ++k) {
         s->pos[k].release(); s->pos0[k].release(); s->mem[k].release(); s->tag[k].release();
@@ -1168,8 +1192,8 @@ int psim_system_upload(psim_system* s, const double* pos, const double* pos0, co
         PSIM_CUDA(cudaMemcpyAsync(s->lflag.p, &one, 4, cudaMemcpyHostToDevice, st));
         ca.rebuild = s->lflag.as<int>();
         ca.lslot_out = s->lslot[ob].as<int>();
-        ca.lbuild = s->lbuild.as<float4>();
-        ca.lpos = s->lpos.as<float4>();
+        set_halo_args(s, ca);
+        PSIM_CUDA(cudaMemsetAsync(s->lhcount.p, 0, 4, st));
     }
     PSIM_CUDA(launch_canonicalize(ca, st));
     if (s->list_on) {

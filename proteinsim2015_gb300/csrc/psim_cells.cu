@@ -162,6 +162,22 @@ __global__ void __launch_bounds__(256) canonicalize_kernel(CanonArgs a, int vel_
             if (a.lpos) {
                 a.lpos[2 * (size_t)g] = h;
                 a.lpos[2 * (size_t)g + 1] = l;
+                l.w = 0.f;
+                // images of a particle near a face, as halo records
+                uint32_t fl = halo_flags(h, a.hr, a.Lf);
+                const int m = halo_copies(fl);
+                int base = 0;
+                if (m > 0) {
+                    base = atomicAdd(a.lhcount, m);
+                    if (base + m > a.hcap) {
+                        atomicOr(a.err, EBIT_LIST);
+                        fl = 0;
+                        base = 0;
+                    } else {
+                        halo_write(a.lpos + 2 * ((size_t)a.n + 1), base, fl, h, l, a.Lhi, a.Llo);
+                    }
+                }
+                a.lhalo[g] = (base << 6) | (int)fl;
             }
         }
     }

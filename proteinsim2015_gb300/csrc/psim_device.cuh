@@ -71,6 +71,75 @@ __device__ __forceinline__ void split_f64(double x, float& hi, float& lo) {
     lo = sign ? -r : r;
 }
 
+// Knuth's TwoSum: s + e == a + b exactly.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// A position held as a float pair (h + l) moved by (sx, sy, sz) boxes, with
+// the box L = Lhi + Llo: the high parts exactly by TwoSum, the low parts
+// absorbing the rounding.
+__device__ __forceinline__ void image_shift(float4& h, float4& l, int sx, int sy, int sz,
+                                            float Lhi, float Llo) {
+    float ex, ey, ez;
+    two_sum(h.x, (float)sx * Lhi, h.x, ex);
+    two_sum(h.y, (float)sy * Lhi, h.y, ey);
+    two_sum(h.z, (float)sz * Lhi, h.z, ez);
+    l.x = (l.x + ex) + (float)sx * Llo;
+    l.y = (l.y + ey) + (float)sy * Llo;
+    l.z = (l.z + ez) + (float)sz * Llo;
+}
+
+// Periodic images a pair list needs of one particle: flag 2 bits per axis
+// (0: none, 1: the +L image -- the particle is within r of the low face --,
+// 3: the -L image, near the high face).  The images of a particle are its
+// copies shifted along every non-empty subset of its flagged axes, numbered
+// by the subset's bits in x, y, z order (1 .. 2^axes - 1).
+__device__ __forceinline__ uint32_t halo_flags(const float4& h, float r, float L) {
+    uint32_t f = 0;
+    f |= h.x < r ? 1u : (h.x > L - r ? 3u : 0u);
+    f |= (h.y < r ? 1u : (h.y > L - r ? 3u : 0u)) << 2;
+    f |= (h.z < r ? 1u : (h.z > L - r ? 3u : 0u)) << 4;
+    return f;
+}
+__device__ __forceinline__ int halo_axis(uint32_t flags, int axis) {
+    return (int)(flags << (30 - 2 * axis)) >> 30;  // sign-extend the 2-bit field
+}
+// The number of images of a particle with these flags.
+__device__ __forceinline__ int halo_copies(uint32_t flags) {
+    const int axes = (flags & 3u ? 1 : 0) + (flags & 12u ? 1 : 0) + (flags & 48u ? 1 : 0);
+    return (1 << axes) - 1;
+}
+// Image `num` (1 .. halo_copies) of a particle: its shift per axis.
+__device__ __forceinline__ void halo_shift(uint32_t flags, int num, int sh[3]) {
+    int bit = 0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int fk = halo_axis(flags, k);
+        sh[k] = 0;
+        if (fk != 0) {
+            if (num & (1 << bit)) sh[k] = fk;
+            ++bit;
+        }
+    }
+}
+// Writes the images of a particle at list slot s (positions h, l) into its
+// halo records pos[2 (base + num - 1)], base = the particle's first halo slot.
+__device__ __forceinline__ void halo_write(float4* pos, int base, uint32_t flags, const float4& h,
+                                           const float4& l, float Lhi, float Llo) {
+    const int m = halo_copies(flags);
+    for (int num = 1; num <= m; ++num) {
+        int sh[3];
+        halo_shift(flags, num, sh);
+        float4 hh = h, ll = l;
+        image_shift(hh, ll, sh[0], sh[1], sh[2], Lhi, Llo);
+        pos[2 * (size_t)(base + num - 1)] = hh;
+        pos[2 * (size_t)(base + num - 1) + 1] = ll;
+    }
+}
+
 // Neighbour cell index wrapped into [0, s) as the reference does
 // ((c % s) + s when negative, AOPotential.cpp:154-160), and the periodic
 // image it implies (-1, 0 or +1 boxes).

@@ -12,49 +12,45 @@
 //
 //   build  the warp kernel of psim_force.cuh with a body that appends, rather
 //          than evaluates, the candidates within rc + skin (plus the rounding
-//          margin of its FP32 test): entry = neighbour slot | image code.
-//          It runs on the step's own cell list, so list order is the cell
-//          order of the build step, and it needs cellSize >= rc + skin.
+//          margin of its FP32 test).  It runs on the step's own cell list, so
+//          list order is the cell order of the build step, and it needs
+//          cellSize >= rc + skin.  A pair across the box edge refers to a
+//          halo record: a copy of the neighbour shifted by the box, made for
+//          every particle within rc + skin of a face and rewritten with it
+//          each step, so the force pass does no periodic arithmetic.
 //   force  a thread per particle walks its list in FP32 with the plugin's pair
 //          body and Kahan-compensated sums (MixedBody, psim_mixed.cu).
 //
 // Positions in list order are kept as exact float pairs and *unwrapped*: the
 // integrator writes each particle's new position as the image nearest its
-// build position, so a pair's periodic image found at the build stays right
-// for the life of the list (the box is larger than 2 (rc + skin)).
+// build position (and its halo images beside it), so a pair's periodic image
+// found at the build stays right for the life of the list (the box is larger
+// than 2 (rc + skin)).
 #pragma once
 
 #include "psim_force.cuh"
 
 namespace psim {
 
-// image code of a list entry: 2 bits per axis (0: none, 1: +L, 3: -L) of the
-// shift applied to the home particle, as in the warp kernel's rows
-__device__ __forceinline__ uint32_t image_code(int sx, int sy, int sz) {
-    return ((uint32_t)(sx & 3) | ((uint32_t)(sy & 3) << 2) | ((uint32_t)(sz & 3) << 4))
-           << kListIdxBits;
-}
-__device__ __forceinline__ int image_axis(uint32_t code, int axis) {
-    return (int)(code << (30 - 2 * axis)) >> 30;  // sign-extend the 2-bit field
-}
-
-// Appends the candidates the warp kernel selects to the home particle's list,
-// then pads the list to a multiple of kListFold with the ghost slot (a
-// far-away dummy particle), so the force pass reads whole batches.  The
-// neighbour's slot travels in the .w lane of its low-part float4.
+// Appends the candidates the warp kernel selects to the home particle's
+// list, then pads the list to a multiple of kListFold with the ghost record
+// (a far-away dummy particle), so the force pass reads whole batches.  The
+// neighbour's slot travels in the .w lane of its low-part float4; a pair
+// across the box edge refers to the neighbour's halo record for that image.
 struct ListBody {
     uint32_t* list;
     int* count;
     int stride;
-    int cap;    // a multiple of kListFold
-    int ghost;  // the ghost slot (n)
+    int cap;           // a multiple of kListFold
+    int ghost;         // the ghost record (n); halo records follow it
+    const int* lhalo;
     using Aux = float4;
     struct Home {
         int i;
     };
     struct Shifted {
         int i;
-        uint32_t code;
+        int sx, sy, sz;   // the neighbour image x_j + s L of this row
     };
     struct Acc {
         int n;
@@ -65,11 +61,36 @@ struct ListBody {
     __device__ __forceinline__ void shift(const Home& h, const float4&, int sx, int sy, int sz,
                                           const DevGeom&, Shifted& o) const {
         o.i = h.i;
-        o.code = image_code(sx, sy, sz);
+        o.sx = sx;
+        o.sy = sy;
+        o.sz = sz;
     }
     __device__ __forceinline__ void eval(const float4&, const float4& lj, const Shifted& hs,
-                                         Acc& a, uint32_t&) const {
-        if (a.n < cap) list[(size_t)a.n * stride + hs.i] = __float_as_uint(lj.w) | hs.code;
+                                         Acc& a, uint32_t& err) const {
+        uint32_t j = __float_as_uint(lj.w);
+        if ((hs.sx | hs.sy | hs.sz) != 0) {
+            // image number: one bit per flagged axis, set where this row shifts
+            const int hal = lhalo[j];
+            const uint32_t fl = (uint32_t)(hal & 63);
+            const int s[3] = {hs.sx, hs.sy, hs.sz};
+            int num = 0, bit = 0;
+            bool ok = true;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const int fk = halo_axis(fl, k);
+                if (s[k] != 0) {
+                    ok = ok && fk == s[k];
+                    num |= 1 << bit;
+                }
+                if (fk != 0) ++bit;
+            }
+            if (!ok) {          // no record of that image: the margin failed
+                err |= EBIT_LIST;
+                return;
+            }
+            j = (uint32_t)(ghost + 1 + (hal >> 6) + num - 1);
+        }
+        if (a.n < cap) list[(size_t)a.n * stride + hs.i] = j;
         a.n++;
     }
     __device__ __forceinline__ void fold(Acc&) const {}
@@ -86,9 +107,10 @@ struct ListBody {
 };
 
 // A thread per particle (current storage order f): its list slot, its list,
-// its neighbours' list-order positions; the force is stored at f.  Lists are
-// padded to whole batches, so each batch's loads are issued together
-// before any of its pair terms.
+// its neighbours' records; the force is stored at f.  Lists are padded to
+// whole batches, so each batch's loads are issued together before any of its
+// pair terms, and every record holds the image the pair needs: no periodic
+// arithmetic per pair.
 template <class Body>
 __global__ void __launch_bounds__(128)
 force_list_kernel(Body body, DevGeom g, PairList pl, ForceOut out) {
@@ -104,8 +126,8 @@ force_list_kernel(Body body, DevGeom g, PairList pl, ForceOut out) {
     cv.posl = pl.pos + 1;
     typename Body::Home home;
     body.load_home(cv, 2 * s, home);
-    typename Body::Shifted hs0;
-    body.shift(home, hh, 0, 0, 0, g, hs0);
+    typename Body::Shifted hs;
+    body.shift(home, hh, 0, 0, 0, g, hs);
     typename Body::Acc acc;
     body.init(acc);
     uint32_t err = 0;
@@ -120,19 +142,11 @@ force_list_kernel(Body body, DevGeom g, PairList pl, ForceOut out) {
             for (int u = 0; u < kBatch; ++u) e[u] = __ldg(lp + (size_t)(k0 + b + u) * pl.stride);
 #pragma unroll
             for (int u = 0; u < kBatch; ++u) {
-                const int j = (int)(e[u] & kListIdxMask);
-                nh[u] = pl.pos[2 * (size_t)j];       // one 32-byte sector per neighbour
-                nl[u] = pl.pos[2 * (size_t)j + 1];
+                nh[u] = pl.pos[2 * (size_t)e[u]];       // one 32-byte sector per neighbour
+                nl[u] = pl.pos[2 * (size_t)e[u] + 1];
             }
 #pragma unroll
-            for (int u = 0; u < kBatch; ++u) {
-                const uint32_t code = e[u] >> kListIdxBits;
-                typename Body::Shifted hs = hs0;
-                if (code != 0)  // a pair across the box edge (rare: a branch)
-                    body.shift(home, hh, image_axis(code, 0), image_axis(code, 1),
-                               image_axis(code, 2), g, hs);
-                body.eval_masked(nh[u], nl[u], hs, acc, err);
-            }
+            for (int u = 0; u < kBatch; ++u) body.eval_masked(nh[u], nl[u], hs, acc, err);
         }
         body.fold(acc);
     }

@@ -48,18 +48,18 @@ cudaError_t launch_forces_fp64(const ForceSetup& fs, const DevGeom& g, const Cel
 cudaError_t launch_forces_mixed(const ForceSetup& fs, const DevGeom& g, const CellView& cv,
                                 const ForceOut& out, cudaStream_t st);
 
-// Verlet pair list of the mixed form (psim_force_list.cuh).  Entries are a
-// neighbour's list slot in the low kListIdxBits bits and the periodic image
-// of the pair above them; the list of slot s is list[k * stride + s].
-constexpr int kListIdxBits = 26;
-constexpr uint32_t kListIdxMask = (1u << kListIdxBits) - 1u;
+// Verlet pair list of the mixed form (psim_force_list.cuh).  Entries are
+// record slots: a particle's list slot (< n), the ghost n that pads lists, or
+// n + 1 + h for halo record h -- a periodic image of a particle near a face,
+// kept up to date beside it.  The list of slot s is list[k * stride + s].
 constexpr int kListFold = 8;   // pair terms per Kahan fold
+constexpr int kHaloBaseMax = (1 << 25) - 1;   // halo records per system
 struct PairList {
     const int* lslot;      // list slot of each current storage slot
     // list order, unwrapped, one 32-byte record per slot (+ the ghost slot n):
     // pos[2 s] = {x, y, z, R} high parts, pos[2 s + 1] = low parts
     const float4* pos;
-    const int* count;      // entries of each list slot
+    const int* count;      // entries of each list slot (a multiple of kListFold)
     const uint32_t* list;
     int stride;
 };
@@ -74,6 +74,7 @@ struct ListBuild {
     int cap;
     float pre_r2;
     const int* gate;
+    const int* lhalo;      // per list slot: first halo record << 6 | halo_flags
 };
 cudaError_t launch_list_build(const DevGeom& g, const CellView& cv, const ListBuild& lb,
                               uint32_t* err, cudaStream_t st);
@@ -135,6 +136,8 @@ struct VgbSystemArgs {
     int* lflag_set;
     int* lflag_clear;
     float ldisp2;
+    const int* lhalo;           // per list slot: first halo record << 6 | halo_flags
+    int* lhcount;               // halo records handed out (reset here for the next build)
 };
 cudaError_t launch_vgb_system(const VgbSystemArgs& a, const VgbParams& p, const DevGeom& g,
                               const NoiseView& nz, cudaStream_t st);
@@ -197,7 +200,7 @@ struct CanonArgs {
     StepState* state;       // may be null: advanced once per rebuild
     int advance;            // 1: this rebuild ends a step (advance state)
     int vel_freq;           // brownianIntegrator::velFreq
-    const uint32_t* err;    // non-zero: a previous kernel failed, skip the work
+    uint32_t* err;          // non-zero: a previous kernel failed, skip the work
     // pair-list bookkeeping (null: none).  lslot is carried with the particles;
     // when *rebuild != 0 the list is rebuilt on the new order, so lslot becomes
     // the identity and posh/posl/lbuild are written -- otherwise posh/posl
@@ -207,6 +210,12 @@ struct CanonArgs {
     int* lslot_out;
     float4* lbuild;
     float4* lpos;           // PairList::pos, written with posh/posl
+    // halo records of the particles within hr of a face (rebuild only):
+    // lhalo per slot, records n + 1 + [0, hcap) handed out by *lhcount
+    int* lhalo;
+    int* lhcount;
+    int hcap;
+    float hr, Lf, Lhi, Llo;
 };
 cudaError_t launch_canonicalize(const CanonArgs& a, cudaStream_t st);
 

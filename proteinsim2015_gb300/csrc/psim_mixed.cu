@@ -37,13 +37,6 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
     s = t;
 }
 
-// Knuth's TwoSum: s + e == a + b exactly.
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
-    s = a + b;
-    const float bb = s - a;
-    e = (a - (s - bb)) + (b - bb);
-}
-
 // One pair (i <- j) in FP32; each row's plain FP32 partial is added to the
 // particle's total with Kahan compensation.
 template <class Pair>
@@ -127,13 +120,7 @@ struct MixedBody {
     // float pair: (h + l) + s (Lhi + Llo)
     __device__ __forceinline__ void image(float4& h, float4& l, int sx, int sy, int sz,
                                           const DevGeom& g) const {
-        float ex, ey, ez;
-        two_sum(h.x, (float)sx * g.Lhi, h.x, ex);
-        two_sum(h.y, (float)sy * g.Lhi, h.y, ey);
-        two_sum(h.z, (float)sz * g.Lhi, h.z, ez);
-        l.x = (l.x + ex) + (float)sx * g.Llo;
-        l.y = (l.y + ey) + (float)sy * g.Llo;
-        l.z = (l.z + ez) + (float)sz * g.Llo;
+        image_shift(h, l, sx, sy, sz, g.Lhi, g.Llo);
     }
     // per-lane partial sums for the cross-lane reduction: 6 floats per lane
     __device__ __forceinline__ void partial(const Acc& a, double* red, int tid,
@@ -217,7 +204,7 @@ cudaError_t launch_forces_list(const ForceSetup& fs, const DevGeom& g, const Pai
 
 cudaError_t launch_list_build(const DevGeom& g, const CellView& cv, const ListBuild& lb,
                               uint32_t* err, cudaStream_t st) {
-    const ListBody body{lb.list, lb.count, lb.stride, lb.cap, g.n};
+    const ListBody body{lb.list, lb.count, lb.stride, lb.cap, g.n, lb.lhalo};
     const ForceOut out{nullptr, nullptr, nullptr, err, lb.gate};
     return launch_force_pass(body, g, cv, out, lb.pre_r2, st);
 }

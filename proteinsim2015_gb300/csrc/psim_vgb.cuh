@@ -190,8 +190,13 @@ __device__ __forceinline__ void list_position(const VgbSystemArgs& a, int f, con
         const float e = h[k] - bb[k];
         d2 += e * e;
     }
-    a.lpos[2 * (size_t)s] = make_float4(h[0], h[1], h[2], b.w);
-    a.lpos[2 * (size_t)s + 1] = make_float4(l[0], l[1], l[2], 0.f);
+    const float4 hv = make_float4(h[0], h[1], h[2], b.w), lv = make_float4(l[0], l[1], l[2], 0.f);
+    a.lpos[2 * (size_t)s] = hv;
+    a.lpos[2 * (size_t)s + 1] = lv;
+    const int hal = a.lhalo[s];
+    if (hal & 63)  // the particle's periodic images in the halo records
+        halo_write(a.lpos + 2 * ((size_t)a.n + 1), hal >> 6, (uint32_t)(hal & 63), hv, lv, g.Lhi,
+                   g.Llo);
     if (d2 > a.ldisp2) *a.lflag_set = 1;
 }
 
@@ -232,7 +237,10 @@ vgb_system_kernel(VgbSystemArgs a, VgbParams p, DevGeom g, NoiseView nz) {
         a.vel[3 * (size_t)tag + 2] = v[2];
     }
     if (a.lslot) list_position(a, f, xn, g);
-    if (f == 0 && a.lflag_clear) *a.lflag_clear = 0;
+    if (f == 0 && a.lflag_clear) {
+        *a.lflag_clear = 0;
+        *a.lhcount = 0;   // halo records are handed out afresh at the next build
+    }
     const int key = hash_pos(xn, g, err);
     a.key[f] = key;
     a.rank[f] = atomicAdd(&a.count[key], 1);
