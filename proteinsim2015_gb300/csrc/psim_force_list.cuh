@@ -106,6 +106,15 @@ struct ListBody {
     }
 };
 
+// One 32-byte record (high and low float4 halves) in a single 256-bit load
+// through the read-only path; the records are 32-byte aligned.
+__device__ __forceinline__ void load_record(const float4* pos, uint32_t j, float4& h, float4& l) {
+    const float4* a = pos + 2 * (size_t)j;
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(h.x), "=f"(h.y), "=f"(h.z), "=f"(h.w), "=f"(l.x), "=f"(l.y), "=f"(l.z), "=f"(l.w)
+        : "l"(a));
+}
+
 // A thread per particle (current storage order f): its list slot, its list,
 // its neighbours' records; the force is stored at f.  Lists are padded to
 // whole batches, so each batch's loads are issued together before any of its
@@ -141,10 +150,7 @@ force_list_kernel(Body body, DevGeom g, PairList pl, ForceOut out) {
 #pragma unroll
             for (int u = 0; u < kBatch; ++u) e[u] = __ldg(lp + (size_t)(k0 + b + u) * pl.stride);
 #pragma unroll
-            for (int u = 0; u < kBatch; ++u) {
-                nh[u] = pl.pos[2 * (size_t)e[u]];       // one 32-byte sector per neighbour
-                nl[u] = pl.pos[2 * (size_t)e[u] + 1];
-            }
+            for (int u = 0; u < kBatch; ++u) load_record(pl.pos, e[u], nh[u], nl[u]);
 #pragma unroll
             for (int u = 0; u < kBatch; ++u) body.eval_masked(nh[u], nl[u], hs, acc, err);
         }
