@@ -173,9 +173,10 @@ int make_geom(const psim_geometry* gm, double rc_max, DevGeom* g) {
     g->Lhi = (float)g->L;
     g->Llo = (float)(g->L - (double)g->Lhi);
     g->inv_csf = (float)g->inv_cs;
-    // FP32 hash error: x rounded (ulp(L)/2) scaled by 1/cs, plus the roundings
-    // of 1/cs and of the product (each ~s 2^-24 cells); 4x that is the guard
-    const double ex = std::ldexp(1.0, std::ilogb(std::max(g->L, 1.0)) - 24) * g->inv_cs +
+    // FP32 hash error: x cut or rounded to FP32 (< ulp(L)) scaled by 1/cs, plus
+    // the roundings of 1/cs and of the product (each ~s 2^-24 cells); 4x that
+    // is the guard
+    const double ex = std::ldexp(1.0, std::ilogb(std::max(g->L, 1.0)) - 23) * g->inv_cs +
                       2.0 * g->s * std::ldexp(1.0, -24);
     const double guard = 4.0 * ex + 1e-6;
     g->hash_guard = guard < 0.25 ? (float)guard : 0.5f;  // 0.5: always the FP64 path
@@ -327,6 +328,13 @@ int make_vgb_params(const psim_integrator_config* ic, VgbParams* p) {
     p->goy2 = c.goy2;
     p->goy3 = c.goy3;
     p->hn = c.hn;
+    p->dt2c1 = p->dt2 * c.coeff1;
+    p->dt2c2 = p->dt2 * c.coeff2;
+    p->sig1f = (float)c.sig1;
+    p->sig2f = (float)c.sig2;
+    p->corrf = (float)c.corr;
+    p->devf = (float)c.dev;
+    p->coeff0f = (float)c.coeff0;
     p->vel_freq = ic->vel_freq;
     p->seed = (uint32_t)ic->seed;
     return PSIM_OK;

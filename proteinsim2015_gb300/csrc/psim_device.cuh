@@ -71,6 +71,28 @@ __device__ __forceinline__ void split_f64(double x, float& hi, float& lo) {
     lo = sign ? -r : r;
 }
 
+// x cut to FP32 toward zero (the hi part of split_f64), by integer operations.
+__device__ __forceinline__ float f32_trunc(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const uint32_t top = (uint32_t)(b >> 32);
+    const int e = (int)((top >> 20) & 0x7FFu);
+    const uint32_t m23 = (uint32_t)(b >> 29) & 0x7FFFFFu;
+    return (e > 896 && e < 1151)
+               ? __uint_as_float((top & 0x80000000u) | ((uint32_t)(e - 896) << 23) | m23)
+               : 0.f;
+}
+
+// A float widened to double exactly, by integer operations (FP32 subnormals,
+// which the noise never produces, become zero).
+__device__ __forceinline__ double widen_f32(float f) {
+    const uint32_t b = __float_as_uint(f);
+    const uint32_t e = (b >> 23) & 0xFFu;
+    const unsigned long long sign = (unsigned long long)(b & 0x80000000u) << 32;
+    const unsigned long long ed = e == 0u ? 0ull : (e == 255u ? 2047ull : (unsigned long long)(e + 896u));
+    const unsigned long long m = e == 0u ? 0ull : (unsigned long long)(b & 0x7FFFFFu) << 29;
+    return __longlong_as_double((long long)(sign | (ed << 52) | m));
+}
+
 // Knuth's TwoSum: s + e == a + b exactly.
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
     s = a + b;
@@ -270,24 +292,31 @@ __device__ __forceinline__ Philox4 philox4x32_10(uint32_t c0, uint32_t c1, uint3
 // Two Gaussians from two 32-bit words by the Box-Muller transform in FP32
 // (the reference itself stores every other deviate as a float,
 // fastRandom.h:16).
-__device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, double& z0, double& z1) {
+__device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, float& z0, float& z1) {
     float u1 = ((float)(a >> 8) + 1.0f) * (1.0f / 16777216.0f);  // (0, 1]
     float u2 = (float)(b >> 8) * (1.0f / 16777216.0f);            // [0, 1)
     float rad = sqrtf(-2.0f * logf(u1));
     float sn, cs;
     sincospif(2.0f * u2, &sn, &cs);
-    z0 = (double)(rad * cs);
-    z1 = (double)(rad * sn);
+    z0 = rad * cs;
+    z1 = rad * sn;
 }
 
 // Six Gaussians for (particle tag, step): the normal step's xi_x..z, mem_x..z.
-__device__ __forceinline__ void philox_gaussians6(uint32_t seed, uint32_t tag, uint32_t step,
-                                                  double g[6]) {
+__device__ __forceinline__ void philox_gaussians6f(uint32_t seed, uint32_t tag, uint32_t step,
+                                                   float g[6]) {
     Philox4 a = philox4x32_10(step, 0u, tag, 0u, seed, 0x5053494Du);
     Philox4 b = philox4x32_10(step, 1u, tag, 0u, seed, 0x5053494Du);
     box_muller(a.v[0], a.v[1], g[0], g[1]);
     box_muller(a.v[2], a.v[3], g[2], g[3]);
     box_muller(b.v[0], b.v[1], g[4], g[5]);
+}
+__device__ __forceinline__ void philox_gaussians6(uint32_t seed, uint32_t tag, uint32_t step,
+                                                  double g[6]) {
+    float f[6];
+    philox_gaussians6f(seed, tag, step, f);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) g[k] = widen_f32(f[k]);
 }
 
 }  // namespace psim

@@ -84,6 +84,10 @@ struct VgbParams {
     double dt, dt2, dt3, dt_inv, c0;
     double coeff0, coeff1, coeff2, coeff3;
     double sig1, sig2, corr, dev, goy2, goy3, hn;
+    // the mixed form's normal step: dt^2 coeff1, dt^2 coeff2, and the noise
+    // coefficients in FP32
+    double dt2c1, dt2c2;
+    float sig1f, sig2f, corrf, devf, coeff0f;
     int vel_freq;
     uint32_t seed;
 };

@@ -17,6 +17,8 @@
 // the reference decides.
 #pragma once
 
+#include <type_traits>
+
 #include "psim_kernels.cuh"
 
 namespace psim {
@@ -127,9 +129,61 @@ __device__ __forceinline__ void vgb_particle(const VgbParams& p, double L, doubl
     }
 }
 
+// normalStep of the mixed form (brownianIntegrator.cpp:225-296): the
+// position terms in FP64 (FMA-contracted), the noise terms -- random numbers
+// drawn in FP32 -- summed in FP32 and added to the position once.  The wrap
+// is normalStep's; the previous position's re-image test runs in FP32 with
+// a wide margin and falls back to FP64 near L/2.  xf: the 6 Gaussians.
+__device__ __forceinline__ void vgb_normal_fast(const VgbParams& p, double L, double half_L,
+                                                const double x[3], const double x0[3],
+                                                double mx[3], const double F[3],
+                                                const double F0[3], const float xf[6], double m,
+                                                double xn[3], double x0n[3], uint32_t& err) {
+    const double c1 = m * p.dt2c1;
+    const double c2 = m * p.dt2c2;
+    double nw[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float mcf = p.sig2f * (p.corrf * f32_trunc(mx[k]) + p.devf * xf[k]);
+        const float noise = p.sig1f * xf[3 + k] + p.coeff0f * mcf;
+        double t = p.c0 * x[k];
+        t -= p.coeff0 * x0[k];
+        t += c1 * F[k];
+        t += c2 * (F[k] - F0[k]);
+        nw[k] = t + widen_f32(noise);
+        mx[k] = widen_f32(xf[3 + k]);
+    }
+    bool lo[3], hi[3];
+    bool any = false;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        lo[k] = neg_d(nw[k]);
+        hi[k] = !lo[k] && ge_pos_d(nw[k], L);
+        any |= lo[k] | hi[k];
+        xn[k] = nw[k];
+    }
+    if (__any_sync(__activemask(), any)) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            if (lo[k]) xn[k] = nw[k] + L;
+            else if (hi[k]) xn[k] = nw[k] - L;
+        }
+    }
+    const float Lf = (float)L;   // a uniform value: converted once per thread
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float df = fabsf(f32_trunc(xn[k]) - f32_trunc(x[k]));
+        bool far = df > 0.6f * Lf;
+        if (df >= 0.4f * Lf && df <= 0.6f * Lf) far = abs_gt_d(xn[k] - x[k], half_L);
+        x0n[k] = far ? ((xn[k] - x[k] < 0) ? x[k] - L : x[k] + L) : x[k];
+        const bool inside = !neg_d(xn[k]) && !ge_pos_d(xn[k], L) && (xn[k] == xn[k]);
+        if (!inside) err |= EBIT_BOUNDS;
+    }
+}
+
 // floor(x / cs) as the reference computes it (systemHandling.cpp:39-41).
 __device__ __forceinline__ int cell_coord_fast(double x, const DevGeom& g) {
-    const float q = __double2float_rn(x) * g.inv_csf;
+    const float q = f32_trunc(x) * g.inv_csf;
     const float f = floorf(q);
     const float fr = q - f;
     if (fr > g.hash_guard && fr < 1.0f - g.hash_guard) return (int)f;
@@ -165,6 +219,25 @@ __device__ __forceinline__ void load_noise(const NoiseView& nz, uint32_t seed, i
         for (int k = 0; k < 6; ++k) xi[k] = b[k];
     } else {
         philox_gaussians6(seed, (uint32_t)tag, (uint32_t)step, xi);
+    }
+}
+
+// The same draws as FP32 values (injected noise is cut to FP32).
+__device__ __forceinline__ void load_noise_f(const NoiseView& nz, uint32_t seed, int n, int tag,
+                                             long long step, float xf[6], uint32_t& err) {
+    if (nz.mode == 1) {
+        const long long idx = step - nz.first;
+        if (idx < 0 || idx >= nz.n_steps) {
+            err |= EBIT_NOISE;
+#pragma unroll
+            for (int k = 0; k < 6; ++k) xf[k] = 0.f;
+            return;
+        }
+        const double* b = nz.buf + ((size_t)idx * (size_t)n + (size_t)tag) * 6;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) xf[k] = f32_trunc(b[k]);
+    } else {
+        philox_gaussians6f(seed, (uint32_t)tag, (uint32_t)step, xf);
     }
 }
 
@@ -224,10 +297,16 @@ vgb_system_kernel(VgbSystemArgs a, VgbParams p, DevGeom g, NoiseView nz) {
         v[1] = a.vel[3 * (size_t)tag + 1];
         v[2] = a.vel[3 * (size_t)tag + 2];
     }
-    double xi[6];
-    load_noise(nz, p.seed, a.n, tag, step, xi, err);
-    double mc[3], xn[3], x0n[3];
-    vgb_particle(p, g.L, g.half, first, vel_step, x, x0, mx, mc, F, F0, v, xi, m, xn, x0n, err);
+    double xn[3], x0n[3];
+    if (std::is_same<Tag, VgbFast>::value && !first && !vel_step) {
+        float xf[6];
+        load_noise_f(nz, p.seed, a.n, tag, step, xf, err);
+        vgb_normal_fast(p, g.L, g.half, x, x0, mx, F, F0, xf, m, xn, x0n, err);
+    } else {
+        double xi[6], mc[3];
+        load_noise(nz, p.seed, a.n, tag, step, xi, err);
+        vgb_particle(p, g.L, g.half, first, vel_step, x, x0, mx, mc, F, F0, v, xi, m, xn, x0n, err);
+    }
     a.ox[f] = xn[0]; a.oy[f] = xn[1]; a.oz[f] = xn[2];
     a.ox0[f] = x0n[0]; a.oy0[f] = x0n[1]; a.oz0[f] = x0n[2];
     a.omx[f] = mx[0]; a.omy[f] = mx[1]; a.omz[f] = mx[2];
