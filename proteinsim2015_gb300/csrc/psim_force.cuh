@@ -84,7 +84,8 @@ force_pass_kernel(Body body, DevGeom g, CellView cv, ForceOut out, float pre_rc2
     const int jlast = g.n - 1;
 
     for (int row = 0; row < 9; ++row) {
-        const int dy = row / 3 - 1, dz = row % 3 - 1;
+        // z-major rows: runs come in increasing sorted-slot order
+        const int dz = row / 3 - 1, dy = row % 3 - 1;
         int sy, sz;
         const int y = wrap_cell(cy + dy, g.s, sy);
         const int z = wrap_cell(cz + dz, g.s, sz);

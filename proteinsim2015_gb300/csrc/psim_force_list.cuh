@@ -123,7 +123,7 @@ __device__ __forceinline__ void load_record(const float4* pos, uint32_t j, float
 template <class Body>
 __global__ void __launch_bounds__(128)
 force_list_kernel(Body body, DevGeom g, PairList pl, ForceOut out) {
-    constexpr int kBatch = 4;
+    constexpr int kBatch = 8;
     static_assert(kListFold % kBatch == 0, "batches tile a fold");
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= g.n || *out.err) return;
