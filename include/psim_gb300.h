@@ -273,6 +273,11 @@ int psim_system_snapshot_wait(psim_system* sys);
 /* Step counter (0 = next step is firstStep) and velocity counter. */
 int psim_system_get_step(psim_system* sys, int64_t* step, int32_t* vel_counter);
 
+/* The plugin force on every particle at the current state (reference
+ * particle_force layout: 3n doubles, original order), from the same force
+ * pass the next step will run (the pair list with a skin).  It does not step. */
+int psim_system_forces(psim_system* sys, double* force);
+
 /* Pair-list rebuilds since the upload (0 without a skin; the list the upload
  * builds is not counted). */
 int psim_system_list_builds(psim_system* sys, int32_t* builds);

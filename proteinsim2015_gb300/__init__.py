@@ -129,6 +129,7 @@ def lib():
             "psim_system_get_step": ([P, C.POINTER(C.c_int64), C.POINTER(C.c_int32)], C.c_int),
             "psim_system_stream": ([P], P),
             "psim_system_list_builds": ([P, C.POINTER(C.c_int32)], C.c_int),
+            "psim_system_forces": ([P, P], C.c_int),
             "psim_system_profile": ([P, C.c_int32, P], C.c_int),
             "psim_system_launches_per_step": ([P], C.c_int),
             "psim_system_cell_occupancy": ([P, C.POINTER(C.c_int32), C.POINTER(C.c_double)], C.c_int),
@@ -411,6 +412,13 @@ class System:
         s, v = C.c_int64(), C.c_int32()
         _check(lib().psim_system_get_step(self._h, C.byref(s), C.byref(v)))
         return s.value, v.value
+
+    def forces(self):
+        """The force on every particle at the current state (3n, original
+        order), from the force pass the next step runs."""
+        out = np.empty(3 * self.n)
+        _check(lib().psim_system_forces(self._h, _p(out)))
+        return out
 
     def list_builds(self):
         b = C.c_int32()

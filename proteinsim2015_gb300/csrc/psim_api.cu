@@ -835,6 +835,20 @@ cudaError_t enqueue_list_build(psim_system* s, int cb, const int* gate) {
     return launch_list_build(s->g, cv, lb, s->err.as<uint32_t>(), s->st);
 }
 
+// The force pass on the state after `total` steps (phase ph): the cell walk,
+// or the pair list in the mixed form with a skin; forces in storage order.
+cudaError_t enqueue_force(psim_system* s, const Phase& ph, const ForceOut& fo) {
+    CellView cv{s->posd.as<double4_32a>(), s->posh.as<float4>(), s->posl.as<float4>(),
+                s->cellid.as<int>(), s->start.as<int>(), s->count[ph.cb].as<int>()};
+    if (s->cfg.precision == PSIM_PRECISION_FP64) return launch_forces_fp64(s->fs, s->g, cv, fo, s->st);
+    if (s->list_on) {
+        PairList pl{s->lslot[ph.ob].as<int>(), s->lpos.as<float4>(), s->lcount.as<int>(),
+                    s->list.as<uint32_t>(), s->n};
+        return launch_forces_list(s->fs, s->g, pl, fo, s->st);
+    }
+    return launch_forces_mixed(s->fs, s->g, cv, fo, s->st);
+}
+
 int enqueue_step(psim_system* s, long long t, cudaEvent_t* evs) {
     const Phase ph = phase_of(t);
     const int n = s->n;
@@ -844,20 +858,9 @@ int enqueue_step(psim_system* s, long long t, cudaEvent_t* evs) {
     // the rebuild flag of this step's parity (pair list only)
     int* lflag = s->list_on ? s->lflag.as<int>() + (t & 1) : nullptr;
     if (evs) PSIM_CUDA(cudaEventRecord(evs[0], st));
-    // forces on the current cell order, or through the pair list
-    CellView cv{s->posd.as<double4_32a>(), s->posh.as<float4>(), s->posl.as<float4>(),
-                s->cellid.as<int>(), s->start.as<int>(), s->count[cb].as<int>()};
     ForceOut fo{d3(s->frc[ph.fcur], n, 0), d3(s->frc[ph.fcur], n, 1), d3(s->frc[ph.fcur], n, 2),
                 s->err.as<uint32_t>(), nullptr};
-    if (s->cfg.precision == PSIM_PRECISION_FP64) {
-        PSIM_CUDA(launch_forces_fp64(s->fs, s->g, cv, fo, st));
-    } else if (s->list_on) {
-        PairList pl{s->lslot[ob].as<int>(), s->lpos.as<float4>(), s->lcount.as<int>(),
-                    s->list.as<uint32_t>(), n};
-        PSIM_CUDA(launch_forces_list(s->fs, s->g, pl, fo, st));
-    } else {
-        PSIM_CUDA(launch_forces_mixed(s->fs, s->g, cv, fo, st));
-    }
+    PSIM_CUDA(enqueue_force(s, ph, fo));
     if (evs) PSIM_CUDA(cudaEventRecord(evs[1], st));
     // integrator: pushParticleForce + nextSystem, hash + count into the next grid
     PSIM_CUDA(cudaMemsetAsync(s->count[ncb].p, 0, 4 * (size_t)s->ncell, st));
@@ -1383,6 +1386,26 @@ int psim_system_get_step(psim_system* s, int64_t* step, int32_t* vel_counter) {
     if (step) *step = ss.step;
     if (vel_counter) *vel_counter = ss.vel_counter;
     return PSIM_OK;
+}
+
+int psim_system_forces(psim_system* s, double* force) {
+    if (!s || !force) return fail(PSIM_ERR_INPUT, "NULL argument");
+    if (!s->uploaded) return fail(PSIM_ERR_INPUT, "no state uploaded");
+    DeviceGuard dg(s->device);
+    int rc = settle(s);
+    if (rc) return rc;
+    const Phase ph = phase_of(s->total);
+    const int n = s->n;
+    ScopedBuf f3, out;
+    PSIM_CUDA(f3.ensure(24 * (size_t)n));
+    PSIM_CUDA(out.ensure(24 * (size_t)n));
+    ForceOut fo{f3.as<double>(), f3.as<double>() + n, f3.as<double>() + 2 * (size_t)n,
+                s->err.as<uint32_t>(), nullptr};
+    PSIM_CUDA(enqueue_force(s, ph, fo));
+    PSIM_CUDA(launch_unsort_force(n, s->tag[ph.ob].as<int>(), fo.fx, fo.fy, fo.fz,
+                                  out.as<double>(), s->st));
+    PSIM_CUDA(cudaMemcpyAsync(force, out.p, 24 * (size_t)n, cudaMemcpyDeviceToHost, s->st));
+    return settle(s);
 }
 
 int psim_system_list_builds(psim_system* s, int32_t* builds) {

@@ -131,3 +131,19 @@ def test_pairlist_skin_is_checked(psim):
         psim.System(g, p, precision=psim.PRECISION_FP64, skin=0.3)
     assert e.value.code == psim.ERR_INPUT
     assert psim.auto_skin(g, p) == pytest.approx(0.4)
+
+
+@pytest.mark.parametrize("skin,precision", [(0.0, 0), (0.0, 1), (0.4, 1)])
+def test_system_forces_match_dropin_fp64(psim, skin, precision):
+    # the force at the current state, from the pass the next step runs,
+    # against the drop-in FP64 evaluation on the system's own cell list
+    g, p, pos, rad = lj_liquid(psim)
+    s = psim.System(g, p, gamma=1.0, dt=DT, kT=KT, precision=precision,
+                    noise_mode=psim.NOISE_PHILOX, skin=skin)
+    s.upload(pos, rad, vel=np.random.default_rng(46).standard_normal(3 * g.n_particles))
+    s.step(37)
+    f = s.forces()
+    hi, cse, srt = s.download_cells()
+    ref = psim.force_evaluate(p, g, srt, hi, cse, precision=psim.PRECISION_FP64)
+    s.close()
+    assert rel_norm(f, ref) < (1e-12 if precision == 0 else 1e-5)
