@@ -234,6 +234,8 @@ public:
         c.precision = precision;
         c.noise_mode = PSIM_NOISE_PHILOX;
         c.device = device;
+        // settings key "skin": the mixed form's Verlet pair-list skin (0: none)
+        c.skin = precision == PSIM_PRECISION_MIXED ? cfg->getParam<double>("skin", 0.0) : 0.0;
         sys_ = psim_system_create(&c);
         if (!sys_) check(PSIM_ERR_INPUT);
     }
