@@ -225,6 +225,30 @@ typedef struct {
     double skin;
 } psim_system_config;
 
+/* ---------------------------------------------- batches of replicas */
+
+/* One replica of a batch: its own box and cell grid, plugin parameters and
+ * Philox seed.  All replicas of a batch use the same plugin (and ljNum); the
+ * AO + Yukawa composite is not batched. */
+typedef struct {
+    psim_geometry geom;
+    psim_force_params force;
+    int32_t seed;
+} psim_replica;
+
+/* Independent systems stepped together: every step is one launch per phase
+ * over all replicas (the force pass runs a warp task per 32 particles of one
+ * replica, with that replica's grid and plugin parameters).  No reference
+ * counterpart (the reference runs one system per process); each replica is
+ * exactly the system psim_system_create would build from its settings, with
+ * integ.seed replaced by the replica's seed, and steps bit for bit like it.
+ * The returned handle takes every psim_system_* call; its arrays are the
+ * replicas' arrays concatenated in replica order (original order within
+ * each).  No pair-list skin. */
+psim_system* psim_batch_create(const psim_replica* reps, int32_t n_reps,
+                               const psim_integrator_config* integ, int32_t precision,
+                               int32_t noise_mode, int32_t device);
+
 /* Creates the system and its device buffers (the role of system::system,
  * system.cpp:69-103, without the random initialisation: states are uploaded). */
 psim_system* psim_system_create(const psim_system_config* cfg);

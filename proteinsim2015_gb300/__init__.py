@@ -91,6 +91,10 @@ class SystemConfig(C.Structure):
                 ("skin", C.c_double)]
 
 
+class Replica(C.Structure):
+    _fields_ = [("geom", Geometry), ("force", ForceParams), ("seed", C.c_int32)]
+
+
 _lib = None
 
 
@@ -116,6 +120,8 @@ def lib():
             "psim_integrator_destroy": ([P], None),
             "psim_integrator_next_system": ([P, C.c_double, C.c_double, C.c_int32] + [P] * 8, C.c_int),
             "psim_system_create": ([C.POINTER(SystemConfig)], P),
+            "psim_batch_create": ([C.POINTER(Replica), C.c_int32, C.POINTER(IntegratorConfig),
+                                   C.c_int32, C.c_int32, C.c_int32], P),
             "psim_system_destroy": ([P], None),
             "psim_system_upload": ([P] * 8, C.c_int),
             "psim_system_set_noise": ([P, P, C.c_int32, C.c_int32], C.c_int),
@@ -463,3 +469,31 @@ class System:
             self.close()
         except Exception:
             pass
+
+
+class Batch(System):
+    """Independent replicas stepped together, one launch per phase.  Each
+    replica is (geometry, force params, seed); arrays are the replicas'
+    arrays concatenated in replica order.  Every System method applies."""
+
+    def __init__(self, replicas, gamma=1.0, dt=0.001, kT=1.0, vel_freq=1000,
+                 precision=PRECISION_MIXED, noise_mode=NOISE_PHILOX, device=0):
+        arr = (Replica * len(replicas))()
+        for k, (g, f, seed) in enumerate(replicas):
+            arr[k] = Replica(geom=g, force=f, seed=int(seed))
+        self._reps = arr
+        self.integ = IntegratorConfig(gamma=gamma, dt=dt, kT=kT, vel_freq=vel_freq, seed=0)
+        self.sizes = [g.n_particles for g, _, _ in replicas]
+        self.offsets = np.concatenate([[0], np.cumsum(self.sizes)]).astype(int)
+        self.n = int(self.offsets[-1])
+        self.ncell = sum(g.cell_scale ** 3 for g, _, _ in replicas)
+        self.skin = 0.0
+        self._h = lib().psim_batch_create(arr, len(replicas), C.byref(self.integ), precision,
+                                          noise_mode, device)
+        if not self._h:
+            _raise_last(ERR_INPUT)
+
+    def split(self, a, width=3):
+        """A concatenated per-particle array cut into the replicas' arrays."""
+        return [a[width * self.offsets[k]:width * self.offsets[k + 1]]
+                for k in range(len(self.sizes))]

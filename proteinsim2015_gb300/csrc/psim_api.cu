@@ -5,6 +5,7 @@
 //   force -> memset(next counts) -> vGB (+hash, count) -> scan -> scatter ->
 //   canonicalise (+gather, step counter)
 // captured once per buffer phase into CUDA graphs.
+#include <climits>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -180,6 +181,9 @@ int make_geom(const psim_geometry* gm, double rc_max, DevGeom* g) {
                       2.0 * g->s * std::ldexp(1.0, -24);
     const double guard = 4.0 * ex + 1e-6;
     g->hash_guard = guard < 0.25 ? (float)guard : 0.5f;  // 0.5: always the FP64 path
+    g->c0 = 0;
+    g->p0 = 0;
+    g->p1 = g->n;
     return PSIM_OK;
 }
 
@@ -787,6 +791,12 @@ struct psim_system {
     int lcap = 0, hcap = 0;
     float lpre = 0.f, ldisp2 = 0.f, hr = 0.f;
     DevBuf lslot[2], lbuild, lpos, list, lcount, lflag, lhalo, lhcount;
+    // a batch of independent replicas (psim_batch_create): per-warp tasks,
+    // per-replica grids, pair functors, prefilter bounds and seeds, and the
+    // replica of each storage slot (fixed: the cells of a replica are
+    // contiguous, so its particles keep their slot range in every cell order)
+    int n_reps = 0, n_tasks = 0;
+    DevBuf b_tasks, b_geoms, b_pairs, b_pre, b_rep, b_seeds;
 };
 
 namespace {
@@ -840,6 +850,13 @@ cudaError_t enqueue_list_build(psim_system* s, int cb, const int* gate) {
 cudaError_t enqueue_force(psim_system* s, const Phase& ph, const ForceOut& fo) {
     CellView cv{s->posd.as<double4_32a>(), s->posh.as<float4>(), s->posl.as<float4>(),
                 s->cellid.as<int>(), s->start.as<int>(), s->count[ph.cb].as<int>()};
+    if (s->n_reps) {
+        BatchView bv{s->b_tasks.as<int2>(), s->n_tasks, s->b_geoms.as<DevGeom>(),
+                     s->b_pairs.p, s->b_pre.as<float>()};
+        if (s->cfg.precision == PSIM_PRECISION_FP64)
+            return launch_forces_fp64(s->fs, s->g, cv, fo, s->st, &bv);
+        return launch_forces_mixed(s->fs, s->g, cv, fo, s->st, &bv);
+    }
     if (s->cfg.precision == PSIM_PRECISION_FP64) return launch_forces_fp64(s->fs, s->g, cv, fo, s->st);
     if (s->list_on) {
         PairList pl{s->lslot[ph.ob].as<int>(), s->lpos.as<float4>(), s->lcount.as<int>(),
@@ -893,6 +910,11 @@ int enqueue_step(psim_system* s, long long t, cudaEvent_t* evs) {
         a.ldisp2 = s->ldisp2;
         a.lhalo = s->lhalo.as<int>();
         a.lhcount = s->lhcount.as<int>();
+    }
+    if (s->n_reps) {
+        a.rep = s->b_rep.as<int>();
+        a.geoms = s->b_geoms.as<DevGeom>();
+        a.seeds = s->b_seeds.as<uint32_t>();
     }
     NoiseView nz{s->cfg.noise_mode, s->noise.as<double>(), s->noise_first, s->noise_steps};
     if (s->cfg.precision == PSIM_PRECISION_FP64)
@@ -983,6 +1005,10 @@ int settle(psim_system* s) {
 
 }  // namespace
 
+namespace {
+psim_system* system_new(const psim_system_config* cfg, const DevGeom& g);
+}
+
 extern "C" {
 
 psim_system* psim_system_create(const psim_system_config* cfg) {
@@ -998,6 +1024,118 @@ psim_system* psim_system_create(const psim_system_config* cfg) {
     }
     DevGeom g;
     if (make_geom(&cfg->geom, max_cutoff(&cfg->force), &g)) return nullptr;
+    return system_new(cfg, g);
+}
+
+psim_system* psim_batch_create(const psim_replica* reps, int32_t n_reps,
+                               const psim_integrator_config* integ, int32_t precision,
+                               int32_t noise_mode, int32_t device) {
+    if (!reps || n_reps <= 0 || !integ) {
+        fail(PSIM_ERR_INPUT, "a batch needs at least one replica and an integrator config");
+        return nullptr;
+    }
+    const int kind = reps[0].force.kind;
+    if (kind == PSIM_FORCE_AO_YUKAWA) {
+        fail(PSIM_ERR_INPUT, "a batch holds single-plugin replicas (not the AO + Yukawa composite)");
+        return nullptr;
+    }
+    std::vector<DevGeom> geoms((size_t)n_reps);
+    long long P = 0, C = 0;
+    for (int r = 0; r < n_reps; ++r) {
+        const psim_force_params* f = &reps[r].force;
+        if (check_params(f)) return nullptr;
+        if (f->kind != kind || (kind == PSIM_FORCE_LJ && f->lj_num != reps[0].force.lj_num)) {
+            fail(PSIM_ERR_INPUT, "replica %d: every replica of a batch uses the same plugin "
+                 "(and ljNum)", r);
+            return nullptr;
+        }
+        DevGeom& g = geoms[r];
+        if (make_geom(&reps[r].geom, max_cutoff(f), &g)) return nullptr;
+        g.c0 = (int)C;
+        g.p0 = (int)P;
+        g.p1 = (int)(P + g.n);
+        P += g.n;
+        C += g.ncell;
+        if (P > INT32_MAX / 2 || C > INT32_MAX / 2) {
+            fail(PSIM_ERR_INPUT, "the batch holds too many particles or cells");
+            return nullptr;
+        }
+    }
+    // the whole batch as one grid for the kernels that need no geometry
+    DevGeom gt = geoms[0];
+    gt.n = (int)P;
+    gt.ncell = (int)C;
+    gt.c0 = 0;
+    gt.p0 = 0;
+    gt.p1 = (int)P;
+    psim_system_config cfg{};
+    cfg.geom = reps[0].geom;
+    cfg.geom.n_particles = (int)P;
+    cfg.integ = *integ;
+    cfg.force = reps[0].force;
+    cfg.precision = precision;
+    cfg.noise_mode = noise_mode;
+    cfg.device = device;
+    cfg.skin = 0.0;
+    if (precision != PSIM_PRECISION_FP64 && precision != PSIM_PRECISION_MIXED) {
+        fail(PSIM_ERR_INPUT, "unknown precision %d", precision);
+        return nullptr;
+    }
+    if (noise_mode != PSIM_NOISE_PHILOX && noise_mode != PSIM_NOISE_INJECTED) {
+        fail(PSIM_ERR_INPUT, "unknown noise mode %d", noise_mode);
+        return nullptr;
+    }
+    psim_system* s = system_new(&cfg, gt);
+    if (!s) return nullptr;
+    DeviceGuard dg(s->device);
+    s->fs.tile = 0;
+    // warp tasks aligned to the replicas' particle ranges
+    std::vector<int2> tasks;
+    std::vector<int> rep((size_t)P);
+    std::vector<float> pre((size_t)n_reps);
+    std::vector<uint32_t> seeds((size_t)n_reps);
+    std::vector<unsigned char> pairs;
+    for (int r = 0; r < n_reps; ++r) {
+        const DevGeom& g = geoms[r];
+        for (int i0 = g.p0; i0 < g.p1; i0 += 32) tasks.push_back(make_int2(r, i0));
+        for (int i = g.p0; i < g.p1; ++i) rep[(size_t)i] = r;
+        const ForceSetup fr = make_setup(&reps[r].force, g.L);
+        pre[(size_t)r] = fr.pre_rc2f;
+        seeds[(size_t)r] = (uint32_t)reps[r].seed;
+        const void* src = kind == PSIM_FORCE_AO ? (const void*)&fr.ao
+                          : kind == PSIM_FORCE_LJ ? (const void*)&fr.lj : (const void*)&fr.cal;
+        const size_t sz = kind == PSIM_FORCE_AO ? sizeof(AOPair)
+                          : kind == PSIM_FORCE_LJ ? sizeof(LJPair) : sizeof(CalPair);
+        const unsigned char* b = static_cast<const unsigned char*>(src);
+        pairs.insert(pairs.end(), b, b + sz);
+    }
+    s->n_reps = n_reps;
+    s->n_tasks = (int)tasks.size();
+    auto put = [&](DevBuf& d, const void* h, size_t bytes) {
+        return !d.ensure(bytes ? bytes : 16) &&
+               (bytes == 0 || cudaMemcpy(d.p, h, bytes, cudaMemcpyHostToDevice) == cudaSuccess);
+    };
+    const bool ok = put(s->b_tasks, tasks.data(), tasks.size() * sizeof(int2)) &&
+                    put(s->b_geoms, geoms.data(), geoms.size() * sizeof(DevGeom)) &&
+                    put(s->b_pairs, pairs.data(), pairs.size()) &&
+                    put(s->b_pre, pre.data(), pre.size() * sizeof(float)) &&
+                    put(s->b_rep, rep.data(), rep.size() * sizeof(int)) &&
+                    put(s->b_seeds, seeds.data(), seeds.size() * sizeof(uint32_t));
+    if (!ok) {
+        fail(PSIM_ERR_CUDA, "batch tables: %s", cudaGetErrorString(cudaGetLastError()));
+        psim_system_destroy(s);
+        return nullptr;
+    }
+    return s;
+}
+
+}  // extern "C"
+
+namespace {
+
+// The system's streams, events and buffers for grid g (the whole batch's
+// particles and cells for a batch); validates the rest of cfg.
+psim_system* system_new(const psim_system_config* cfg, const DevGeom& g) {
     VgbParams vp;
     if (make_vgb_params(&cfg->integ, &vp)) return nullptr;
     const double rc = max_cutoff(&cfg->force);
@@ -1099,6 +1237,10 @@ psim_system* psim_system_create(const psim_system_config* cfg) {
     return s;
 }
 
+}  // namespace
+
+extern "C" {
+
 void psim_system_destroy(psim_system* s) {
     if (!s) return;
     DeviceGuard dg(s->device);
@@ -1108,7 +1250,8 @@ void psim_system_destroy(psim_system* s) {
     DevBuf* arrs[] = {&s->cellid, &s->key, &s->rank, &s->tmp, &s->start, &s->scratch, &s->posd,
                       &s->posh, &s->posl, &s->vel, &s->err, &s->state, &s->occ, &s->noise,
                       &s->snap, &s->lslot[0], &s->lslot[1], &s->lbuild, &s->lpos, &s->list,
-                      &s->lcount, &s->lflag, &s->lhalo, &s->lhcount};
+                      &s->lcount, &s->lflag, &s->lhalo, &s->lhcount, &s->b_tasks,
+                      &s->b_geoms, &s->b_pairs, &s->b_pre, &s->b_rep, &s->b_seeds};
     for (DevBuf* b : arrs) b->release();
     for (int k = 0; k < 2; ++k) {
         s->pos[k].release(); s->pos0[k].release(); s->mem[k].release(); s->tag[k].release();
@@ -1172,7 +1315,9 @@ int psim_system_upload(psim_system* s, const double* pos, const double* pos0, co
     PSIM_CUDA(cudaMemsetAsync(s->count[ph.cb].p, 0, 4 * (size_t)s->ncell, st));
     PSIM_CUDA(launch_hash_count(n, d3(s->pos[sb], n, 0), d3(s->pos[sb], n, 1),
                                 d3(s->pos[sb], n, 2), s->g, s->key.as<int>(), s->rank.as<int>(),
-                                s->count[ph.cb].as<int>(), s->err.as<uint32_t>(), st));
+                                s->count[ph.cb].as<int>(), s->err.as<uint32_t>(), st,
+                                s->n_reps ? s->b_rep.as<int>() : nullptr,
+                                s->n_reps ? s->b_geoms.as<DevGeom>() : nullptr));
     PSIM_CUDA(launch_scan(s->count[ph.cb].as<int>(), s->start.as<int>(), s->ncell,
                           s->scratch.as<int>(), st));
     PSIM_CUDA(launch_scatter(n, s->key.as<int>(), s->rank.as<int>(), s->start.as<int>(),

@@ -38,6 +38,9 @@ struct DevGeom {
     float Lhi, Llo; // L as a float pair (Lhi + Llo == L to ~1e-14)
     float inv_csf;  // 1 / cellSize in FP32 (the FP32 cell hash)
     float hash_guard; // distance from a cell face (in cells) below which FP64 decides
+    // a system's place in a batch of independent replicas (one system: 0, 0, n):
+    // its first global cell and its particle range in every storage order
+    int c0, p0, p1;
 };
 
 // floor(x / cs) exactly as the reference computes it (systemHandling.cpp:39-41):

@@ -50,6 +50,14 @@ struct F64Body {
         double n0, n1, n2, c0, c1, c2;
     };
     __device__ __forceinline__ const Aux* aux(const CellView& cv) const { return cv.posd; }
+    // the body of replica r of a batch: its own pair functor and box
+    __device__ __forceinline__ F64Body for_replica(const void* pairs, int r,
+                                                   const DevGeom& g) const {
+        F64Body b = *this;
+        b.pf = static_cast<const Pair*>(pairs)[r];
+        b.geom = g;
+        return b;
+    }
     __device__ __forceinline__ void init(Acc& a) const {
         a.n0 = a.n1 = a.n2 = a.c0 = a.c1 = a.c2 = 0.0;
     }
@@ -126,36 +134,40 @@ struct F64Body {
 
 template <class Pair>
 static cudaError_t run_fp64(const Pair& p, const DevGeom& g, const CellView& cv,
-                            const ForceOut& out, float pre, cudaStream_t st, int tile) {
-    if (tile) return launch_force_cells(F64Body<Pair>{p, g}, g, cv, out, pre, st);
-    return launch_force_pass(F64Body<Pair>{p, g}, g, cv, out, pre, st);
+                            const ForceOut& out, float pre, cudaStream_t st, int tile,
+                            const BatchView* bv) {
+    if (tile && !bv) return launch_force_cells(F64Body<Pair>{p, g}, g, cv, out, pre, st);
+    return launch_force_pass(F64Body<Pair>{p, g}, g, cv, out, pre, st, bv);
 }
 
 template <int N>
 static cudaError_t run_lj_fp64(const LJPair& lj, const DevGeom& g, const CellView& cv,
-                               const ForceOut& out, float pre, cudaStream_t st, int tile) {
+                               const ForceOut& out, float pre, cudaStream_t st, int tile,
+                               const BatchView* bv) {
     LJFixed<N> p;
     static_cast<LJPair&>(p) = lj;
-    return run_fp64(p, g, cv, out, pre, st, tile);
+    return run_fp64(p, g, cv, out, pre, st, tile, bv);
 }
 
 cudaError_t launch_forces_fp64(const ForceSetup& fs, const DevGeom& g, const CellView& cv,
-                               const ForceOut& out, cudaStream_t st) {
+                               const ForceOut& out, cudaStream_t st, const BatchView* bv) {
     const int t = fs.tile;
+    const float pre = fs.pre_rc2f;
     switch (fs.kind) {
-    case 1: return run_fp64(fs.ao, g, cv, out, fs.pre_rc2f, st, t);
+    case 1: return run_fp64(fs.ao, g, cv, out, pre, st, t, bv);
     case 2:
         switch (fs.lj.n) {
-        case 0: return run_lj_fp64<0>(fs.lj, g, cv, out, fs.pre_rc2f, st, t);
-        case 6: return run_lj_fp64<6>(fs.lj, g, cv, out, fs.pre_rc2f, st, t);
-        case 12: return run_lj_fp64<12>(fs.lj, g, cv, out, fs.pre_rc2f, st, t);
-        case 18: return run_lj_fp64<18>(fs.lj, g, cv, out, fs.pre_rc2f, st, t);
-        default: return run_fp64(fs.lj, g, cv, out, fs.pre_rc2f, st, t);
+        case 0: return run_lj_fp64<0>(fs.lj, g, cv, out, pre, st, t, bv);
+        case 6: return run_lj_fp64<6>(fs.lj, g, cv, out, pre, st, t, bv);
+        case 12: return run_lj_fp64<12>(fs.lj, g, cv, out, pre, st, t, bv);
+        case 18: return run_lj_fp64<18>(fs.lj, g, cv, out, pre, st, t, bv);
+        default: return run_fp64(fs.lj, g, cv, out, pre, st, t, bv);
         }
-    case 3: return run_fp64(fs.cal, g, cv, out, fs.pre_rc2f, st, t);
+    case 3: return run_fp64(fs.cal, g, cv, out, pre, st, t, bv);
     case 4: {
+        if (bv) return cudaErrorInvalidValue;  // batches hold single-plugin replicas
         ComboPair cp{fs.ao, fs.lj, fs.ao.rc2 > fs.lj.rc2 ? fs.ao.rc2 : fs.lj.rc2};
-        return run_fp64(cp, g, cv, out, fs.pre_rc2f, st, t);
+        return run_fp64(cp, g, cv, out, pre, st, t, bv);
     }
     }
     return cudaErrorInvalidValue;
@@ -182,13 +194,14 @@ cudaError_t launch_vgb_aos(const VgbAosArgs& a, const VgbParams& p, double L, cu
 // ------------------------------------------------------------------ hashing
 
 __global__ void __launch_bounds__(256)
-hash_count_kernel(int n, const double* x, const double* y, const double* z, DevGeom g,
-                  int* key, int* rank, int* count, uint32_t* err_out) {
+hash_count_kernel(int n, const double* x, const double* y, const double* z, DevGeom g0,
+                  int* key, int* rank, int* count, uint32_t* err_out, const int* rep,
+                  const DevGeom* geoms) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     uint32_t err = 0;
     const double p[3] = {x[i], y[i], z[i]};
-    const int k = hash_pos(p, g, err);
+    const int k = hash_pos(p, rep ? geoms[rep[i]] : g0, err);
     key[i] = k;
     rank[i] = atomicAdd(&count[k], 1);
     if (err) atomicOr(err_out, err);
@@ -196,9 +209,10 @@ hash_count_kernel(int n, const double* x, const double* y, const double* z, DevG
 
 cudaError_t launch_hash_count(int n, const double* x, const double* y, const double* z,
                               const DevGeom& g, int* key, int* rank, int* count, uint32_t* err,
-                              cudaStream_t st) {
+                              cudaStream_t st, const int* rep, const DevGeom* geoms) {
     if (n == 0) return cudaSuccess;
-    hash_count_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, x, y, z, g, key, rank, count, err);
+    hash_count_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, x, y, z, g, key, rank, count, err, rep,
+                                                       geoms);
     return cudaGetLastError();
 }
 

@@ -48,19 +48,34 @@ constexpr int kStagePad = 2 * kStage + kUnroll;
 
 template <class Body>
 __global__ void __launch_bounds__(kForceWarps * 32)
-force_pass_kernel(Body body, DevGeom g, CellView cv, ForceOut out, float pre_rc2) {
+force_pass_kernel(Body body0, DevGeom g0, CellView cv, ForceOut out, float pre0, BatchView bv) {
     using Aux = typename Body::Aux;
     __shared__ float4 s_hi[kForceWarps][kStagePad];
     __shared__ Aux s_aux[kForceWarps][kStage];
     __shared__ uint32_t s_q[kForceWarps][kQueueCap][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     // an error latched by an earlier kernel (or a closed gate) stops the
     // pass; read once and broadcast so every lane takes the same path
     const bool failed = __shfl_sync(
         0xffffffffu, (lane == 0) ? (*out.err != 0 || (out.gate && *out.gate == 0)) : false, 0);
     if (failed) return;  // warp-uniform; the kernel synchronises warps only
-    const bool active = i < g.n;
+    // one system, or the warp's task in a batch of replicas (warp-uniform)
+    int i;
+    DevGeom g = g0;
+    Body body = body0;
+    float pre_rc2 = pre0;
+    if (bv.tasks) {
+        const int task = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+        if (task >= bv.n_tasks) return;
+        const int2 t = bv.tasks[task];
+        g = bv.geoms[t.x];
+        body = body0.for_replica(bv.pairs, t.x, g);
+        pre_rc2 = bv.pre[t.x];
+        i = t.y + lane;
+    } else {
+        i = blockIdx.x * blockDim.x + threadIdx.x;
+    }
+    const bool active = i < g.p1;
     float4* st_hi = s_hi[w];
     Aux* st_aux = s_aux[w];
     uint32_t (*q)[32] = s_q[w];
@@ -73,7 +88,7 @@ force_pass_kernel(Body body, DevGeom g, CellView cv, ForceOut out, float pre_rc2
     body.init(acc);
     if (active) {
         hi = cv.posh[i];
-        const int c = cv.cellid[i];
+        const int c = cv.cellid[i] - g.c0;
         cx = c % g.s;
         cy = (c / g.s) % g.s;
         cz = c / g.s2;
@@ -81,7 +96,7 @@ force_pass_kernel(Body body, DevGeom g, CellView cv, ForceOut out, float pre_rc2
     }
     uint32_t err = 0;
     int cnt = 0;
-    const int jlast = g.n - 1;
+    const int jlast = g.p1 - 1;
 
     for (int row = 0; row < 9; ++row) {
         // z-major rows: runs come in increasing sorted-slot order
@@ -89,7 +104,7 @@ force_pass_kernel(Body body, DevGeom g, CellView cv, ForceOut out, float pre_rc2
         int sy, sz;
         const int y = wrap_cell(cy + dy, g.s, sy);
         const int z = wrap_cell(cz + dz, g.s, sz);
-        const int base = g.s * y + g.s2 * z;
+        const int base = g.c0 + g.s * y + g.s2 * z;
 #pragma unroll 1
         for (int part = 0; part < 2; ++part) {
             // part 0: the cells of [cx-1, cx+1] inside the grid, contiguous;
@@ -191,11 +206,18 @@ force_pass_kernel(Body body, DevGeom g, CellView cv, ForceOut out, float pre_rc2
 
 template <class Body>
 cudaError_t launch_force_pass(const Body& body, const DevGeom& g, const CellView& cv,
-                              const ForceOut& out, float pre_rc2, cudaStream_t st) {
-    if (g.n == 0) return cudaSuccess;
+                              const ForceOut& out, float pre_rc2, cudaStream_t st,
+                              const BatchView* bv = nullptr) {
     const int threads = kForceWarps * 32;
-    force_pass_kernel<Body><<<(g.n + threads - 1) / threads, threads, 0, st>>>(body, g, cv, out,
-                                                                              pre_rc2);
+    if (bv && bv->tasks) {
+        if (bv->n_tasks == 0) return cudaSuccess;
+        const int blocks = (bv->n_tasks + kForceWarps - 1) / kForceWarps;
+        force_pass_kernel<Body><<<blocks, threads, 0, st>>>(body, g, cv, out, pre_rc2, *bv);
+        return cudaGetLastError();
+    }
+    if (g.n == 0) return cudaSuccess;
+    force_pass_kernel<Body><<<(g.n + threads - 1) / threads, threads, 0, st>>>(
+        body, g, cv, out, pre_rc2, BatchView{});
     return cudaGetLastError();
 }
 

@@ -43,10 +43,23 @@ struct ForceOut {
     const int* gate;   // may be null; else the pass runs only when *gate != 0
 };
 
+// Independent replicas in one launch: per warp a task (replica, first
+// particle) inside the replica's particle range, and per replica its
+// geometry, pair functor (the body's Pair type) and FP32 prefilter bound.
+struct BatchView {
+    const int2* tasks;   // null: one system
+    int n_tasks;
+    const DevGeom* geoms;
+    const void* pairs;
+    const float* pre;
+};
+
 cudaError_t launch_forces_fp64(const ForceSetup& fs, const DevGeom& g, const CellView& cv,
-                               const ForceOut& out, cudaStream_t st);
+                               const ForceOut& out, cudaStream_t st,
+                               const BatchView* bv = nullptr);
 cudaError_t launch_forces_mixed(const ForceSetup& fs, const DevGeom& g, const CellView& cv,
-                                const ForceOut& out, cudaStream_t st);
+                                const ForceOut& out, cudaStream_t st,
+                                const BatchView* bv = nullptr);
 
 // Verlet pair list of the mixed form (psim_force_list.cuh).  Entries are
 // record slots: a particle's list slot (< n), the ghost n that pads lists, or
@@ -142,6 +155,12 @@ struct VgbSystemArgs {
     float ldisp2;
     const int* lhalo;           // per list slot: first halo record << 6 | halo_flags
     int* lhcount;               // halo records handed out (reset here for the next build)
+    // a batch of replicas (rep null: one system): the replica of each storage
+    // slot, their geometries and Philox seeds (a replica's noise is keyed by
+    // its own seed and its particles' indices within it)
+    const int* rep;
+    const DevGeom* geoms;
+    const uint32_t* seeds;
 };
 cudaError_t launch_vgb_system(const VgbSystemArgs& a, const VgbParams& p, const DevGeom& g,
                               const NoiseView& nz, cudaStream_t st);
@@ -167,9 +186,11 @@ struct VgbAosArgs {
 cudaError_t launch_vgb_aos(const VgbAosArgs& a, const VgbParams& p, double L, cudaStream_t st);
 
 // Cell hash + atomic count of positions given as three coordinate arrays.
+// rep/geoms (may be null): a batch's replica of each particle and their grids.
 cudaError_t launch_hash_count(int n, const double* x, const double* y, const double* z,
                               const DevGeom& g, int* key, int* rank, int* count,
-                              uint32_t* err, cudaStream_t st);
+                              uint32_t* err, cudaStream_t st, const int* rep = nullptr,
+                              const DevGeom* geoms = nullptr);
 
 // ---------------------------------------------------------- cells (psim_cells.cu)
 // Exclusive scan of count[ncell] into start[ncell]; scratch needs

@@ -30,6 +30,13 @@ struct ComboPairF {
     }
 };
 
+// The FP32 cutoff of a pair functor (the larger one for the composite).
+template <class P>
+__device__ __forceinline__ float pair_rc2f(const P& p) { return p.rc2f; }
+__device__ __forceinline__ float pair_rc2f(const ComboPairF& p) {
+    return p.ao.rc2f > p.lj.rc2f ? p.ao.rc2f : p.lj.rc2f;
+}
+
 __device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
     const float y = v - c;
     const float t = s + y;
@@ -55,6 +62,14 @@ struct MixedBody {
         float s0, s1, s2, k0, k1, k2, p0, p1, p2;
     };
     __device__ __forceinline__ const Aux* aux(const CellView& cv) const { return cv.posl; }
+    // the body of replica r of a batch: its own pair functor and cutoff
+    __device__ __forceinline__ MixedBody for_replica(const void* pairs, int r,
+                                                     const DevGeom&) const {
+        MixedBody b = *this;
+        b.pf = static_cast<const Pair*>(pairs)[r];
+        b.rc2f = pair_rc2f(b.pf);
+        return b;
+    }
     __device__ __forceinline__ void init(Acc& a) const {
         a.s0 = a.s1 = a.s2 = a.k0 = a.k1 = a.k2 = a.p0 = a.p1 = a.p2 = 0.f;
     }
@@ -187,11 +202,12 @@ static cudaError_t with_pair(const ForceSetup& fs, Run&& run) {
 }
 
 cudaError_t launch_forces_mixed(const ForceSetup& fs, const DevGeom& g, const CellView& cv,
-                                const ForceOut& out, cudaStream_t st) {
+                                const ForceOut& out, cudaStream_t st, const BatchView* bv) {
+    if (bv && fs.kind == 4) return cudaErrorInvalidValue;  // batches hold single-plugin replicas
     return with_pair(fs, [&](auto p, float rc2f) {
         const MixedBody<decltype(p)> body{p, rc2f};
-        if (fs.tile) return launch_force_cells(body, g, cv, out, fs.pre_rc2f, st);
-        return launch_force_pass(body, g, cv, out, fs.pre_rc2f, st);
+        if (fs.tile && !bv) return launch_force_cells(body, g, cv, out, fs.pre_rc2f, st);
+        return launch_force_pass(body, g, cv, out, fs.pre_rc2f, st, bv);
     });
 }
 

@@ -129,6 +129,9 @@ extern "C" int psim_cells_build_noalloc(const psim_geometry* gm, const double* d
     g.inv_cs = 1.0 / gm->cell_size;
     g.inv_csf = (float)g.inv_cs;
     g.hash_guard = 0.5f;  // FP64 hash everywhere: this path is not performance critical
+    g.c0 = 0;
+    g.p0 = 0;
+    g.p1 = g.n;
 
     Carve c{static_cast<char*>(base)};
     double* x = static_cast<double*>(c.take(24 * n));

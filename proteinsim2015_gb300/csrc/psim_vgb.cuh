@@ -201,11 +201,13 @@ __device__ __forceinline__ int hash_pos(const double xn[3], const DevGeom& g, ui
         }
         c[k] = q;
     }
-    return c[0] + g.s * c[1] + g.s2 * c[2];  // systemHandling.cpp:43
+    return g.c0 + c[0] + g.s * c[1] + g.s2 * c[2];  // systemHandling.cpp:43 (+ the batch offset)
 }
 
+// tag: the particle's index in the injected buffer; ptag: its Philox key
 __device__ __forceinline__ void load_noise(const NoiseView& nz, uint32_t seed, int n, int tag,
-                                           long long step, double xi[6], uint32_t& err) {
+                                           int ptag, long long step, double xi[6],
+                                           uint32_t& err) {
     if (nz.mode == 1) {
         const long long idx = step - nz.first;
         if (idx < 0 || idx >= nz.n_steps) {
@@ -218,13 +220,14 @@ __device__ __forceinline__ void load_noise(const NoiseView& nz, uint32_t seed, i
 #pragma unroll
         for (int k = 0; k < 6; ++k) xi[k] = b[k];
     } else {
-        philox_gaussians6(seed, (uint32_t)tag, (uint32_t)step, xi);
+        philox_gaussians6(seed, (uint32_t)ptag, (uint32_t)step, xi);
     }
 }
 
 // The same draws as FP32 values (injected noise is cut to FP32).
 __device__ __forceinline__ void load_noise_f(const NoiseView& nz, uint32_t seed, int n, int tag,
-                                             long long step, float xf[6], uint32_t& err) {
+                                             int ptag, long long step, float xf[6],
+                                             uint32_t& err) {
     if (nz.mode == 1) {
         const long long idx = step - nz.first;
         if (idx < 0 || idx >= nz.n_steps) {
@@ -237,7 +240,7 @@ __device__ __forceinline__ void load_noise_f(const NoiseView& nz, uint32_t seed,
 #pragma unroll
         for (int k = 0; k < 6; ++k) xf[k] = f32_trunc(b[k]);
     } else {
-        philox_gaussians6f(seed, (uint32_t)tag, (uint32_t)step, xf);
+        philox_gaussians6f(seed, (uint32_t)ptag, (uint32_t)step, xf);
     }
 }
 
@@ -275,15 +278,23 @@ __device__ __forceinline__ void list_position(const VgbSystemArgs& a, int f, con
 
 template <class Tag>
 __global__ void __launch_bounds__(256)
-vgb_system_kernel(VgbSystemArgs a, VgbParams p, DevGeom g, NoiseView nz) {
+vgb_system_kernel(VgbSystemArgs a, VgbParams p, DevGeom g0, NoiseView nz) {
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= a.n || *a.err) return;
+    // one system, or this particle's replica in a batch
+    DevGeom g = g0;
+    if (a.rep) {
+        const int r = a.rep[f];
+        g = a.geoms[r];
+        p.seed = a.seeds[r];
+    }
     const long long step = a.state->step;
     const int vc = a.state->vel_counter;
     const bool first = (step == 0);
     const bool vel_step = !first && (p.vel_freq == 0 || vc == p.vel_freq);
     const int o = a.perm[f];
     const int tag = a.tag[f];
+    const int ntag = tag - g.p0;   // the index within the replica keys its Philox noise
     const double m = a.inv_mass[f];
     uint32_t err = 0;
     const double x[3] = {a.x[o], a.y[o], a.z[o]};
@@ -300,11 +311,11 @@ vgb_system_kernel(VgbSystemArgs a, VgbParams p, DevGeom g, NoiseView nz) {
     double xn[3], x0n[3];
     if (std::is_same<Tag, VgbFast>::value && !first && !vel_step) {
         float xf[6];
-        load_noise_f(nz, p.seed, a.n, tag, step, xf, err);
+        load_noise_f(nz, p.seed, a.n, tag, ntag, step, xf, err);
         vgb_normal_fast(p, g.L, g.half, x, x0, mx, F, F0, xf, m, xn, x0n, err);
     } else {
         double xi[6], mc[3];
-        load_noise(nz, p.seed, a.n, tag, step, xi, err);
+        load_noise(nz, p.seed, a.n, tag, ntag, step, xi, err);
         vgb_particle(p, g.L, g.half, first, vel_step, x, x0, mx, mc, F, F0, v, xi, m, xn, x0n, err);
     }
     a.ox[f] = xn[0]; a.oy[f] = xn[1]; a.oz[f] = xn[2];

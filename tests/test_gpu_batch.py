@@ -1,0 +1,65 @@
+"""Batches of independent replicas (psim_batch_create): one launch per phase
+over all replicas, each replica stepping bit for bit like the system built
+from its own settings."""
+import numpy as np
+import pytest
+
+from proteinsim2015_gb300 import init
+
+pytestmark = pytest.mark.gpu
+
+
+def ao_replica(psim, n, phi, contact_kT, q, seed):
+    """A replica as config C2 draws them: AO colloids (sigma = 1) at volume
+    fraction phi, contact attraction contact_kT, polymer/colloid ratio q."""
+    box = (n * np.pi / 6.0 / phi) ** (1.0 / 3.0)
+    rc = 1.0 + q
+    scale = max(3, int(np.floor(box / rc)))
+    g = psim.geometry(n, box, box / scale, scale)
+    wd = contact_kT * q / (1.5 + q)        # U(1) = -kT wd (rc + 0.5) / (rc - 1)
+    f = psim.make_force("AO", rc, kT=1.0, well_depth=wd)
+    pos = init.rsa(n, box, 1.0, seed=seed).reshape(-1)
+    return g, f, pos
+
+
+REPLICAS = [(700, 0.10, 2.0, 0.10), (2500, 0.25, 4.0, 0.15), (1200, 0.05, 1.0, 0.20),
+            (3100, 0.30, 6.0, 0.05), (513, 0.20, 3.0, 0.12)]
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_batch_steps_like_its_replicas(psim, precision):
+    reps, states = [], []
+    for k, (n, phi, a, q) in enumerate(REPLICAS):
+        g, f, pos = ao_replica(psim, n, phi, a, q, seed=60 + k)
+        reps.append((g, f, 1000 + 17 * k))
+        states.append(pos)
+    rng = np.random.default_rng(61)
+    vels = [rng.standard_normal(3 * g.n_particles) for g, _, _ in reps]
+    b = psim.Batch(reps, gamma=1.0, dt=0.001, kT=1.0, vel_freq=7, precision=precision)
+    b.upload(np.concatenate(states), np.full(b.n, 0.5), vel=np.concatenate(vels))
+    for k in (1, 5, 13):          # crosses graph phases and velocity steps
+        b.step(k)
+    out = b.download()
+    assert b.get_step()[0] == 19
+    for k, (g, f, seed) in enumerate(reps):
+        s = psim.System(g, f, gamma=1.0, dt=0.001, kT=1.0, vel_freq=7, seed=seed,
+                        precision=precision)
+        s.upload(states[k], np.full(g.n_particles, 0.5), vel=vels[k])
+        s.step(19)
+        ref = s.download()
+        s.close()
+        for key in ("pos", "pos0", "vel", "frc", "frc0"):
+            assert np.array_equal(b.split(out[key])[k], ref[key]), (k, key)
+    b.close()
+
+
+def test_batch_refuses_mixed_plugins(psim):
+    g1, f1, _ = ao_replica(psim, 500, 0.1, 2.0, 0.1, seed=62)
+    f2 = psim.make_force("LJ", 1.1, kT=1.0, well_depth=1.0, lj_num=6)
+    with pytest.raises(psim.PsimError) as e:
+        psim.Batch([(g1, f1, 1), (g1, f2, 2)])
+    assert e.value.code == psim.ERR_INPUT
+    f3 = psim.make_force("AO_YUK", 1.1, kT=1.0, well_depth=0.2, cutoff2=1.1, well_depth2=1.0,
+                         yukawa_strength=1.0, debye_length=0.25, lj_num=0)
+    with pytest.raises(psim.PsimError):
+        psim.Batch([(g1, f3, 1)])
