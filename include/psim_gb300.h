@@ -225,6 +225,16 @@ typedef struct {
     double skin;
 } psim_system_config;
 
+/* ---------------------------------------------- initial states (host) */
+
+/* Random sequential addition: n points uniform in the periodic cube of edge
+ * box, each at least min_sep from all earlier ones (pos: 3n, original order).
+ * Stands in for the reference's initialiser (systemInit.cpp:31-160), whose
+ * O(N^2) overlap sweep cannot build large or dense systems.  max_trials > 0
+ * bounds the attempts (7701 when exceeded, near the RSA jamming limit). */
+int psim_init_rsa(int32_t n, double box, double min_sep, uint64_t seed, int64_t max_trials,
+                  double* pos);
+
 /* ---------------------------------------------- batches of replicas */
 
 /* One replica of a batch: its own box and cell grid, plugin parameters and

@@ -27,8 +27,8 @@ SOURCES = {
     "psim_cells.cu": [],
     "psim_api.cu": [],
     "psim_noalloc.cu": [],
+    "psim_init.cu": [],
 }
-HEADERS = ["psim_device.cuh", "psim_kernels.cuh"]
 
 
 def nvcc():
@@ -47,7 +47,8 @@ def _stale(target, deps):
 
 def _compile(src, extra, verbose):
     obj = os.path.join(OUT_DIR, src.replace(".cu", ".o"))
-    deps = [os.path.join(CSRC, src)] + [os.path.join(CSRC, h) for h in HEADERS] + [
+    headers = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith(".cuh")]
+    deps = [os.path.join(CSRC, src)] + headers + [
         os.path.join(ROOT, "include", "psim_gb300.h"), __file__]
     if not _stale(obj, deps):
         return obj

@@ -26,6 +26,19 @@ def reference_box(n, radius, conc, scale):
     return box, cell, vp / float(box) ** 3
 
 
+def rsa_native(n, box, min_sep=1.0, seed=90210, max_trials=0):
+    """Random sequential addition in the native library (host code, O(1) per
+    trial): the same construction as rsa() with its own random stream, fast
+    enough for batches of millions of particles."""
+    import proteinsim2015_gb300 as psim
+    out = np.empty(3 * int(n))
+    rc = psim.lib().psim_init_rsa(int(n), float(box), float(min_sep), int(seed) & (2 ** 64 - 1),
+                                  int(max_trials), out.ctypes.data)
+    if rc != 0:
+        raise psim.PsimError(rc, psim.lib().psim_last_error_string().decode())
+    return out.reshape(-1, 3)
+
+
 def rsa(n, box, min_sep=1.0, seed=90210, max_tries=200):
     """Random sequential addition of n points in a periodic cube with minimum
     separation ``min_sep`` (a cell grid keeps each trial O(1))."""
