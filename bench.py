@@ -290,6 +290,35 @@ def e2e_dropin(psim, w, state, n_steps):
     return n * n_steps / el, h2d, d2h
 
 
+def run_batched(psim, dev, steps=2000, n_reps=512, tune=True):
+    """The batched-replica workload: 512 independent AO systems (N, phi,
+    contact attraction and q drawn per replica), gamma = 1, dt = 1e-3, mixed
+    form, every step one launch per phase over all replicas; each replica's
+    cell size chosen by the autotuner per size bucket."""
+    from proteinsim2015_gb300 import batch
+    draws = batch.c2_draws(n_reps)
+    t0 = time.time()
+    factors, report = batch.autotune(psim, draws, device=dev) if tune else ([1.0] * n_reps, {})
+    t_tune = time.time() - t0
+    pos, vel = batch.states(draws)
+    b = psim.Batch(batch.replicas(psim, draws, factors), gamma=1.0, dt=0.001, kT=1.0,
+                   vel_freq=1000, precision=psim.PRECISION_MIXED, device=dev)
+    b.upload(pos, np.full(b.n, 0.5), vel=vel)
+    b.step(3)
+    ms = b.time_steps(steps)
+    prof = b.profile(5)
+    value = b.n * steps / (ms * 1e-3)
+    b.close()
+    return {"workload": "c2_%d_ao_replicas" % n_reps, "value": value, "unit": UNIT,
+            "n_particles": int(b.n), "replicas": n_reps, "steps": steps,
+            "ms_per_step": ms / steps, "launches_per_step": 7,
+            "phases_ms": {k: round(v, 5) for k, v in prof.items()},
+            "autotune": {"seconds": round(t_tune, 1),
+                         "buckets": {str(k): {"factor": v[0],
+                                              "rates": {str(f): r for f, r in v[1].items()}}
+                                     for k, v in report.items()}}}
+
+
 def run_gpu(args):
     import proteinsim2015_gb300 as psim
     ws, rank, local = dist_env()
@@ -364,6 +393,11 @@ def run_gpu(args):
     peaks = measured_peaks()
     # ---- CPU baseline: the oracle restatement on the host cores, bounded sample
     cpu = cpu_baseline(15.0)
+    # ---- batched replicas (512 AO systems), against this single large system
+    batched = None
+    if args.batched_steps > 0 and ws == 1:
+        batched = run_batched(psim, dev, args.batched_steps)
+        batched["vs_single_system"] = batched["value"] / value
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps, "higher_is_better": True,
@@ -395,6 +429,7 @@ def run_gpu(args):
                      "peak_source": "measured FP32 FMA probe (MEASURED_PEAKS.json has no FP32 figure)",
                      "hbm_peak_gbs": peaks.get("hbm_gbs")},
         "cpu_baseline": cpu,
+        "batched": batched,
         "clocks": clk.summary(),
     }
     print(json.dumps(line))
@@ -412,6 +447,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-baseline-json", type=float, default=None,
                     help=argparse.SUPPRESS)
+    ap.add_argument("--batched-steps", type=int, default=2000,
+                    help="steps of the batched-replica run (0: skip it)")
     ap.add_argument("--skin", type=float, default=SKIN,
                     help="pair-list skin of the mixed form (0: walk the 27 cells every step)")
     ap.add_argument("--profile-only", action="store_true",
