@@ -312,6 +312,33 @@ int psim_system_get_step(psim_system* sys, int64_t* step, int32_t* vel_counter);
  * pass the next step will run (the pair list with a skin).  It does not step. */
 int psim_system_forces(psim_system* sys, double* force);
 
+/* ------------------------------------------- observables of the state */
+
+/* analysisManager::getTemperature (analysisGeneral.cpp:26-43): sum of v^2 over
+ * 3N, from the velocities of the last velocity step. */
+int psim_system_temperature(psim_system* sys, double* kT);
+/* analysisManager::meanDisplacement (analysisGeneral.cpp:45-55): mean
+ * |x - x0|^2 over the particles (x0: the previous position, re-imaged). */
+int psim_system_mean_displacement(psim_system* sys, double* msd);
+/* <EAP> of analysisOutput.cpp:117-123: particle::calculatePotential
+ * (particle.cpp:133-149, FP32 as there) averaged over the particles. */
+int psim_system_potential(psim_system* sys, double* eap);
+/* initDisplacementTracker (analysisTracker.cpp:26-37): from here on every
+ * crossing of the box is counted by the integrator. */
+int psim_system_track_start(psim_system* sys);
+/* trackedDisplacement (analysisTracker.cpp:66-85): mean squared unwrapped
+ * displacement since psim_system_track_start. */
+int psim_system_tracked_displacement(psim_system* sys, double* msd);
+/* system::updateInteractions (systemHandling.cpp:94-161): per particle, the
+ * neighbours of its 27 cells closer than r_contact (the reference uses 1.2);
+ * coor: n ints in original order (may be NULL), total: their sum (may be NULL).
+ * r_contact <= cellSize.  Single systems only. */
+int psim_system_interactions(psim_system* sys, double r_contact, int32_t* coor, int64_t* total);
+/* The radial distribution function: ordered pairs per particle with r in each
+ * of n_bins equal bins of [r_min, r_max), over the ideal-gas count
+ * N rho 4/3 pi (r1^3 - r0^3).  r_max <= cellSize.  Single systems only. */
+int psim_system_rdf(psim_system* sys, double r_min, double r_max, int32_t n_bins, double* g);
+
 /* Pair-list rebuilds since the upload (0 without a skin; the list the upload
  * builds is not counted). */
 int psim_system_list_builds(psim_system* sys, int32_t* builds);

@@ -137,6 +137,13 @@ def lib():
             "psim_system_get_step": ([P, C.POINTER(C.c_int64), C.POINTER(C.c_int32)], C.c_int),
             "psim_system_stream": ([P], P),
             "psim_system_list_builds": ([P, C.POINTER(C.c_int32)], C.c_int),
+            "psim_system_temperature": ([P, C.POINTER(C.c_double)], C.c_int),
+            "psim_system_mean_displacement": ([P, C.POINTER(C.c_double)], C.c_int),
+            "psim_system_potential": ([P, C.POINTER(C.c_double)], C.c_int),
+            "psim_system_track_start": ([P], C.c_int),
+            "psim_system_tracked_displacement": ([P, C.POINTER(C.c_double)], C.c_int),
+            "psim_system_interactions": ([P, C.c_double, P, C.POINTER(C.c_int64)], C.c_int),
+            "psim_system_rdf": ([P, C.c_double, C.c_double, C.c_int32, P], C.c_int),
             "psim_system_forces": ([P, P], C.c_int),
             "psim_system_profile": ([P, C.c_int32, P], C.c_int),
             "psim_system_launches_per_step": ([P], C.c_int),
@@ -427,6 +434,42 @@ class System:
         out = np.empty(3 * self.n)
         _check(lib().psim_system_forces(self._h, _p(out)))
         return out
+
+    def _scalar(self, fn):
+        v = C.c_double()
+        _check(fn(self._h, C.byref(v)))
+        return v.value
+
+    def temperature(self):
+        """sum v^2 / 3N of the last velocity step (getTemperature)."""
+        return self._scalar(lib().psim_system_temperature)
+
+    def mean_displacement(self):
+        """mean |x - x0|^2 (meanDisplacement)."""
+        return self._scalar(lib().psim_system_mean_displacement)
+
+    def potential(self):
+        """<EAP>: calculatePotential averaged over the particles."""
+        return self._scalar(lib().psim_system_potential)
+
+    def track_start(self):
+        _check(lib().psim_system_track_start(self._h))
+
+    def tracked_displacement(self):
+        """mean squared unwrapped displacement since track_start()."""
+        return self._scalar(lib().psim_system_tracked_displacement)
+
+    def interactions(self, r_contact=1.2):
+        """Coordination numbers (original order) and their sum (updateInteractions)."""
+        coor = np.empty(self.n, dtype=np.int32)
+        tot = C.c_int64()
+        _check(lib().psim_system_interactions(self._h, r_contact, _p(coor), C.byref(tot)))
+        return coor, tot.value
+
+    def rdf(self, r_min, r_max, n_bins):
+        g = np.empty(int(n_bins))
+        _check(lib().psim_system_rdf(self._h, r_min, r_max, int(n_bins), _p(g)))
+        return g
 
     def list_builds(self):
         b = C.c_int32()

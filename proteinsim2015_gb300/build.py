@@ -28,6 +28,7 @@ SOURCES = {
     "psim_api.cu": [],
     "psim_noalloc.cu": [],
     "psim_init.cu": [],
+    "psim_observe.cu": [],
 }
 
 

@@ -797,6 +797,9 @@ struct psim_system {
     // contiguous, so its particles keep their slot range in every cell order)
     int n_reps = 0, n_tasks = 0;
     DevBuf b_tasks, b_geoms, b_pairs, b_pre, b_rep, b_seeds;
+    // displacement tracker: box images crossed per particle and the start
+    // positions (original order), counted by the integrator once started
+    DevBuf img, track_start;
 };
 
 namespace {
@@ -916,6 +919,7 @@ int enqueue_step(psim_system* s, long long t, cudaEvent_t* evs) {
         a.geoms = s->b_geoms.as<DevGeom>();
         a.seeds = s->b_seeds.as<uint32_t>();
     }
+    a.img = s->img.as<int>();   // null until the displacement tracker starts
     NoiseView nz{s->cfg.noise_mode, s->noise.as<double>(), s->noise_first, s->noise_steps};
     if (s->cfg.precision == PSIM_PRECISION_FP64)
         PSIM_CUDA(launch_vgb_system(a, s->vp, s->g, nz, st));
@@ -1251,7 +1255,8 @@ void psim_system_destroy(psim_system* s) {
                       &s->posh, &s->posl, &s->vel, &s->err, &s->state, &s->occ, &s->noise,
                       &s->snap, &s->lslot[0], &s->lslot[1], &s->lbuild, &s->lpos, &s->list,
                       &s->lcount, &s->lflag, &s->lhalo, &s->lhcount, &s->b_tasks,
-                      &s->b_geoms, &s->b_pairs, &s->b_pre, &s->b_rep, &s->b_seeds};
+                      &s->b_geoms, &s->b_pairs, &s->b_pre, &s->b_rep, &s->b_seeds,
+                      &s->img, &s->track_start};
     for (DevBuf* b : arrs) b->release();
     for (int k = 0; k < 2; ++k) {
         s->pos[k].release(); s->pos0[k].release(); s->mem[k].release(); s->tag[k].release();
@@ -1551,6 +1556,197 @@ int psim_system_forces(psim_system* s, double* force) {
                                   out.as<double>(), s->st));
     PSIM_CUDA(cudaMemcpyAsync(force, out.p, 24 * (size_t)n, cudaMemcpyDeviceToHost, s->st));
     return settle(s);
+}
+
+// ------------------------------------------------------------ observables
+
+namespace {
+
+int ready(psim_system* s, const void* out) {
+    if (!s || !out) return fail(PSIM_ERR_INPUT, "NULL argument");
+    if (!s->uploaded) return fail(PSIM_ERR_INPUT, "no state uploaded");
+    return PSIM_OK;
+}
+
+// One reduction of the state after `total` steps, copied to the host.
+int reduce(psim_system* s, ObserveArgs& a, double* out) {
+    const Phase ph = phase_of(s->total);
+    const int n = s->n;
+    a.n = n;
+    a.x = d3(s->pos[ph.sb], n, 0); a.y = d3(s->pos[ph.sb], n, 1); a.z = d3(s->pos[ph.sb], n, 2);
+    a.x0 = d3(s->pos0[ph.sb], n, 0); a.y0 = d3(s->pos0[ph.sb], n, 1);
+    a.z0 = d3(s->pos0[ph.sb], n, 2);
+    a.fx = d3(s->frc[ph.fprev], n, 0); a.fy = d3(s->frc[ph.fprev], n, 1);
+    a.fz = d3(s->frc[ph.fprev], n, 2);
+    const int fb = (ph.fprev + 2) % 3;
+    a.gx = d3(s->frc[fb], n, 0); a.gy = d3(s->frc[fb], n, 1); a.gz = d3(s->frc[fb], n, 2);
+    a.perm_prev = s->perm[1 - ph.pb].as<int>();
+    a.tag = s->tag[1 - ph.ob].as<int>();   // the storage order's tags (as download)
+    a.L = s->g.L;
+    ScopedBuf scratch, res;
+    PSIM_CUDA(scratch.ensure(8 * (size_t)observe_scratch_doubles()));
+    PSIM_CUDA(res.ensure(8));
+    PSIM_CUDA(launch_observe(a, scratch.as<double>(), res.as<double>(), s->st));
+    PSIM_CUDA(cudaMemcpyAsync(out, res.p, 8, cudaMemcpyDeviceToHost, s->st));
+    PSIM_CUDA(cudaStreamSynchronize(s->st));
+    return PSIM_OK;
+}
+
+// The sorted FP64 positions of the current cell list and a 27-cell walk.
+int pair_scan(psim_system* s, PairScanArgs& a) {
+    if (s->n_reps) return fail(PSIM_ERR_INPUT, "pair observables are per system, not per batch");
+    const Phase ph = phase_of(s->total);
+    ScopedBuf pd;
+    PSIM_CUDA(pd.ensure(32 * (size_t)s->n));
+    PSIM_CUDA(launch_gather_posd(s->n, s->perm[ph.pb].as<int>(), d3(s->pos[ph.sb], s->n, 0),
+                                 d3(s->pos[ph.sb], s->n, 1), d3(s->pos[ph.sb], s->n, 2),
+                                 s->radius[ph.ob].as<double>(), pd.as<double4_32a>(), s->st));
+    a.g = s->g;
+    a.posd = pd.as<double4_32a>();
+    a.cellid = s->cellid.as<int>();
+    a.cstart = s->start.as<int>();
+    a.ccount = s->count[ph.cb].as<int>();
+    a.tag = s->tag[ph.ob].as<int>();
+    PSIM_CUDA(launch_pair_scan(a, s->st));
+    PSIM_CUDA(cudaStreamSynchronize(s->st));
+    return PSIM_OK;
+}
+
+}  // namespace
+
+int psim_system_temperature(psim_system* s, double* kT) {
+    int rc = ready(s, kT);
+    if (rc) return rc;
+    DeviceGuard dg(s->device);
+    if ((rc = settle(s))) return rc;
+    ScopedBuf scratch, res;
+    PSIM_CUDA(scratch.ensure(8 * (size_t)observe_scratch_doubles()));
+    PSIM_CUDA(res.ensure(8));
+    PSIM_CUDA(launch_sum_squares(3LL * s->n, s->vel.as<double>(), scratch.as<double>(),
+                                 res.as<double>(), s->st));
+    double v2 = 0.0;
+    PSIM_CUDA(cudaMemcpyAsync(&v2, res.p, 8, cudaMemcpyDeviceToHost, s->st));
+    PSIM_CUDA(cudaStreamSynchronize(s->st));
+    *kT = s->n ? v2 / 3.0 / s->n : 0.0;
+    return PSIM_OK;
+}
+
+int psim_system_mean_displacement(psim_system* s, double* msd) {
+    int rc = ready(s, msd);
+    if (rc) return rc;
+    DeviceGuard dg(s->device);
+    if ((rc = settle(s))) return rc;
+    ObserveArgs a{};
+    a.what = OBS_MEAN_DISP;
+    double sum = 0.0;
+    if ((rc = reduce(s, a, &sum))) return rc;
+    *msd = s->n ? sum / s->n : 0.0;
+    return PSIM_OK;
+}
+
+int psim_system_potential(psim_system* s, double* eap) {
+    int rc = ready(s, eap);
+    if (rc) return rc;
+    DeviceGuard dg(s->device);
+    if ((rc = settle(s))) return rc;
+    ObserveArgs a{};
+    a.what = OBS_POTENTIAL;
+    double sum = 0.0;
+    if ((rc = reduce(s, a, &sum))) return rc;
+    *eap = s->n ? sum / s->n : 0.0;
+    return PSIM_OK;
+}
+
+int psim_system_track_start(psim_system* s) {
+    if (!s) return fail(PSIM_ERR_INPUT, "NULL system");
+    if (!s->uploaded) return fail(PSIM_ERR_INPUT, "no state uploaded");
+    if (s->n_reps) return fail(PSIM_ERR_INPUT, "the tracker is per system, not per batch");
+    DeviceGuard dg(s->device);
+    int rc = settle(s);
+    if (rc) return rc;
+    const size_t b = 24 * (size_t)s->n;
+    const bool fresh = s->img.p == nullptr;
+    PSIM_CUDA(s->img.ensure(12 * (size_t)s->n));
+    PSIM_CUDA(s->track_start.ensure(b));
+    if (fresh) drop_graphs(s);   // the captured steps start counting images
+    const Phase ph = phase_of(s->total);
+    PSIM_CUDA(cudaMemsetAsync(s->img.p, 0, 12 * (size_t)s->n, s->st));
+    PSIM_CUDA(launch_merge_xyz(s->n, d3(s->pos[ph.sb], s->n, 0), d3(s->pos[ph.sb], s->n, 1),
+                               d3(s->pos[ph.sb], s->n, 2), s->tag[1 - ph.ob].as<int>(), nullptr,
+                               s->track_start.as<double>(), s->st));
+    PSIM_CUDA(cudaStreamSynchronize(s->st));
+    return PSIM_OK;
+}
+
+int psim_system_tracked_displacement(psim_system* s, double* msd) {
+    int rc = ready(s, msd);
+    if (rc) return rc;
+    if (!s->img.p) return fail(PSIM_ERR_INPUT, "the displacement tracker was not started");
+    DeviceGuard dg(s->device);
+    if ((rc = settle(s))) return rc;
+    ObserveArgs a{};
+    a.what = OBS_TRACKED;
+    a.img = s->img.as<int>();
+    a.start = s->track_start.as<double>();
+    double sum = 0.0;
+    if ((rc = reduce(s, a, &sum))) return rc;
+    *msd = s->n ? sum / s->n : 0.0;
+    return PSIM_OK;
+}
+
+int psim_system_interactions(psim_system* s, double r_contact, int32_t* coor, int64_t* total) {
+    if (!s || !s->uploaded) return fail(PSIM_ERR_INPUT, "NULL system or no state uploaded");
+    if (!(r_contact > 0.0) || r_contact > s->g.cs)
+        return fail(PSIM_ERR_INPUT, "contact distance %g outside (0, cellSize]", r_contact);
+    DeviceGuard dg(s->device);
+    int rc = settle(s);
+    if (rc) return rc;
+    ScopedBuf cb, tot;
+    PSIM_CUDA(cb.ensure(4 * (size_t)s->n));
+    PSIM_CUDA(tot.ensure(8));
+    PSIM_CUDA(cudaMemsetAsync(tot.p, 0, 8, s->st));
+    PairScanArgs a{};
+    a.r_contact = r_contact;
+    a.coor = cb.as<int>();
+    a.n_pairs = tot.as<unsigned long long>();
+    if ((rc = pair_scan(s, a))) return rc;
+    if (coor) PSIM_CUDA(cudaMemcpy(coor, cb.p, 4 * (size_t)s->n, cudaMemcpyDeviceToHost));
+    unsigned long long t = 0;
+    PSIM_CUDA(cudaMemcpy(&t, tot.p, 8, cudaMemcpyDeviceToHost));
+    if (total) *total = (int64_t)t;
+    return PSIM_OK;
+}
+
+int psim_system_rdf(psim_system* s, double r_min, double r_max, int32_t n_bins, double* g_r) {
+    if (!s || !g_r || !s->uploaded) return fail(PSIM_ERR_INPUT, "NULL argument or no state");
+    if (!(r_min >= 0.0) || !(r_max > r_min) || r_max > s->g.cs || n_bins <= 0 || n_bins > 8192)
+        return fail(PSIM_ERR_INPUT, "g(r) range [%g, %g) with %d bins: need 0 <= r_min < r_max "
+                    "<= cellSize and 1..8192 bins", r_min, r_max, n_bins);
+    DeviceGuard dg(s->device);
+    int rc = settle(s);
+    if (rc) return rc;
+    ScopedBuf hb;
+    PSIM_CUDA(hb.ensure(8 * (size_t)n_bins));
+    PSIM_CUDA(cudaMemsetAsync(hb.p, 0, 8 * (size_t)n_bins, s->st));
+    PairScanArgs a{};
+    a.r_contact = 0.0;
+    a.r_min = r_min;
+    a.r_max = r_max;
+    a.inv_dr = n_bins / (r_max - r_min);
+    a.n_bins = n_bins;
+    a.hist = hb.as<unsigned long long>();
+    if ((rc = pair_scan(s, a))) return rc;
+    std::vector<unsigned long long> h((size_t)n_bins);
+    PSIM_CUDA(cudaMemcpy(h.data(), hb.p, 8 * (size_t)n_bins, cudaMemcpyDeviceToHost));
+    // ordered pairs per particle in each shell over the ideal-gas count
+    const double rho = s->n / (s->g.L * s->g.L * s->g.L);
+    const double dr = (r_max - r_min) / n_bins;
+    for (int k = 0; k < n_bins; ++k) {
+        const double r0 = r_min + k * dr, r1 = r0 + dr;
+        const double shell = 4.0 / 3.0 * M_PI * (r1 * r1 * r1 - r0 * r0 * r0);
+        g_r[k] = s->n ? (double)h[(size_t)k] / (s->n * rho * shell) : 0.0;
+    }
+    return PSIM_OK;
 }
 
 int psim_system_list_builds(psim_system* s, int32_t* builds) {

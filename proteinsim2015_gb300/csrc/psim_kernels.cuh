@@ -161,6 +161,9 @@ struct VgbSystemArgs {
     const int* rep;
     const DevGeom* geoms;
     const uint32_t* seeds;
+    // box images each particle has crossed (3n, original order; may be null):
+    // the unwrapped position is x + img L
+    int* img;
 };
 cudaError_t launch_vgb_system(const VgbSystemArgs& a, const VgbParams& p, const DevGeom& g,
                               const NoiseView& nz, cudaStream_t st);
@@ -286,5 +289,43 @@ cudaError_t launch_pair_count(const DevGeom& g, const CellView& cv, float rc2,
                               unsigned long long* total, cudaStream_t st);
 // FMA-chain throughput probe: `iters` rounds of 8 independent FMA chains per thread.
 cudaError_t launch_fma_probe(int blocks, int threads, int iters, float* sink, cudaStream_t st);
+
+// Observables of the device-resident state (psim_observe.cu).
+enum ObserveWhat { OBS_MEAN_DISP = 0, OBS_TRACKED = 1, OBS_POTENTIAL = 2 };
+struct ObserveArgs {
+    int n;
+    int what;                   // ObserveWhat
+    const double* x; const double* y; const double* z;      // positions, storage order
+    const double* x0; const double* y0; const double* z0;   // previous positions, same order
+    const double* fx; const double* fy; const double* fz;   // force of the last step, same order
+    const double* gx; const double* gy; const double* gz;   // the force before, previous order
+    const int* perm_prev;       // storage slot -> slot of the previous order
+    const int* tag;             // original index of each storage slot
+    const int* img;             // box images crossed (3n, original order)
+    const double* start;        // positions when tracking started (3n, original order)
+    double L;
+};
+// sum of v[i]^2 (count values); scratch: observe_scratch_doubles() doubles
+cudaError_t launch_sum_squares(long long count, const double* v, double* scratch, double* out,
+                               cudaStream_t st);
+cudaError_t launch_observe(const ObserveArgs& a, double* scratch, double* out, cudaStream_t st);
+int observe_scratch_doubles();
+// 27-cell walk over sorted FP64 positions: coordination numbers (r < r_contact,
+// written at the original index) and a histogram of r in [r_min, r_max)
+struct PairScanArgs {
+    DevGeom g;
+    const double4_32a* posd;
+    const int* cellid;
+    const int* cstart;
+    const int* ccount;
+    const int* tag;
+    double r_contact;
+    int* coor;                      // may be null
+    unsigned long long* n_pairs;    // may be null: sum of the coordination numbers
+    double r_min, r_max, inv_dr;
+    int n_bins;                     // 0: no histogram
+    unsigned long long* hist;
+};
+cudaError_t launch_pair_scan(const PairScanArgs& a, cudaStream_t st);
 
 }  // namespace psim

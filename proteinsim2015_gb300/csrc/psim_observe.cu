@@ -1,0 +1,162 @@
+// psim_observe.cu -- observables of the device-resident state: the analysis
+// the reference runs between steps, on the GPU so the state stays in HBM.
+//
+//   temperature          analysisManager::getTemperature  (analysisGeneral.cpp:26-43)
+//   mean displacement    analysisManager::meanDisplacement (analysisGeneral.cpp:45-55)
+//   tracked displacement trackedDisplacement (analysisTracker.cpp:26-85), every wrap counted
+//   potential ("EAP")    particle::calculatePotential (particle.cpp:133-149), summed
+//   coordination         system::updateInteractions (systemHandling.cpp:94-161)
+//   g(r)                 a pair-distance histogram over the same 27-cell walk
+//
+// Sums are deterministic: each block writes its partial, one block adds the
+// partials in block order.
+#include "psim_kernels.cuh"
+
+namespace psim {
+
+namespace {
+
+constexpr int kRedThreads = 256;
+constexpr int kRedBlocks = 512;
+
+__device__ double block_sum(double v, double* sh) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x == 0)
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += sh[k];
+    __syncthreads();
+    return t;  // valid in thread 0
+}
+
+__global__ void __launch_bounds__(kRedThreads) finish_kernel(const double* part, int n, double* out) {
+    __shared__ double sh[kRedThreads / 32];
+    // each thread adds a fixed stride of partials, then the block in lane order
+    double v = 0.0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) v += part[k];
+    const double t = block_sum(v, sh);
+    if (threadIdx.x == 0) *out = t;
+}
+
+// sum of |v|^2 over count values
+__global__ void __launch_bounds__(kRedThreads) sumsq_kernel(long long count, const double* v,
+                                                            double* part) {
+    __shared__ double sh[kRedThreads / 32];
+    double s = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count;
+         i += (long long)gridDim.x * blockDim.x)
+        s += v[i] * v[i];
+    const double t = block_sum(s, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+__global__ void __launch_bounds__(kRedThreads) observe_kernel(ObserveArgs a, double* part) {
+    __shared__ double sh[kRedThreads / 32];
+    double s = 0.0;
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < a.n; f += gridDim.x * blockDim.x) {
+        const double x[3] = {a.x[f], a.y[f], a.z[f]};
+        if (a.what == OBS_MEAN_DISP) {
+            const double d0 = x[0] - a.x0[f], d1 = x[1] - a.y0[f], d2 = x[2] - a.z0[f];
+            s += d0 * d0 + d1 * d1 + d2 * d2;
+        } else if (a.what == OBS_TRACKED) {
+            const int t = a.tag[f];
+            for (int k = 0; k < 3; ++k) {
+                // the reference sums this in FP32 (analysisTracker.cpp:68-83)
+                const double d = (x[k] + a.L * a.img[3 * (size_t)t + k]) - a.start[3 * (size_t)t + k];
+                s += d * d;
+            }
+        } else {  // OBS_POTENTIAL: particle::calculatePotential in FP32
+            const int o = a.perm_prev ? a.perm_prev[f] : f;
+            const float dx = (float)(x[0] - a.x0[f]), dy = (float)(x[1] - a.y0[f]),
+                        dz = (float)(x[2] - a.z0[f]);
+            const double F[3] = {a.fx[f], a.fy[f], a.fz[f]};
+            const double G[3] = {a.gx[o], a.gy[o], a.gz[o]};
+            const float dfx = (float)(F[0] - G[0]), dfy = (float)(F[1] - G[1]),
+                        dfz = (float)(F[2] - G[2]);
+            const float dr = sqrtf(dx * dx + dy * dy + dz * dz);
+            const float df = sqrtf(dfx * dfx + dfy * dfy + dfz * dfz);
+            const float f0 = sqrtf((float)(G[0] * G[0] + G[1] * G[1] + G[2] * G[2]));
+            const float p = (f0 * dr) + (0.5f * df * dr);
+            s += (double)(-p);
+        }
+    }
+    const double t = block_sum(s, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+// The 27-cell walk of updateInteractions (systemHandling.cpp:126-161) on
+// the sorted FP64 positions: neighbours closer than r_contact are counted
+// (pbcDist's minimum image, utilities.cpp:79-104), and distances in
+// [r_min, r_max) are binned for g(r).
+__global__ void __launch_bounds__(128) pairs_kernel(PairScanArgs a) {
+    extern __shared__ unsigned int hist[];
+    for (int b = threadIdx.x; b < a.n_bins; b += blockDim.x) hist[b] = 0u;
+    __syncthreads();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < a.g.n) {
+        const double4_32a pi = a.posd[i];
+        const int c = a.cellid[i];
+        const int cx = c % a.g.s, cy = (c / a.g.s) % a.g.s, cz = c / a.g.s2;
+        int coor = 0;
+        for (int dx = -1; dx <= 1; ++dx)
+            for (int dy = -1; dy <= 1; ++dy)
+                for (int dz = -1; dz <= 1; ++dz) {
+                    int sh;
+                    const int x = wrap_cell(cx + dx, a.g.s, sh);
+                    const int y = wrap_cell(cy + dy, a.g.s, sh);
+                    const int z = wrap_cell(cz + dz, a.g.s, sh);
+                    const int cell = x + a.g.s * y + a.g.s2 * z;
+                    const int st = a.cstart[cell], en = st + a.ccount[cell];
+                    for (int j = st; j < en; ++j) {
+                        if (j == i) continue;
+                        const double4_32a pj = a.posd[j];
+                        double d0 = fabs(pj.x - pi.x), d1 = fabs(pj.y - pi.y),
+                               d2 = fabs(pj.z - pi.z);
+                        if (d0 > a.g.half) d0 -= a.g.L;
+                        if (d1 > a.g.half) d1 -= a.g.L;
+                        if (d2 > a.g.half) d2 -= a.g.L;
+                        const double r = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+                        if (r < a.r_contact) ++coor;
+                        if (a.n_bins > 0 && r >= a.r_min && r < a.r_max) {
+                            int b = (int)((r - a.r_min) * a.inv_dr);
+                            b = b < a.n_bins ? b : a.n_bins - 1;
+                            atomicAdd(&hist[b], 1u);
+                        }
+                    }
+                }
+        if (a.coor) a.coor[a.tag[i]] = coor;
+        if (a.n_pairs) atomicAdd(a.n_pairs, (unsigned long long)coor);
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < a.n_bins; b += blockDim.x)
+        if (hist[b]) atomicAdd(&a.hist[b], (unsigned long long)hist[b]);
+}
+
+}  // namespace
+
+cudaError_t launch_sum_squares(long long count, const double* v, double* scratch, double* out,
+                               cudaStream_t st) {
+    sumsq_kernel<<<kRedBlocks, kRedThreads, 0, st>>>(count, v, scratch);
+    finish_kernel<<<1, kRedThreads, 0, st>>>(scratch, kRedBlocks, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_observe(const ObserveArgs& a, double* scratch, double* out, cudaStream_t st) {
+    observe_kernel<<<kRedBlocks, kRedThreads, 0, st>>>(a, scratch);
+    finish_kernel<<<1, kRedThreads, 0, st>>>(scratch, kRedBlocks, out);
+    return cudaGetLastError();
+}
+
+int observe_scratch_doubles() { return kRedBlocks; }
+
+cudaError_t launch_pair_scan(const PairScanArgs& a, cudaStream_t st) {
+    if (a.g.n == 0) return cudaSuccess;
+    const size_t smem = sizeof(unsigned int) * (size_t)(a.n_bins > 0 ? a.n_bins : 1);
+    pairs_kernel<<<(a.g.n + 127) / 128, 128, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace psim

@@ -321,6 +321,13 @@ vgb_system_kernel(VgbSystemArgs a, VgbParams p, DevGeom g0, NoiseView nz) {
     a.ox[f] = xn[0]; a.oy[f] = xn[1]; a.oz[f] = xn[2];
     a.ox0[f] = x0n[0]; a.oy0[f] = x0n[1]; a.oz0[f] = x0n[2];
     a.omx[f] = mx[0]; a.omy[f] = mx[1]; a.omz[f] = mx[2];
+    if (a.img) {
+        // a wrap re-imaged the previous position by one box: count it
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+            if (__double_as_longlong(x0n[k]) != __double_as_longlong(x[k]))
+                a.img[3 * (size_t)tag + k] += (x0n[k] < x[k]) ? 1 : -1;
+    }
     if (vel_step) {
         a.vel[3 * (size_t)tag] = v[0];
         a.vel[3 * (size_t)tag + 1] = v[1];

@@ -1,0 +1,89 @@
+"""Observables of the device-resident state against numpy restatements of
+the reference's analysis routines on the downloaded state."""
+import numpy as np
+import pytest
+
+from gpu_helpers import rsa_state
+
+pytestmark = pytest.mark.gpu
+
+
+def ao_system(psim, n=600, box=12.0, scale=4, precision=0, vel_freq=0, seed=70, skin=0.0):
+    pos, rad = rsa_state(n, box, seed=seed)
+    g = psim.geometry(n, box, box / scale, scale)
+    s = psim.System(g, psim.make_force("AO", 1.1, kT=1.0, well_depth=0.25), gamma=1.0,
+                    dt=0.002, kT=1.0, vel_freq=vel_freq, precision=precision, skin=skin)
+    s.upload(pos, rad, vel=np.random.default_rng(seed).standard_normal(3 * n))
+    return s, g
+
+
+def min_image(d, L):
+    # pbcDist (utilities.cpp:79-104): |d| > L/2 -> |d| - L
+    a = np.abs(d)
+    return np.where(a > L / 2.0, a - L, a)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_temperature_displacement_and_potential(psim, precision):
+    s, g = ao_system(psim, precision=precision)
+    s.step(25)
+    st = s.download()
+    n = g.n_particles
+    v = st["vel"]
+    assert s.temperature() == pytest.approx(np.sum(v * v) / 3.0 / n, rel=1e-12)
+    d = st["pos"] - st["pos0"]
+    assert s.mean_displacement() == pytest.approx(np.sum(d * d) / n, rel=1e-12)
+    # particle::calculatePotential in FP32, averaged (analysisOutput.cpp:117-123)
+    f32 = np.float32
+    dx = (st["pos"] - st["pos0"]).reshape(-1, 3).astype(f32)
+    df = (st["frc"] - st["frc0"]).reshape(-1, 3).astype(f32)
+    f0 = st["frc0"].reshape(-1, 3)
+    dr = np.sqrt(np.sum(dx * dx, axis=1, dtype=f32))
+    dfn = np.sqrt(np.sum(df * df, axis=1, dtype=f32))
+    f0n = np.sqrt(np.sum(f0 * f0, axis=1).astype(f32))
+    pot = -(f0n * dr + f32(0.5) * dfn * dr)
+    assert s.potential() == pytest.approx(np.mean(pot.astype(np.float64)), rel=1e-5, abs=1e-9)
+    s.close()
+
+
+def test_tracked_displacement_counts_every_wrap(psim):
+    s, g = ao_system(psim, n=400, box=9.0, scale=3, precision=1)
+    L = g.box_size
+    s.step(2)
+    s.track_start()
+    start = s.download()["pos"].copy()
+    prev, unwrapped = start.copy(), start.copy()
+    for _ in range(40):
+        s.step(5)   # a particle moves far less than L/2 in 5 steps
+        cur = s.download()["pos"]
+        d = cur - prev
+        d -= L * np.round(d / L)
+        unwrapped += d
+        prev = cur
+    ref = np.mean(np.sum(((unwrapped - start) ** 2).reshape(-1, 3), axis=1))
+    assert np.any(np.abs(unwrapped - prev) > L / 2)   # some particle did cross the box
+    assert s.tracked_displacement() == pytest.approx(ref, rel=1e-9)
+    s.close()
+
+
+@pytest.mark.parametrize("skin", [0.0, 0.4])
+def test_interactions_and_rdf_match_all_pairs(psim, skin):
+    s, g = ao_system(psim, n=700, box=12.0, scale=4, precision=1, skin=skin)
+    s.step(10)
+    hi, cse, srt = s.download_cells()
+    pos = s.download()["pos"].reshape(-1, 3)
+    L = g.box_size
+    d = min_image(pos[:, None, :] - pos[None, :, :], L)
+    r = np.sqrt(np.sum(d * d, axis=2))
+    np.fill_diagonal(r, np.inf)
+    coor, tot = s.interactions(1.2)
+    assert np.array_equal(coor, np.sum(r < 1.2, axis=1))
+    assert tot == int(np.sum(r < 1.2))
+    rmin, rmax, nb = 0.8, 3.0, 44
+    gr = s.rdf(rmin, rmax, nb)
+    hist, edges = np.histogram(r[np.isfinite(r)], bins=nb, range=(rmin, rmax))
+    n = g.n_particles
+    rho = n / L ** 3
+    shell = 4.0 / 3.0 * np.pi * (edges[1:] ** 3 - edges[:-1] ** 3)
+    assert np.allclose(gr, hist / (n * rho * shell), rtol=1e-12)
+    s.close()
