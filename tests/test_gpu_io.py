@@ -1,0 +1,49 @@
+"""Snapshot frames copied on the side stream while the system steps, and
+recovery images that restart a system (RecoverySystem semantics)."""
+import numpy as np
+import pytest
+
+from gpu_helpers import rsa_state
+from proteinsim2015_gb300 import io
+
+pytestmark = pytest.mark.gpu
+
+
+def make(psim, pos, rad, n, box=12.0, scale=4):
+    g = psim.geometry(n, box, box / scale, scale)
+    s = psim.System(g, psim.make_force("AO", 1.1, kT=1.0, well_depth=0.25), dt=0.002,
+                    precision=psim.PRECISION_MIXED)
+    s.upload(pos, rad)
+    return s
+
+
+def test_frame_overlaps_steps_and_recovery_restarts(psim, tmp_path):
+    n = 500
+    pos, rad = rsa_state(n, 12.0, seed=80)
+    a, b = make(psim, pos, rad, n), make(psim, pos, rad, n)
+    w = io.SnapshotWriter(a, str(tmp_path / "trial"), exact=True)
+    a.step(5)
+    path = w.frame(5.0)
+    a.step_async(7)          # the copy of step 5's positions overlaps these steps
+    w.wait()
+    a.sync()
+    b.step(5)
+    lines = open(path).read().split("\n")
+    assert lines[0] == str(n) and lines[1] == "Current Time: 5"
+    got = np.array([[float(v) for v in line.split()[1:]] for line in lines[2:2 + n]]).reshape(-1)
+    assert np.array_equal(got, b.download()["pos"])
+    # a recovery image of step 12, read back into a fresh system: the next
+    # step is firstStep, as after RecoverySystem
+    rec = w.recovery(12.0, np.ones(n), rad)
+    assert rec.endswith("snapshots/time-12/recovery.txt")
+    c = make(psim, pos, rad, n)
+    st = io.recover(c, rec)
+    assert c.get_step()[0] == 0
+    d = c.download()
+    ref = a.download()
+    for k in ("pos", "frc", "frc0"):
+        assert np.array_equal(d[k], ref[k]), k
+    c.step(3)
+    assert np.all(np.isfinite(c.download()["pos"]))
+    for s in (a, b, c):
+        s.close()
