@@ -334,6 +334,16 @@ int psim_system_tracked_displacement(psim_system* sys, double* msd);
  * coor: n ints in original order (may be NULL), total: their sum (may be NULL).
  * r_contact <= cellSize.  Single systems only. */
 int psim_system_interactions(psim_system* sys, double r_contact, int32_t* coor, int64_t* total);
+/* analysisManager::findClusters / writeClusters (analysisCluster.cpp:26-78):
+ * the connected components of the contact graph (pairs closer than r_contact,
+ * the reference uses 1.2).  root: n ints in original order (may be NULL), the
+ * smallest original index of each particle's cluster; n_clusters: clusters of
+ * more than min_size particles (the reference keeps > 4); avg_size: their
+ * members over their number, in integers as writeClusters returns it.
+ * r_contact <= cellSize.  Single systems only. */
+int psim_system_clusters(psim_system* sys, double r_contact, int32_t min_size, int32_t* root,
+                         int32_t* n_clusters, int32_t* avg_size);
+
 /* The radial distribution function: ordered pairs per particle with r in each
  * of n_bins equal bins of [r_min, r_max), over the ideal-gas count
  * N rho 4/3 pi (r1^3 - r0^3).  r_max <= cellSize.  Single systems only. */

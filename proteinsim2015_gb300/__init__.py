@@ -144,6 +144,8 @@ def lib():
             "psim_system_tracked_displacement": ([P, C.POINTER(C.c_double)], C.c_int),
             "psim_system_interactions": ([P, C.c_double, P, C.POINTER(C.c_int64)], C.c_int),
             "psim_system_rdf": ([P, C.c_double, C.c_double, C.c_int32, P], C.c_int),
+            "psim_system_clusters": ([P, C.c_double, C.c_int32, P, C.POINTER(C.c_int32),
+                                      C.POINTER(C.c_int32)], C.c_int),
             "psim_system_forces": ([P, P], C.c_int),
             "psim_system_profile": ([P, C.c_int32, P], C.c_int),
             "psim_system_launches_per_step": ([P], C.c_int),
@@ -465,6 +467,20 @@ class System:
         tot = C.c_int64()
         _check(lib().psim_system_interactions(self._h, r_contact, _p(coor), C.byref(tot)))
         return coor, tot.value
+
+    def clusters(self, r_contact=1.2, min_size=4):
+        """findClusters + writeClusters: (root of every particle -- the smallest
+        original index of its cluster --, the clusters of more than min_size
+        particles as sorted index arrays in root order, their integer mean size)."""
+        root = np.empty(self.n, dtype=np.int32)
+        nc, avg = C.c_int32(), C.c_int32()
+        _check(lib().psim_system_clusters(self._h, r_contact, int(min_size), _p(root),
+                                          C.byref(nc), C.byref(avg)))
+        order = np.argsort(root, kind="stable")
+        bounds = np.flatnonzero(np.diff(root[order])) + 1
+        groups = [g for g in np.split(order, bounds) if len(g) > min_size]
+        assert len(groups) == nc.value
+        return root, groups, avg.value
 
     def rdf(self, r_min, r_max, n_bins):
         g = np.empty(int(n_bins))

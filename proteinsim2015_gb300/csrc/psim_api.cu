@@ -1592,11 +1592,11 @@ int reduce(psim_system* s, ObserveArgs& a, double* out) {
     return PSIM_OK;
 }
 
-// The sorted FP64 positions of the current cell list and a 27-cell walk.
-int pair_scan(psim_system* s, PairScanArgs& a) {
+// The sorted FP64 positions of the current cell list (into pd) and the cell
+// ranges, for a 27-cell walk.
+int sorted_view(psim_system* s, ScopedBuf& pd, PairScanArgs& a) {
     if (s->n_reps) return fail(PSIM_ERR_INPUT, "pair observables are per system, not per batch");
     const Phase ph = phase_of(s->total);
-    ScopedBuf pd;
     PSIM_CUDA(pd.ensure(32 * (size_t)s->n));
     PSIM_CUDA(launch_gather_posd(s->n, s->perm[ph.pb].as<int>(), d3(s->pos[ph.sb], s->n, 0),
                                  d3(s->pos[ph.sb], s->n, 1), d3(s->pos[ph.sb], s->n, 2),
@@ -1607,6 +1607,13 @@ int pair_scan(psim_system* s, PairScanArgs& a) {
     a.cstart = s->start.as<int>();
     a.ccount = s->count[ph.cb].as<int>();
     a.tag = s->tag[ph.ob].as<int>();
+    return PSIM_OK;
+}
+
+int pair_scan(psim_system* s, PairScanArgs& a) {
+    ScopedBuf pd;
+    int rc = sorted_view(s, pd, a);
+    if (rc) return rc;
     PSIM_CUDA(launch_pair_scan(a, s->st));
     PSIM_CUDA(cudaStreamSynchronize(s->st));
     return PSIM_OK;
@@ -1714,6 +1721,48 @@ int psim_system_interactions(psim_system* s, double r_contact, int32_t* coor, in
     unsigned long long t = 0;
     PSIM_CUDA(cudaMemcpy(&t, tot.p, 8, cudaMemcpyDeviceToHost));
     if (total) *total = (int64_t)t;
+    return PSIM_OK;
+}
+
+int psim_system_clusters(psim_system* s, double r_contact, int32_t min_size, int32_t* root,
+                         int32_t* n_clusters, int32_t* avg_size) {
+    if (!s || !s->uploaded) return fail(PSIM_ERR_INPUT, "NULL system or no state uploaded");
+    if (!(r_contact > 0.0) || r_contact > s->g.cs)
+        return fail(PSIM_ERR_INPUT, "contact distance %g outside (0, cellSize]", r_contact);
+    DeviceGuard dg(s->device);
+    int rc = settle(s);
+    if (rc) return rc;
+    const size_t n = (size_t)s->n;
+    ScopedBuf pd, lab, rt, sz, eb;
+    PSIM_CUDA(lab.ensure(4 * n));
+    PSIM_CUDA(rt.ensure(4 * n));
+    PSIM_CUDA(sz.ensure(4 * n));
+    PSIM_CUDA(eb.ensure(4));
+    PSIM_CUDA(cudaMemsetAsync(sz.p, 0, 4 * n, s->st));
+    PSIM_CUDA(cudaMemsetAsync(eb.p, 0, 4, s->st));
+    PairScanArgs a{};
+    a.r_contact = r_contact;
+    if ((rc = sorted_view(s, pd, a))) return rc;
+    PSIM_CUDA(launch_clusters(a, lab.as<int>(), rt.as<int>(), sz.as<int>(), eb.as<uint32_t>(),
+                              s->st));
+    std::vector<int> hroot(n), hsize(n);
+    uint32_t bits = 0;
+    PSIM_CUDA(cudaMemcpyAsync(hroot.data(), rt.p, 4 * n, cudaMemcpyDeviceToHost, s->st));
+    PSIM_CUDA(cudaMemcpyAsync(hsize.data(), sz.p, 4 * n, cudaMemcpyDeviceToHost, s->st));
+    PSIM_CUDA(cudaMemcpyAsync(&bits, eb.p, 4, cudaMemcpyDeviceToHost, s->st));
+    PSIM_CUDA(cudaStreamSynchronize(s->st));
+    if (bits) return fail(PSIM_ERR_INPUT, "cluster search did not converge");
+    if (root) std::copy(hroot.begin(), hroot.end(), root);
+    // analysisManager::writeClusters (analysisCluster.cpp:64-78): clusters of
+    // more than min_size particles, and their integer mean size
+    long long members = 0, count = 0;
+    for (size_t i = 0; i < n; ++i)
+        if (hroot[i] == (int)i && hsize[i] > min_size) {
+            ++count;
+            members += hsize[i];
+        }
+    if (n_clusters) *n_clusters = (int32_t)count;
+    if (avg_size) *avg_size = count ? (int32_t)(members / count) : 0;
     return PSIM_OK;
 }
 

@@ -327,5 +327,10 @@ struct PairScanArgs {
     unsigned long long* hist;
 };
 cudaError_t launch_pair_scan(const PairScanArgs& a, cudaStream_t st);
+// Clusters of the contact graph (r < a.r_contact): root[original index] = the
+// smallest original index of its cluster, size[root] = cluster size (zeroed
+// by the caller); label: union-find scratch (n ints).
+cudaError_t launch_clusters(const PairScanArgs& a, int* label, int* root, int* size,
+                            uint32_t* err, cudaStream_t st);
 
 }  // namespace psim

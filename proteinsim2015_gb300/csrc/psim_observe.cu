@@ -135,7 +135,105 @@ __global__ void __launch_bounds__(128) pairs_kernel(PairScanArgs a) {
         if (hist[b]) atomicAdd(&a.hist[b], (unsigned long long)hist[b]);
 }
 
+// ---------------------------------------------------------------- clusters
+// Connected components of the contact graph (r < r_contact), the clusters of
+// analysisManager::findClusters (analysisCluster.cpp:26-62), by lock-free
+// union-find over original indices: an edge hooks the larger of its two roots
+// under the smaller with atomicCAS, so each component's root ends as its
+// smallest original index -- the order findClusters visits clusters in.
+// Parents always have smaller indices, so a chain is at most n long and a
+// failed hook means the root was hooked by another thread (at most n times);
+// both loops are capped at n + 1 anyway and report EBIT_INDEX past it.
+
+__device__ int uf_find(const int* label, int x, int n, uint32_t& err) {
+    int p = ((const volatile int*)label)[x];
+    for (int k = 0; p != x; ++k) {
+        if (k > n) {
+            err |= EBIT_INDEX;
+            return x;
+        }
+        x = p;
+        p = ((const volatile int*)label)[x];
+    }
+    return x;
+}
+
+__device__ void uf_union(int* label, int a, int b, int n, uint32_t& err) {
+    for (int it = 0; it <= n; ++it) {
+        a = uf_find(label, a, n, err);
+        b = uf_find(label, b, n, err);
+        if (a == b || err) return;
+        if (a > b) {
+            const int t = a;
+            a = b;
+            b = t;
+        }
+        const int old = atomicCAS(&label[b], b, a);
+        if (old == b) return;   // hooked; else b gained a parent meanwhile: retry
+    }
+    err |= EBIT_INDEX;
+}
+
+__global__ void __launch_bounds__(256) uf_init_kernel(int n, int* label) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) label[i] = i;
+}
+
+__global__ void __launch_bounds__(128) uf_edges_kernel(PairScanArgs a, int* label,
+                                                        uint32_t* err_out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.g.n) return;
+    uint32_t err = 0;
+    const double4_32a pi = a.posd[i];
+    const int ti = a.tag[i];
+    const int c = a.cellid[i];
+    const int cx = c % a.g.s, cy = (c / a.g.s) % a.g.s, cz = c / a.g.s2;
+    for (int dx = -1; dx <= 1; ++dx)
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dz = -1; dz <= 1; ++dz) {
+                int sh;
+                const int x = wrap_cell(cx + dx, a.g.s, sh);
+                const int y = wrap_cell(cy + dy, a.g.s, sh);
+                const int z = wrap_cell(cz + dz, a.g.s, sh);
+                const int cell = x + a.g.s * y + a.g.s2 * z;
+                const int st = a.cstart[cell], en = st + a.ccount[cell];
+                for (int j = st; j < en; ++j) {
+                    const int tj = a.tag[j];
+                    if (tj <= ti) continue;   // each undirected edge once
+                    const double4_32a pj = a.posd[j];
+                    double d0 = fabs(pj.x - pi.x), d1 = fabs(pj.y - pi.y), d2 = fabs(pj.z - pi.z);
+                    if (d0 > a.g.half) d0 -= a.g.L;
+                    if (d1 > a.g.half) d1 -= a.g.L;
+                    if (d2 > a.g.half) d2 -= a.g.L;
+                    if (sqrt(d0 * d0 + d1 * d1 + d2 * d2) < a.r_contact)
+                        uf_union(label, ti, tj, a.g.n, err);
+                }
+            }
+    if (err) atomicOr(err_out, err);
+}
+
+__global__ void __launch_bounds__(256) uf_final_kernel(int n, const int* label, int* root,
+                                                        int* size, uint32_t* err_out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t err = 0;
+    const int r = uf_find(label, i, n, err);
+    root[i] = r;
+    atomicAdd(&size[r], 1);
+    if (err) atomicOr(err_out, err);
+}
+
 }  // namespace
+
+cudaError_t launch_clusters(const PairScanArgs& a, int* label, int* root, int* size,
+                            uint32_t* err, cudaStream_t st) {
+    const int n = a.g.n;
+    if (n == 0) return cudaSuccess;
+    uf_init_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, label);
+    uf_edges_kernel<<<(n + 127) / 128, 128, 0, st>>>(a, label, err);
+    uf_final_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, label, root, size, err);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_sum_squares(long long count, const double* v, double* scratch, double* out,
                                cudaStream_t st) {

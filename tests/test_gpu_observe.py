@@ -87,3 +87,27 @@ def test_interactions_and_rdf_match_all_pairs(psim, skin):
     shell = 4.0 / 3.0 * np.pi * (edges[1:] ** 3 - edges[:-1] ** 3)
     assert np.allclose(gr, hist / (n * rho * shell), rtol=1e-12)
     s.close()
+
+
+def test_clusters_match_connected_components(psim):
+    sp = pytest.importorskip("scipy.sparse")
+    csgraph = pytest.importorskip("scipy.sparse.csgraph")
+    n, box, scale = 1500, 14.0, 4   # phi ~ 0.29: many contacts closer than 1.2
+    s, g = ao_system(psim, n=n, box=box, scale=scale, precision=1, seed=72)
+    s.step(5)
+    pos = s.download()["pos"].reshape(-1, 3)
+    d = min_image(pos[:, None, :] - pos[None, :, :], box)
+    r = np.sqrt(np.sum(d * d, axis=2))
+    np.fill_diagonal(r, np.inf)
+    ncomp, lab = csgraph.connected_components(sp.csr_matrix(r < 1.2), directed=False)
+    root, groups, avg = s.clusters(1.2, 4)
+    # the same partition, each cluster named by its smallest original index
+    first = {}
+    for i in range(n):
+        first.setdefault(lab[i], i)
+    assert np.array_equal(root, np.array([first[lab[i]] for i in range(n)]))
+    big = [np.flatnonzero(lab == c) for c in range(ncomp) if np.sum(lab == c) > 4]
+    big.sort(key=lambda m: m[0])
+    assert len(groups) == len(big) and all(np.array_equal(a, b) for a, b in zip(groups, big))
+    assert avg == (sum(len(m) for m in big) // len(big) if big else 0)
+    s.close()
