@@ -42,6 +42,7 @@ template <class Pair>
 struct F64Body {
     Pair pf;
     using Aux = double4_32a;  // the FP64 neighbour positions {x, y, z, R}
+    static constexpr bool kBatchable = !std::is_same<Pair, ComboPair>::value;
     struct Home {
         double4_32a p;
     };
@@ -180,9 +181,7 @@ cudaError_t launch_forces_fp64(const ForceSetup& fs, const DevGeom& g, const Cel
 
 cudaError_t launch_vgb_system(const VgbSystemArgs& a, const VgbParams& p, const DevGeom& g,
                               const NoiseView& nz, cudaStream_t st) {
-    if (a.n == 0) return cudaSuccess;
-    vgb_system_kernel<VgbExact><<<(a.n + 255) / 256, 256, 0, st>>>(a, p, g, nz);
-    return cudaGetLastError();
+    return launch_vgb_system_t<VgbExact>(a, p, g, nz, st);
 }
 
 cudaError_t launch_vgb_aos(const VgbAosArgs& a, const VgbParams& p, double L, cudaStream_t st) {

@@ -46,39 +46,16 @@ constexpr int kQueueCap = kQueue + kUnroll;   // slots per lane
 // t < len test masks.
 constexpr int kStagePad = 2 * kStage + kUnroll;
 
+// The warp's walk: particle i of the lane (inactive lanes i >= g.p1), with
+// the warp's shared stage and queues.
 template <class Body>
-__global__ void __launch_bounds__(kForceWarps * 32)
-force_pass_kernel(Body body0, DevGeom g0, CellView cv, ForceOut out, float pre0, BatchView bv) {
+__device__ __forceinline__ void force_pass_warp(const Body& body, const DevGeom& g,
+                                                const CellView& cv, const ForceOut& out,
+                                                float pre_rc2, int i, int lane,
+                                                float4* st_hi, typename Body::Aux* st_aux,
+                                                uint32_t (*q)[32]) {
     using Aux = typename Body::Aux;
-    __shared__ float4 s_hi[kForceWarps][kStagePad];
-    __shared__ Aux s_aux[kForceWarps][kStage];
-    __shared__ uint32_t s_q[kForceWarps][kQueueCap][32];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    // an error latched by an earlier kernel (or a closed gate) stops the
-    // pass; read once and broadcast so every lane takes the same path
-    const bool failed = __shfl_sync(
-        0xffffffffu, (lane == 0) ? (*out.err != 0 || (out.gate && *out.gate == 0)) : false, 0);
-    if (failed) return;  // warp-uniform; the kernel synchronises warps only
-    // one system, or the warp's task in a batch of replicas (warp-uniform)
-    int i;
-    DevGeom g = g0;
-    Body body = body0;
-    float pre_rc2 = pre0;
-    if (bv.tasks) {
-        const int task = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-        if (task >= bv.n_tasks) return;
-        const int2 t = bv.tasks[task];
-        g = bv.geoms[t.x];
-        body = body0.for_replica(bv.pairs, t.x, g);
-        pre_rc2 = bv.pre[t.x];
-        i = t.y + lane;
-    } else {
-        i = blockIdx.x * blockDim.x + threadIdx.x;
-    }
     const bool active = i < g.p1;
-    float4* st_hi = s_hi[w];
-    Aux* st_aux = s_aux[w];
-    uint32_t (*q)[32] = s_q[w];
     const Aux* g_aux = body.aux(cv);
 
     float4 hi = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -204,20 +181,61 @@ force_pass_kernel(Body body0, DevGeom g0, CellView cv, ForceOut out, float pre0,
     if (err) atomicOr(out.err, err);
 }
 
+// An error latched by an earlier kernel (or a closed gate) stops the pass;
+// read once by lane 0 and broadcast so every lane takes the same path.
+__device__ __forceinline__ bool pass_failed(const ForceOut& out, int lane) {
+    return __shfl_sync(0xffffffffu,
+                       (lane == 0) ? (*out.err != 0 || (out.gate && *out.gate == 0)) : false, 0);
+}
+
+// One system: the geometry and body are kernel parameters.
+template <class Body>
+__global__ void __launch_bounds__(kForceWarps * 32)
+force_pass_kernel(Body body, DevGeom g, CellView cv, ForceOut out, float pre_rc2) {
+    __shared__ float4 s_hi[kForceWarps][kStagePad];
+    __shared__ typename Body::Aux s_aux[kForceWarps][kStage];
+    __shared__ uint32_t s_q[kForceWarps][kQueueCap][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (pass_failed(out, lane)) return;  // warp-uniform; warps synchronise only themselves
+    force_pass_warp(body, g, cv, out, pre_rc2, blockIdx.x * blockDim.x + threadIdx.x, lane,
+                    s_hi[w], s_aux[w], s_q[w]);
+}
+
+// A batch of replicas: each warp takes a task (replica, first particle) and
+// that replica's geometry, pair functor and prefilter bound.
+template <class Body>
+__global__ void __launch_bounds__(kForceWarps * 32)
+force_batch_kernel(Body body0, CellView cv, ForceOut out, BatchView bv) {
+    __shared__ float4 s_hi[kForceWarps][kStagePad];
+    __shared__ typename Body::Aux s_aux[kForceWarps][kStage];
+    __shared__ uint32_t s_q[kForceWarps][kQueueCap][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (pass_failed(out, lane)) return;
+    const int task = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (task >= bv.n_tasks) return;
+    const int2 t = bv.tasks[task];
+    const DevGeom g = bv.geoms[t.x];
+    const Body body = body0.for_replica(bv.pairs, t.x, g);
+    force_pass_warp(body, g, cv, out, bv.pre[t.x], t.y + lane, lane, s_hi[w], s_aux[w], s_q[w]);
+}
+
 template <class Body>
 cudaError_t launch_force_pass(const Body& body, const DevGeom& g, const CellView& cv,
                               const ForceOut& out, float pre_rc2, cudaStream_t st,
                               const BatchView* bv = nullptr) {
     const int threads = kForceWarps * 32;
     if (bv && bv->tasks) {
-        if (bv->n_tasks == 0) return cudaSuccess;
-        const int blocks = (bv->n_tasks + kForceWarps - 1) / kForceWarps;
-        force_pass_kernel<Body><<<blocks, threads, 0, st>>>(body, g, cv, out, pre_rc2, *bv);
-        return cudaGetLastError();
+        if constexpr (Body::kBatchable) {
+            if (bv->n_tasks == 0) return cudaSuccess;
+            const int blocks = (bv->n_tasks + kForceWarps - 1) / kForceWarps;
+            force_batch_kernel<Body><<<blocks, threads, 0, st>>>(body, cv, out, *bv);
+            return cudaGetLastError();
+        }
+        return cudaErrorInvalidValue;
     }
     if (g.n == 0) return cudaSuccess;
-    force_pass_kernel<Body><<<(g.n + threads - 1) / threads, threads, 0, st>>>(
-        body, g, cv, out, pre_rc2, BatchView{});
+    force_pass_kernel<Body><<<(g.n + threads - 1) / threads, threads, 0, st>>>(body, g, cv, out,
+                                                                              pre_rc2);
     return cudaGetLastError();
 }
 

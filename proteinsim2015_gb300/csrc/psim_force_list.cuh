@@ -45,6 +45,7 @@ struct ListBody {
     int ghost;         // the ghost record (n); halo records follow it
     const int* lhalo;
     using Aux = float4;
+    static constexpr bool kBatchable = false;   // pair lists are built for one system only
     struct Home {
         int i;
     };
@@ -56,9 +57,6 @@ struct ListBody {
         int n;
     };
     __device__ __forceinline__ const Aux* aux(const CellView& cv) const { return cv.posl; }
-    __device__ __forceinline__ ListBody for_replica(const void*, int, const DevGeom&) const {
-        return *this;  // pair lists are built for one system only
-    }
     __device__ __forceinline__ void init(Acc& a) const { a.n = 0; }
     __device__ __forceinline__ void load_home(const CellView&, int i, Home& h) const { h.i = i; }
     __device__ __forceinline__ void shift(const Home& h, const float4&, int sx, int sy, int sz,

@@ -51,6 +51,7 @@ struct MixedBody {
     Pair pf;
     float rc2f;
     using Aux = float4;  // the low parts of the neighbour positions
+    static constexpr bool kBatchable = !std::is_same<Pair, ComboPairF>::value;
     struct Home {
         float4 lo;
     };
@@ -229,9 +230,7 @@ cudaError_t launch_list_build(const DevGeom& g, const CellView& cv, const ListBu
 // instance, with a*b+c contracted into FMA by this translation unit.
 cudaError_t launch_vgb_system_fast(const VgbSystemArgs& a, const VgbParams& p, const DevGeom& g,
                                    const NoiseView& nz, cudaStream_t st) {
-    if (a.n == 0) return cudaSuccess;
-    vgb_system_kernel<VgbFast><<<(a.n + 255) / 256, 256, 0, st>>>(a, p, g, nz);
-    return cudaGetLastError();
+    return launch_vgb_system_t<VgbFast>(a, p, g, nz, st);
 }
 
 }  // namespace psim

@@ -276,18 +276,11 @@ __device__ __forceinline__ void list_position(const VgbSystemArgs& a, int f, con
     if (d2 > a.ldisp2) *a.lflag_set = 1;
 }
 
+// One particle of the system-order update (slot f), with its system's
+// geometry g and parameters p.
 template <class Tag>
-__global__ void __launch_bounds__(256)
-vgb_system_kernel(VgbSystemArgs a, VgbParams p, DevGeom g0, NoiseView nz) {
-    const int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= a.n || *a.err) return;
-    // one system, or this particle's replica in a batch
-    DevGeom g = g0;
-    if (a.rep) {
-        const int r = a.rep[f];
-        g = a.geoms[r];
-        p.seed = a.seeds[r];
-    }
+__device__ __forceinline__ void vgb_system_one(const VgbSystemArgs& a, const VgbParams& p,
+                                               const DevGeom& g, const NoiseView& nz, int f) {
     const long long step = a.state->step;
     const int vc = a.state->vel_counter;
     const bool first = (step == 0);
@@ -342,6 +335,35 @@ vgb_system_kernel(VgbSystemArgs a, VgbParams p, DevGeom g0, NoiseView nz) {
     a.key[f] = key;
     a.rank[f] = atomicAdd(&a.count[key], 1);
     if (err) atomicOr(a.err, err);
+}
+
+// One system (the geometry is a kernel parameter) or, with kBatch, each
+// particle's replica of a batch (its geometry and Philox seed from tables).
+template <class Tag, bool kBatch>
+__global__ void __launch_bounds__(256)
+vgb_system_kernel(VgbSystemArgs a, VgbParams p, DevGeom g0, NoiseView nz) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= a.n || *a.err) return;
+    if constexpr (kBatch) {
+        const int r = a.rep[f];
+        VgbParams pr = p;
+        pr.seed = a.seeds[r];
+        vgb_system_one<Tag>(a, pr, a.geoms[r], nz, f);
+    } else {
+        vgb_system_one<Tag>(a, p, g0, nz, f);
+    }
+}
+
+template <class Tag>
+cudaError_t launch_vgb_system_t(const VgbSystemArgs& a, const VgbParams& p, const DevGeom& g,
+                                const NoiseView& nz, cudaStream_t st) {
+    if (a.n == 0) return cudaSuccess;
+    const int blocks = (a.n + 255) / 256;
+    if (a.rep)
+        vgb_system_kernel<Tag, true><<<blocks, 256, 0, st>>>(a, p, g, nz);
+    else
+        vgb_system_kernel<Tag, false><<<blocks, 256, 0, st>>>(a, p, g, nz);
+    return cudaGetLastError();
 }
 
 // nextSystem on the reference's own AoS arrays in original order.
