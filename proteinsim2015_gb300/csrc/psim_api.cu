@@ -791,6 +791,9 @@ struct psim_system {
     int lcap = 0, hcap = 0;
     float lpre = 0.f, ldisp2 = 0.f, hr = 0.f;
     DevBuf lslot[2], lbuild, lpos, list, lcount, lflag, lhalo, lhcount;
+    // compact 16-byte records when every particle has one radius (set by the upload)
+    int lcompact = 0;
+    float lradius = 0.f, lunit = 0.f;
     // a batch of independent replicas (psim_batch_create): per-warp tasks,
     // per-replica grids, pair functors, prefilter bounds and seeds, and the
     // replica of each storage slot (fixed: the cells of a replica are
@@ -829,6 +832,7 @@ double* d3(DevBuf& b, int n, int k) { return b.as<double>() + (size_t)k * n; }
 void set_halo_args(psim_system* s, CanonArgs& ca) {
     ca.lbuild = s->lbuild.as<float4>();
     ca.lpos = s->lpos.as<float4>();
+    ca.linv_unit = s->lcompact ? 1.0f / s->lunit : 0.f;
     ca.lhalo = s->lhalo.as<int>();
     ca.lhcount = s->lhcount.as<int>();
     ca.hcap = s->hcap;
@@ -863,7 +867,7 @@ cudaError_t enqueue_force(psim_system* s, const Phase& ph, const ForceOut& fo) {
     if (s->cfg.precision == PSIM_PRECISION_FP64) return launch_forces_fp64(s->fs, s->g, cv, fo, s->st);
     if (s->list_on) {
         PairList pl{s->lslot[ph.ob].as<int>(), s->lpos.as<float4>(), s->lcount.as<int>(),
-                    s->list.as<uint32_t>(), s->n};
+                    s->list.as<uint32_t>(), s->n, s->lcompact, s->lradius, s->lunit};
         return launch_forces_list(s->fs, s->g, pl, fo, s->st);
     }
     return launch_forces_mixed(s->fs, s->g, cv, fo, s->st);
@@ -908,6 +912,7 @@ int enqueue_step(psim_system* s, long long t, cudaEvent_t* evs) {
         a.lslot = s->lslot[ob].as<int>();
         a.lbuild = s->lbuild.as<float4>();
         a.lpos = s->lpos.as<float4>();
+        a.linv_unit = s->lcompact ? 1.0f / s->lunit : 0.f;
         a.lflag_set = lflag;
         a.lflag_clear = s->lflag.as<int>() + (1 - (t & 1));
         a.ldisp2 = s->ldisp2;
@@ -1226,10 +1231,6 @@ psim_system* system_new(const psim_system_config* cfg, const DevGeom& g) {
              !s->lflag.ensure(8) && !s->lhalo.ensure(4 * n) && !s->lhcount.ensure(4) &&
              cudaMemset(s->lflag.p, 0, 8) == cudaSuccess &&
              cudaMemset(s->lhcount.p, 0, 4) == cudaSuccess;
-        // the ghost slot n that pads the lists: far from every particle
-        const float4 ghost[2] = {make_float4(1e18f, 1e18f, 1e18f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f)};
-        ok = ok && cudaMemcpy(s->lpos.as<float4>() + 2 * n, ghost, 32, cudaMemcpyHostToDevice) ==
-                       cudaSuccess;
     }
     if (ok) ok = cudaMemset(s->err.p, 0, 4) == cudaSuccess &&
                  cudaMemset(s->state.p, 0, sizeof(StepState)) == cudaSuccess;
@@ -1345,6 +1346,24 @@ int psim_system_upload(psim_system* s, const double* pos, const double* pos0, co
     ca.posd = s->cfg.precision == PSIM_PRECISION_FP64 ? s->posd.as<double4_32a>() : nullptr;
     ca.posh = s->posh.as<float4>();
     ca.posl = s->cfg.precision == PSIM_PRECISION_MIXED ? s->posl.as<float4>() : nullptr;
+    if (s->list_on) {
+        // compact records when all radii are equal; the ghost record n that
+        // pads the lists lies far from every particle (zero low parts)
+        int compact = n > 0 ? 1 : 0;
+        for (int i = 1; i < n && compact; ++i) compact = radius[i] == radius[0];
+        const float R = n > 0 ? (float)radius[0] : 0.f;
+        if (compact != s->lcompact || R != s->lradius) drop_graphs(s);
+        s->lcompact = compact;
+        s->lradius = R;
+        // low-part unit: |lo| of a record stays below the last place of its
+        // high part, or ~2x that after a halo shift; M bounds every coordinate
+        const double M = s->g.L + 2.0 * (max_cutoff(&s->cfg.force) + s->skin) + 1.0;
+        s->lunit = (float)std::ldexp(1.0, std::ilogb(M) - 31);
+        const float4 ghost[2] = {make_float4(1e18f, 1e18f, 1e18f, compact ? 0.f : R),
+                                 make_float4(0.f, 0.f, 0.f, 0.f)};
+        float4* grec = s->lpos.as<float4>() + (compact ? 1 : 2) * (size_t)n;
+        PSIM_CUDA(cudaMemcpyAsync(grec, ghost, compact ? 16 : 32, cudaMemcpyHostToDevice, st));
+    }
     if (s->list_on) {
         // the first list, on the first cell order: flag 0 raised for the
         // build, lowered for step 0 (whose integrator raises it when needed)

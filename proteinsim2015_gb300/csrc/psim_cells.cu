@@ -160,9 +160,8 @@ __global__ void __launch_bounds__(256) canonicalize_kernel(CanonArgs a, int vel_
             if (a.posl) a.posl[g] = l;
             if (a.lbuild) a.lbuild[g] = h;
             if (a.lpos) {
-                a.lpos[2 * (size_t)g] = h;
-                a.lpos[2 * (size_t)g + 1] = l;
                 l.w = 0.f;
+                store_record(a.lpos, a.linv_unit, (size_t)g, h, l);
                 // images of a particle near a face, as halo records
                 uint32_t fl = halo_flags(h, a.hr, a.Lf);
                 const int m = halo_copies(fl);
@@ -174,7 +173,8 @@ __global__ void __launch_bounds__(256) canonicalize_kernel(CanonArgs a, int vel_
                         fl = 0;
                         base = 0;
                     } else {
-                        halo_write(a.lpos + 2 * ((size_t)a.n + 1), base, fl, h, l, a.Lhi, a.Llo);
+                        halo_write(a.lpos + (a.linv_unit != 0.f ? 1 : 2) * ((size_t)a.n + 1),
+                                   a.linv_unit, base, fl, h, l, a.Lhi, a.Llo);
                     }
                 }
                 a.lhalo[g] = (base << 6) | (int)fl;

@@ -150,18 +150,52 @@ __device__ __forceinline__ void halo_shift(uint32_t flags, int num, int sh[3]) {
         }
     }
 }
-// Writes the images of a particle at list slot s (positions h, l) into its
-// halo records pos[2 (base + num - 1)], base = the particle's first halo slot.
-__device__ __forceinline__ void halo_write(float4* pos, int base, uint32_t flags, const float4& h,
-                                           const float4& l, float Lhi, float Llo) {
+// ------------------------------------------------- pair-list position records
+// A full record is 32 bytes: {x, y, z, R} high parts and the low parts.  When
+// every particle has the same radius a compact 16-byte record suffices: the
+// high parts and, in .w, each low part as a 10-bit code in units of lo_unit
+// (code - 512) * lo_unit, lo_unit = U / 1024 with U twice the last place of
+// the largest coordinate a record can hold, so |lo| < U / 2 always.  The
+// code is exact to lo_unit / 2 -- ~7e-9 for a 109-wide box -- an absolute
+// error far under the FP32 rounding of a pair separation.
+__device__ __forceinline__ uint32_t lo_code(float lo, float inv_unit) {
+    const int q = __float2int_rn(lo * inv_unit) + 512;
+    return (uint32_t)(q < 0 ? 0 : (q > 1023 ? 1023 : q));
+}
+__device__ __forceinline__ float4 compact_record(const float4& h, const float4& l,
+                                                 float inv_unit) {
+    const uint32_t w = lo_code(l.x, inv_unit) | (lo_code(l.y, inv_unit) << 10) |
+                       (lo_code(l.z, inv_unit) << 20);
+    return make_float4(h.x, h.y, h.z, __uint_as_float(w));
+}
+// 2^23 + code as a float, so that fma(magic, unit, -(2^23 + 512) unit) is the
+// low part exactly
+__device__ __forceinline__ float lo_magic(uint32_t code) {
+    return __uint_as_float(0x4B000000u | code);
+}
+// record `slot` of a full (inv_unit == 0) or compact record array
+__device__ __forceinline__ void store_record(float4* pos, float inv_unit, size_t slot,
+                                             const float4& h, const float4& l) {
+    if (inv_unit != 0.f) {
+        pos[slot] = compact_record(h, l, inv_unit);
+    } else {
+        pos[2 * slot] = h;
+        pos[2 * slot + 1] = l;
+    }
+}
+
+// Writes the images of a particle (positions h, l) into its halo records
+// base + num - 1 of `pos` (the records after the ghost).
+__device__ __forceinline__ void halo_write(float4* pos, float inv_unit, int base, uint32_t flags,
+                                           const float4& h, const float4& l, float Lhi,
+                                           float Llo) {
     const int m = halo_copies(flags);
     for (int num = 1; num <= m; ++num) {
         int sh[3];
         halo_shift(flags, num, sh);
         float4 hh = h, ll = l;
         image_shift(hh, ll, sh[0], sh[1], sh[2], Lhi, Llo);
-        pos[2 * (size_t)(base + num - 1)] = hh;
-        pos[2 * (size_t)(base + num - 1) + 1] = ll;
+        store_record(pos, inv_unit, (size_t)(base + num - 1), hh, ll);
     }
 }
 

@@ -121,7 +121,7 @@ __device__ __forceinline__ void load_record(const float4* pos, uint32_t j, float
 // whole batches, so each batch's loads are issued together before any of its
 // pair terms, and every record holds the image the pair needs: no periodic
 // arithmetic per pair.
-template <class Body>
+template <class Body, bool kCompact>
 __global__ void __launch_bounds__(128)
 force_list_kernel(Body body, DevGeom g, PairList pl, ForceOut out) {
     constexpr int kBatch = 8;
@@ -129,13 +129,30 @@ force_list_kernel(Body body, DevGeom g, PairList pl, ForceOut out) {
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= g.n || *out.err) return;
     const int s = pl.lslot[f];
-    const float4 hh = pl.pos[2 * (size_t)s];
-    // the body reads the home's low part as cv.posl[i]: point it at the
-    // records' second halves, indexed in float4 units
+    float4 hh, hl;
+    // compact records: a neighbour's low part minus the home's comes out of one
+    // FMA per axis, fma(2^23 + code, unit, c) with c = -(2^23 + 512) unit - l_i,
+    // so the body sees the home's low part as 0
+    float cx = 0.f, cy = 0.f, cz = 0.f;
+    const float unit = pl.lo_unit;
+    if (kCompact) {
+        const float4 c = pl.pos[s];
+        const uint32_t w = __float_as_uint(c.w);
+        const float nb = -8389120.0f * unit;   // -(2^23 + 512) unit, exact
+        cx = nb - fmaf(lo_magic(w & 1023u), unit, nb);
+        cy = nb - fmaf(lo_magic((w >> 10) & 1023u), unit, nb);
+        cz = nb - fmaf(lo_magic((w >> 20) & 1023u), unit, nb);
+        hh = make_float4(c.x, c.y, c.z, pl.radius);
+        hl = make_float4(0.f, 0.f, 0.f, 0.f);
+    } else {
+        hh = pl.pos[2 * (size_t)s];
+        hl = pl.pos[2 * (size_t)s + 1];
+    }
+    // the body reads the home's low part as cv.posl[i]
     CellView cv{};
-    cv.posl = pl.pos + 1;
+    cv.posl = &hl;
     typename Body::Home home;
-    body.load_home(cv, 2 * s, home);
+    body.load_home(cv, 0, home);
     typename Body::Shifted hs;
     body.shift(home, hh, 0, 0, 0, g, hs);
     typename Body::Acc acc;
@@ -150,8 +167,22 @@ force_list_kernel(Body body, DevGeom g, PairList pl, ForceOut out) {
             float4 nh[kBatch], nl[kBatch];
 #pragma unroll
             for (int u = 0; u < kBatch; ++u) e[u] = __ldg(lp + (size_t)(k0 + b + u) * pl.stride);
+            if (kCompact) {
+                float4 c[kBatch];   // 16-byte records: all loads first
 #pragma unroll
-            for (int u = 0; u < kBatch; ++u) load_record(pl.pos, e[u], nh[u], nl[u]);
+                for (int u = 0; u < kBatch; ++u) c[u] = __ldg(pl.pos + e[u]);
+#pragma unroll
+                for (int u = 0; u < kBatch; ++u) {
+                    const uint32_t w = __float_as_uint(c[u].w);
+                    nh[u] = make_float4(c[u].x, c[u].y, c[u].z, pl.radius);
+                    nl[u] = make_float4(fmaf(lo_magic(w & 1023u), unit, cx),
+                                        fmaf(lo_magic((w >> 10) & 1023u), unit, cy),
+                                        fmaf(lo_magic((w >> 20) & 1023u), unit, cz), 0.f);
+                }
+            } else {
+#pragma unroll
+                for (int u = 0; u < kBatch; ++u) load_record(pl.pos, e[u], nh[u], nl[u]);
+            }
 #pragma unroll
             for (int u = 0; u < kBatch; ++u) body.eval_masked(nh[u], nl[u], hs, acc, err);
         }
@@ -165,7 +196,10 @@ template <class Body>
 cudaError_t launch_force_list(const Body& body, const DevGeom& g, const PairList& pl,
                               const ForceOut& out, cudaStream_t st) {
     if (g.n == 0) return cudaSuccess;
-    force_list_kernel<Body><<<(g.n + 127) / 128, 128, 0, st>>>(body, g, pl, out);
+    if (pl.compact)
+        force_list_kernel<Body, true><<<(g.n + 127) / 128, 128, 0, st>>>(body, g, pl, out);
+    else
+        force_list_kernel<Body, false><<<(g.n + 127) / 128, 128, 0, st>>>(body, g, pl, out);
     return cudaGetLastError();
 }
 

@@ -69,12 +69,17 @@ constexpr int kListFold = 8;   // pair terms per Kahan fold
 constexpr int kHaloBaseMax = (1 << 25) - 1;   // halo records per system
 struct PairList {
     const int* lslot;      // list slot of each current storage slot
-    // list order, unwrapped, one 32-byte record per slot (+ the ghost slot n):
-    // pos[2 s] = {x, y, z, R} high parts, pos[2 s + 1] = low parts
+    // list order, unwrapped, one record per slot (+ the ghost slot n and the
+    // halo records): full, pos[2 s] = {x, y, z, R} high parts and pos[2 s + 1]
+    // the low parts; or compact (one float4, compact_record, low parts in
+    // units of lo_unit) when every particle has the radius `radius`
     const float4* pos;
     const int* count;      // entries of each list slot (a multiple of kListFold)
     const uint32_t* list;
     int stride;
+    int compact;
+    float radius;
+    float lo_unit;
 };
 cudaError_t launch_forces_list(const ForceSetup& fs, const DevGeom& g, const PairList& pl,
                                const ForceOut& out, cudaStream_t st);
@@ -150,6 +155,7 @@ struct VgbSystemArgs {
     const int* lslot;
     const float4* lbuild;       // list order: positions at the build, .w radius
     float4* lpos;               // PairList::pos
+    float linv_unit;            // 1 / PairList::lo_unit (compact), or 0 (full records)
     int* lflag_set;
     int* lflag_clear;
     float ldisp2;
@@ -238,6 +244,7 @@ struct CanonArgs {
     int* lslot_out;
     float4* lbuild;
     float4* lpos;           // PairList::pos, written with posh/posl
+    float linv_unit;        // 1 / PairList::lo_unit (compact), or 0 (full records)
     // halo records of the particles within hr of a face (rebuild only):
     // lhalo per slot, records n + 1 + [0, hcap) handed out by *lhcount
     int* lhalo;

@@ -267,12 +267,11 @@ __device__ __forceinline__ void list_position(const VgbSystemArgs& a, int f, con
         d2 += e * e;
     }
     const float4 hv = make_float4(h[0], h[1], h[2], b.w), lv = make_float4(l[0], l[1], l[2], 0.f);
-    a.lpos[2 * (size_t)s] = hv;
-    a.lpos[2 * (size_t)s + 1] = lv;
+    store_record(a.lpos, a.linv_unit, (size_t)s, hv, lv);
     const int hal = a.lhalo[s];
     if (hal & 63)  // the particle's periodic images in the halo records
-        halo_write(a.lpos + 2 * ((size_t)a.n + 1), hal >> 6, (uint32_t)(hal & 63), hv, lv, g.Lhi,
-                   g.Llo);
+        halo_write(a.lpos + (a.linv_unit != 0.f ? 1 : 2) * ((size_t)a.n + 1), a.linv_unit,
+                   hal >> 6, (uint32_t)(hal & 63), hv, lv, g.Lhi, g.Llo);
     if (d2 > a.ldisp2) *a.lflag_set = 1;
 }
 
@@ -340,7 +339,7 @@ __device__ __forceinline__ void vgb_system_one(const VgbSystemArgs& a, const Vgb
 // One system (the geometry is a kernel parameter) or, with kBatch, each
 // particle's replica of a batch (its geometry and Philox seed from tables).
 template <class Tag, bool kBatch>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 4)
 vgb_system_kernel(VgbSystemArgs a, VgbParams p, DevGeom g0, NoiseView nz) {
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= a.n || *a.err) return;

@@ -147,3 +147,23 @@ def test_system_forces_match_dropin_fp64(psim, skin, precision):
     ref = psim.force_evaluate(p, g, srt, hi, cse, precision=psim.PRECISION_FP64)
     s.close()
     assert rel_norm(f, ref) < (1e-12 if precision == 0 else 1e-5)
+
+
+def test_pairlist_with_unequal_radii(psim):
+    # two radii: the list keeps full 32-byte records (uniform radii use the
+    # compact 16-byte ones, which every test above runs)
+    g, p, pos, rad = lj_liquid(psim)
+    rad = rad.copy()
+    rad[::3] = 0.45
+    n = g.n_particles
+    rng = np.random.default_rng(47)
+    vel = rng.standard_normal(3 * n) * np.sqrt(KT)
+    steps = 40
+    noise = rng.standard_normal(steps * n * 6)
+    ref = run(psim, g, p, pos, rad, vel, noise, steps, 0.0)
+    got = run(psim, g, p, pos, rad, vel, noise, steps, 0.4)
+    assert got["builds"] >= 1
+    assert rel_norm(got["frc"], ref["frc"]) < 1e-5
+    d = got["pos"] - ref["pos"]
+    d -= g.box_size * np.round(d / g.box_size)
+    assert np.max(np.abs(d)) < 1e-6
