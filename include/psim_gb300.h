@@ -235,6 +235,52 @@ typedef struct {
 int psim_init_rsa(int32_t n, double box, double min_sep, uint64_t seed, int64_t max_trials,
                   double* pos);
 
+/* ------------------------------------------- differentiable trajectory */
+
+/* Gradients of a trajectory loss with the noise held fixed (no reference
+ * counterpart: the reference has no derivatives).  The trajectory is the vGB
+ * positions update of the plain FP64 form (brownianIntegrator.cpp:191-296:
+ * firstStep, then normal steps, Philox noise keyed by particle and step as
+ * the system's, uniform mass) under the AO plugin plus the Yukawa term of the
+ * LennardJones plugin with ljNum = 0; the loss is the squared distance
+ * between the trajectory's time-averaged, Gaussian-smoothed g(r) (samples
+ * every sample_every steps; n_bins bins of [r_min, r_max), kernel width
+ * sigma) and a target.  The reverse pass recomputes checkpoint_every-step
+ * segments from checkpoints of the forward pass. */
+typedef struct psim_adjoint psim_adjoint;
+
+typedef struct {
+    psim_geometry geom;             /* cellSize >= every cutoff and r_max + 4 sigma */
+    psim_integrator_config integ;   /* gamma, dt, kT, seed (velFreq unused) */
+    double mass;
+    int32_t n_steps, checkpoint_every, sample_every;
+    double r_min, r_max;
+    int32_t n_bins;
+    double sigma;
+} psim_adjoint_config;
+
+typedef struct {
+    double kT;
+    double ao_well_depth, ao_cutoff;   /* AOPotential wellDepth, cutOff (0: no AO term) */
+    double yuk_amplitude;              /* kT wellDepth yukawaStrength of the LJ plugin */
+    double yuk_length;                 /* debyeLength */
+    double yuk_cutoff;                 /* its cutOff (0: no Yukawa term) */
+} psim_adjoint_params;
+
+psim_adjoint* psim_adjoint_create(const psim_adjoint_config* cfg, int32_t device);
+void psim_adjoint_destroy(psim_adjoint* adj);
+/* The trajectory from pos0/vel0 (3n, original order; vel0 may be NULL):
+ * g_mean (n_bins) and, if not NULL, the final positions (3n, unwrapped). */
+int psim_adjoint_forward(psim_adjoint* adj, const psim_adjoint_params* p, const double* pos0,
+                         const double* vel0, double* g_mean, double* pos_final);
+/* Loss against g_target, its g_mean (may be NULL), and the gradient
+ * grad[4] = dL/d(ao_well_depth, ao_cutoff, yuk_amplitude, yuk_length) -- the
+ * AO cutoff through the AO coefficients only, its cutoff held fixed -- and,
+ * if not NULL, dL/d(pos0) (3n). */
+int psim_adjoint_gradient(psim_adjoint* adj, const psim_adjoint_params* p, const double* pos0,
+                          const double* vel0, const double* g_target, double* loss,
+                          double* g_mean, double* grad, double* grad_pos0);
+
 /* ---------------------------------------------- batches of replicas */
 
 /* One replica of a batch: its own box and cell grid, plugin parameters and

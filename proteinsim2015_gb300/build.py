@@ -29,6 +29,7 @@ SOURCES = {
     "psim_noalloc.cu": [],
     "psim_init.cu": [],
     "psim_observe.cu": [],
+    "psim_adjoint.cu": ["--fmad=false"],
 }
 
 
