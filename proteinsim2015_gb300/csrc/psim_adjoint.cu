@@ -47,12 +47,13 @@ namespace {
 struct AdjPair {
     double c1, c2, ao_rc2;   // ao_rc2 = 0: no AO term
     double Y, lam, y_rc2;    // y_rc2 = 0: no Yukawa term
+    double inv_lam;          // 1 / lam
 };
 
 // s(r) = F_pair / r (force on i along x_j - x_i), ds/dr and ds/dth
 __device__ __forceinline__ void pair_terms(const AdjPair& q, double r2, double& s, double& ds,
                                            double dth[4]) {
-    const double r = sqrt(r2), ri = 1.0 / r;
+    const double ri = rsqrt(r2), r = r2 * ri;
     s = 0.0;
     ds = 0.0;
     dth[0] = dth[1] = dth[2] = dth[3] = 0.0;
@@ -66,12 +67,12 @@ __device__ __forceinline__ void pair_terms(const AdjPair& q, double r2, double& 
         dth[1] = -1.0;
     }
     if (r2 < q.y_rc2) {
-        const double e = exp(-r / q.lam);
+        const double e = exp(-r * q.inv_lam);
         const double lr = q.lam + r;
         s += -q.Y * e * lr * ri3;
-        ds += q.Y * e * ri3 * (r / q.lam + 3.0 * lr * ri);
+        ds += q.Y * e * ri3 * (r * q.inv_lam + 3.0 * lr * ri);
         dth[2] = -e * lr * ri3;
-        dth[3] = -q.Y * e * ri3 * (r * lr / (q.lam * q.lam) + 1.0);
+        dth[3] = -q.Y * e * ri3 * (r * lr * q.inv_lam * q.inv_lam + 1.0);
     }
 }
 
@@ -97,14 +98,19 @@ __global__ void __launch_bounds__(256) adj_hash_kernel(int n, const double* x, A
     rank[i] = atomicAdd(&count[k], 1);
 }
 
+// sorted positions, wrapped into the box: FP64 and an FP32 copy for the
+// candidate test
 __global__ void __launch_bounds__(256) adj_place_kernel(int n, const double* x, const int* key,
                                                         const int* rank, const int* start,
-                                                        int* order, double4_32a* sp, double L) {
+                                                        int* order, double4_32a* sp, float4* spf,
+                                                        double L) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int p = start[key[i]] + rank[i];
     order[p] = i;
-    sp[p] = make_double4_32a(x[i], x[n + i], x[2 * n + i], 0.0);
+    const double a = wrap_box(x[i], L), b = wrap_box(x[n + i], L), c = wrap_box(x[2 * n + i], L);
+    sp[p] = make_double4_32a(a, b, c, 0.0);
+    spf[p] = make_float4((float)a, (float)b, (float)c, 0.f);
 }
 
 struct AdjWalk {
@@ -112,19 +118,31 @@ struct AdjWalk {
     AdjPair q;
     int n;
     const int* order;
-    const double4_32a* sp;   // sorted positions (unwrapped)
+    const double4_32a* sp;   // sorted positions, wrapped
+    const float4* spf;       // the same in FP32
     const int* start;
     const int* count;
     const int* key;
 };
 
-// every neighbour j of sorted slot p within the largest cutoff: fn(j, d, r2)
+// minimum image of a difference of two wrapped coordinates
+template <class T>
+__device__ __forceinline__ T min_image(T d, T L, T half) {
+    return d > half ? d - L : (d < -half ? d + L : d);
+}
+
+// every neighbour j of sorted slot p within the largest cutoff: fn(j, d, r2).
+// Candidates are tested in FP32 with a margin first; FP64 decides.
 template <class Fn>
 __device__ __forceinline__ void for_pairs(const AdjWalk& w, int p, const double4_32a& pi,
                                           double rc2, Fn&& fn) {
     const int c = w.key[w.order[p]];
     const int cx = c % w.g.s, cy = (c / w.g.s) % w.g.s, cz = c / w.g.s2;
-    const double L = w.g.L;
+    const double L = w.g.L, half = 0.5 * L;
+    const float Lf = (float)L, hf = 0.5f * Lf;
+    const float4 pf = w.spf[p];
+    const float rcf = (float)sqrt(rc2) + 1e-3f + 4e-6f * Lf;
+    const float pre = rcf * rcf;
     for (int dx = -1; dx <= 1; ++dx)
         for (int dy = -1; dy <= 1; ++dy)
             for (int dz = -1; dz <= 1; ++dz) {
@@ -134,9 +152,13 @@ __device__ __forceinline__ void for_pairs(const AdjWalk& w, int p, const double4
                 const int st = w.start[cell], en = st + w.count[cell];
                 for (int q = st; q < en; ++q) {
                     if (q == p) continue;
+                    const float4 qf = w.spf[q];
+                    const float ex = min_image(qf.x - pf.x, Lf, hf), ey = min_image(qf.y - pf.y, Lf, hf),
+                                ez = min_image(qf.z - pf.z, Lf, hf);
+                    if (ex * ex + ey * ey + ez * ez >= pre) continue;
                     const double4_32a pj = w.sp[q];
-                    double d[3] = {pj.x - pi.x, pj.y - pi.y, pj.z - pi.z};
-                    for (int k = 0; k < 3; ++k) d[k] -= L * rint(d[k] / L);   // minimum image
+                    const double d[3] = {min_image(pj.x - pi.x, L, half), min_image(pj.y - pi.y, L, half),
+                                         min_image(pj.z - pi.z, L, half)};
                     const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
                     if (r2 < rc2) fn(q, d, r2);
                 }
@@ -165,18 +187,35 @@ struct AdjHist {
 
 __device__ __forceinline__ double gauss(double z, double norm) { return norm * exp(-0.5 * z * z); }
 
+// The kernel values G_b = norm exp(-z_b^2 / 2) of distance r at the bins
+// b_lo..b_hi, z_b = (r - r_b) / sigma, by the recurrence of consecutive bins
+// (z_{b+1} = z_b - dz): G_{b+1} = G_b q_b, q_{b+1} = q_b e^{-dz^2},
+// q_b = e^{dz z_b - dz^2 / 2} -- two exponentials per distance.  fn(b, z, G).
+template <class Fn>
+__device__ __forceinline__ void gauss_bins(const AdjHist& h, double r, Fn&& fn) {
+    const int b0 = (int)floor((r - h.r_min) / h.dr);
+    const int lo = max(0, b0 - h.reach), hi = min(h.n_bins - 1, b0 + h.reach);
+    if (lo > hi) return;
+    const double dz = h.dr * h.inv_sig;
+    double z = (r - (h.r_min + (lo + 0.5) * h.dr)) * h.inv_sig;
+    double G = gauss(z, h.norm);
+    double q = exp(dz * z - 0.5 * dz * dz);
+    const double qq = exp(-dz * dz);
+    for (int b = lo; b <= hi; ++b) {
+        fn(b, z, G);
+        G *= q;
+        q *= qq;
+        z -= dz;
+    }
+}
+
 __global__ void __launch_bounds__(128) adj_hist_kernel(AdjWalk w, double rc2, AdjHist h,
                                                        double* hist) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= w.n) return;
     const double4_32a pi = w.sp[p];
     for_pairs(w, p, pi, rc2, [&](int, const double*, double r2) {
-        const double r = sqrt(r2);
-        const int b0 = (int)floor((r - h.r_min) / h.dr);
-        for (int b = max(0, b0 - h.reach); b <= min(h.n_bins - 1, b0 + h.reach); ++b) {
-            const double rb = h.r_min + (b + 0.5) * h.dr;
-            atomicAdd(&hist[b], h.dr * gauss((r - rb) * h.inv_sig, h.norm));
-        }
+        gauss_bins(h, sqrt(r2), [&](int b, double, double G) { atomicAdd(&hist[b], h.dr * G); });
     });
 }
 
@@ -216,12 +255,10 @@ __global__ void __launch_bounds__(128) adj_reverse_kernel(AdjWalk w, double rc2,
             for (int k = 0; k < 4; ++k) th[k] += dth[k] * dui;
             if (a.wgt) {
                 // d/dx_i of the smoothed counts of pairs (i, j) and (j, i)
-                const int b0 = (int)floor((r - a.h.r_min) / a.h.dr);
                 double wr = 0.0;
-                for (int b = max(0, b0 - a.h.reach); b <= min(a.h.n_bins - 1, b0 + a.h.reach); ++b) {
-                    const double z = (r - (a.h.r_min + (b + 0.5) * a.h.dr)) * a.h.inv_sig;
-                    wr += a.wgt[b] * a.h.dr * gauss(z, a.h.norm) * (-z * a.h.inv_sig);
-                }
+                gauss_bins(a.h, r, [&](int b, double z, double G) {
+                    wr += a.wgt[b] * a.h.dr * G * (-z * a.h.inv_sig);
+                });
                 for (int k = 0; k < 3; ++k) gl[k] += 2.0 * wr * (-d[k] / r);
             }
         });
@@ -344,7 +381,7 @@ struct psim_adjoint {
     AdjHist hist{};
     double rc2 = 0.0, walk_rc2 = 0.0;
     int blocks128 = 0;
-    Buf key, rank, count, start, scan, order, sp, F[3], mem, v0, traj, ck, lam[3], u[2], part, acc,
+    Buf key, rank, count, start, scan, order, sp, spf, F[3], mem, v0, traj, ck, lam[3], u[2], part, acc,
         hsum, wgt, x0;
 };
 
@@ -360,11 +397,13 @@ int build_walk(psim_adjoint* a, const double* x, AdjWalk& w) {
                          a->st));
     adj_place_kernel<<<(n + 255) / 256, 256, 0, a->st>>>(n, x, a->key.as<int>(), a->rank.as<int>(),
                                                          a->start.as<int>(), a->order.as<int>(),
-                                                         a->sp.as<double4_32a>(), a->grid.L);
+                                                         a->sp.as<double4_32a>(),
+                                                         a->spf.as<float4>(), a->grid.L);
     w.g = a->grid;
     w.n = n;
     w.order = a->order.as<int>();
     w.sp = a->sp.as<double4_32a>();
+    w.spf = a->spf.as<float4>();
     w.start = a->start.as<int>();
     w.count = a->count.as<int>();
     w.key = a->key.as<int>();
@@ -434,6 +473,7 @@ void set_pair(const psim_adjoint_params* p, AdjPair& q, double dwd[2], double dr
     if (p->yuk_cutoff > 0.0) {
         q.Y = p->yuk_amplitude;
         q.lam = p->yuk_length;
+        q.inv_lam = 1.0 / p->yuk_length;
         q.y_rc2 = p->yuk_cutoff * p->yuk_cutoff;
     }
 }
@@ -548,6 +588,7 @@ psim_adjoint* psim_adjoint_create(const psim_adjoint_config* cfg, int32_t device
               !a->count.ensure(4 * nc) && !a->start.ensure(4 * nc) &&
               !a->scan.ensure(4 * (size_t)scan_scratch_ints((int)nc)) &&
               !a->order.ensure(4 * (size_t)n) && !a->sp.ensure(32 * (size_t)n) &&
+              !a->spf.ensure(16 * (size_t)n) &&
               !a->F[0].ensure(b3) && !a->F[1].ensure(b3) && !a->F[2].ensure(b3) &&
               !a->mem.ensure(b3 * (size_t)(nck + 1)) && !a->v0.ensure(b3) &&
               !a->traj.ensure(b3 * (size_t)(a->K + 2)) && !a->ck.ensure(3 * b3 * (size_t)nck) &&
