@@ -4,8 +4,9 @@ Workload (the single large system): N = 2^20 particles at number density
 0.8 in a cubic periodic box (an FCC lattice of 64^3 cells, a = (4/0.8)^(1/3),
 L = 109.438), LennardJones plugin with ljNum 6, yukawaStrength 0 and
 kT * wellDepth = epsilon = 1 at kT = 1.5, cutOff 2.5, Maxwell-Boltzmann
-velocities at kT = 1.5, gamma = 1, dt = 0.002, cell grid 43^3.  One step =
-forces -> push -> nextSystem -> cell-list rebuild (system.cpp:187-206).
+velocities at kT = 1.5, gamma = 1, dt = 0.002, cell grid 37^3 (the finest
+with cellSize >= cutOff + the pair-list skin 0.4).  One step = forces -> push
+-> nextSystem -> cell-list rebuild (system.cpp:187-206).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -16,7 +17,11 @@ force error against FP64 on that state; `e2e` runs the reference-layout
 drop-ins (cells_build -> force_evaluate -> nextSystem) on host buffers in
 pinned memory, every copy inside the timed region.  `--impl reference` times
 the CPU implementation of the path (oracle/_ref when present, else the
-oracle's restatement) on the host cores.
+oracle's restatement) on the host cores.  Sub-objects of the line report the
+other workloads on the same GPU: `batched` (512 AO replicas in one set of
+launches), `differentiable` (the adjoint of a 2,000-step AO + Yukawa
+trajectory, N = 32768) and `gel` (2^23 aggregating AO colloids, with the
+cell occupancy over time).
 """
 import argparse
 import json
@@ -198,6 +203,9 @@ def cpu_baseline_child(budget_s):
         out = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": "N=%d, %d whole steps (%.1f s) of the same workload" % (
                    w["n"], steps, secs)}
+        v1, steps1, secs1 = cpu_port_rate(w, budget_s / 3.0, 1)
+        out["one_thread"] = {"value": v1, "unit": UNIT, "cores": 1,
+                             "sample": "N=%d, %d whole steps (%.1f s)" % (w["n"], steps1, secs1)}
     except Exception as e:
         out = {"value": None, "unit": UNIT, "cores": cores, "kind": "port", "error": str(e)}
     print(json.dumps(out))
@@ -352,6 +360,46 @@ def run_differentiable(psim, dev, steps=2000):
             "note": "q through the AO coefficients; the cutoff 1 + q is held fixed"}
 
 
+def run_gel(psim, dev, steps=1000, skin=0.3, chunk=100):
+    """The gel stress workload: N = 2^23 AO colloids at phi = 0.30 (q = 0.08,
+    6 kT contact attraction, cutoff 1.08), seeded RSA start, gamma = 1,
+    dt = 1e-3, mixed form with a pair list; the cell list is rebuilt every
+    step.  Reports the maximum and mean particles per cell every `chunk`
+    steps while the colloids aggregate, and the clusters at the end."""
+    from proteinsim2015_gb300 import init, batch
+    n, phi = 1 << 23, 0.30
+    box = (n * math.pi / 6.0 / phi) ** (1.0 / 3.0)
+    f = batch.ao_params(psim, 6.0, 0.08)
+    scale = int(math.floor(box / (f.cutoff + skin)))
+    g = psim.geometry(n, box, box / scale, scale)
+    t0 = time.time()
+    pos = init.rsa_native(n, box, 1.0, seed=2023).reshape(-1)
+    t_init = time.time() - t0
+    vel = init.maxwell(n, 1.0, seed=5).reshape(-1)
+    s = psim.System(g, f, gamma=1.0, dt=0.001, kT=1.0, vel_freq=1000, seed=11,
+                    precision=psim.PRECISION_MIXED, device=dev, skin=skin)
+    s.upload(pos, np.full(n, 0.5), vel=vel)
+    s.step(3)
+    occ, ms = [s.cell_occupancy()], 0.0
+    for _ in range(max(1, steps // chunk)):
+        ms += s.time_steps(chunk)
+        occ.append(s.cell_occupancy())
+    done = max(1, steps // chunk) * chunk
+    prof = s.profile(5)
+    _, groups, avg = s.clusters(1.2, 4)
+    out = {"workload": "c4_gel_ao_phi0.30_N2^23", "n_particles": n, "box": box,
+           "cell_scale": scale, "skin": skin, "steps": done,
+           "value": n * done / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms / done,
+           "phases_ms": {k: round(v, 5) for k, v in prof.items()},
+           "list_builds": s.list_builds(),
+           "occupancy_max": [m for m, _ in occ], "occupancy_mean": occ[0][1],
+           "occupancy_every_steps": chunk, "rsa_seconds": round(t_init, 2),
+           "clusters_gt4": len(groups), "mean_cluster_size": avg,
+           "temperature": s.temperature()}
+    s.close()
+    return out
+
+
 def run_gpu(args):
     import proteinsim2015_gb300 as psim
     ws, rank, local = dist_env()
@@ -432,6 +480,7 @@ def run_gpu(args):
         batched = run_batched(psim, dev, args.batched_steps)
         batched["vs_single_system"] = batched["value"] / value
     differentiable = run_differentiable(psim, dev) if args.batched_steps > 0 and ws == 1 else None
+    gel = run_gel(psim, dev, args.gel_steps) if args.gel_steps > 0 and ws == 1 else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps, "higher_is_better": True,
@@ -465,6 +514,7 @@ def run_gpu(args):
         "cpu_baseline": cpu,
         "batched": batched,
         "differentiable": differentiable,
+        "gel": gel,
         "clocks": clk.summary(),
     }
     print(json.dumps(line))
@@ -484,6 +534,8 @@ def main():
                     help=argparse.SUPPRESS)
     ap.add_argument("--batched-steps", type=int, default=2000,
                     help="steps of the batched-replica run (0: skip it)")
+    ap.add_argument("--gel-steps", type=int, default=1000,
+                    help="steps of the 2^23 AO gel run (0: skip it)")
     ap.add_argument("--skin", type=float, default=SKIN,
                     help="pair-list skin of the mixed form (0: walk the 27 cells every step)")
     ap.add_argument("--profile-only", action="store_true",
