@@ -237,6 +237,7 @@ ForceSetup make_setup(const psim_force_params* p, double L) {
     fs.cal.rc2f = (float)fs.cal.rc2;
     fs.rc_max = max_cutoff(p);
     fs.pre_rc2f = prefilter_r2(fs.rc_max, L);
+    fs.lj_pure = p->kind == PSIM_FORCE_LJ && p->yukawa_strength == 0.0;
     return fs;
 }
 
@@ -1109,6 +1110,7 @@ psim_system* psim_batch_create(const psim_replica* reps, int32_t n_reps,
         for (int i0 = g.p0; i0 < g.p1; i0 += 32) tasks.push_back(make_int2(r, i0));
         for (int i = g.p0; i < g.p1; ++i) rep[(size_t)i] = r;
         const ForceSetup fr = make_setup(&reps[r].force, g.L);
+        s->fs.lj_pure = s->fs.lj_pure && fr.lj_pure;
         pre[(size_t)r] = fr.pre_rc2f;
         seeds[(size_t)r] = (uint32_t)reps[r].seed;
         const void* src = kind == PSIM_FORCE_AO ? (const void*)&fr.ao

@@ -266,4 +266,42 @@ struct LJFixed : LJPair {
     }
 };
 
+// LennardJones with an even exponent fixed at compile time and no Yukawa term
+// (yukawaStrength 0, the plain 2n-n potential): fNet = -kT wd (2L-1) 4n L / r
+// with L = (size^2 / r^2)^(n/2), a function of r^2 alone.
+template <int N>
+struct LJPure : LJPair {
+    static_assert(N > 0 && N % 2 == 0, "an even, positive exponent");
+    __device__ __forceinline__ float fnet32(float, float, float rinv, float size) const {
+        const float lj = powi_fixed<N>(size * rinv);
+        return -kTwdf * ((2.0f * lj - 1.0f) * (four_nf * rinv * lj));
+    }
+};
+
+static_assert(sizeof(LJPure<6>) == sizeof(LJPair), "batches store LJPair parameters");
+
+// FP32 reciprocal, approximate (rcp.approx: max error ~1 ulp)
+__device__ __forceinline__ float rcp_approx(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// F(r)/r of a pair at r^2 for the pair-list pass, the value the cell walk's
+// body forms as fnet32(r2, r, 1/r, size) / r.  s2 = size^2.
+template <class P>
+__device__ __forceinline__ float list_fr32(const P& p, float r2, float size, float) {
+    const float rinv = rsqrtf(r2);
+    return p.fnet32(r2, r2 * rinv, rinv, size) * rinv;
+}
+// the plain LJ form needs only 1/r^2: C (2L - 1) L / r^2 with C = -kT wd 4n
+// and L = (s2 / r^2)^(n/2), one reciprocal and no square root
+template <int N>
+__device__ __forceinline__ float list_fr32(const LJPure<N>& p, float r2, float, float s2) {
+    const float rinv2 = rcp_approx(r2);
+    const float lj = powi_fixed<N / 2>(s2 * rinv2);
+    const float c = -p.kTwdf * p.four_nf;
+    return fmaf(2.0f * c, lj, -c) * (lj * rinv2);
+}
+
 }  // namespace psim

@@ -116,23 +116,48 @@ __device__ __forceinline__ void load_record(const float4* pos, uint32_t j, float
         : "l"(a));
 }
 
+// A neighbour record as the force pass holds it between its load and its
+// pair term: one float4 (compact) or the high and low halves (full).
+template <bool kCompact>
+struct ListRec {
+    float4 h;
+};
+template <>
+struct ListRec<false> {
+    float4 h, l;
+};
+__device__ __forceinline__ ListRec<true> load_rec(const float4* pos, uint32_t j,
+                                                  ListRec<true>) {
+    return ListRec<true>{__ldg(pos + j)};
+}
+__device__ __forceinline__ ListRec<false> load_rec(const float4* pos, uint32_t j,
+                                                   ListRec<false>) {
+    ListRec<false> r;
+    load_record(pos, j, r.h, r.l);
+    return r;
+}
+
 // A thread per particle (current storage order f): its list slot, its list,
-// its neighbours' records; the force is stored at f.  Lists are padded to
-// whole batches, so each batch's loads are issued together before any of its
-// pair terms, and every record holds the image the pair needs: no periodic
-// arithmetic per pair.
+// its neighbours' records; the force is stored at f.  The list is walked in
+// batches of 4 entries (lists are padded to multiples of 8, kListFold).  Each
+// batch's records are loaded one batch ahead of its pair terms, and its list
+// entries -- streamed from DRAM -- one batch ahead of the records, so the
+// latency of both overlaps the terms of the batch before.  Every record holds
+// the image the pair needs: no periodic arithmetic per pair.  A separation
+// is d = (x_j,hi - x_i,hi) + (x_j,lo - x_i,lo): the first difference is exact
+// for nearby values and the second comes out of the record's decode
+// (compact) or one subtraction (full), so d carries one FP32 rounding.
 template <class Body, bool kCompact>
 __global__ void __launch_bounds__(128)
 force_list_kernel(Body body, DevGeom g, PairList pl, ForceOut out) {
-    constexpr int kBatch = 8;
+    constexpr int kBatch = 4;
     static_assert(kListFold % kBatch == 0, "batches tile a fold");
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= g.n || *out.err) return;
     const int s = pl.lslot[f];
     float4 hh, hl;
     // compact records: a neighbour's low part minus the home's comes out of one
-    // FMA per axis, fma(2^23 + code, unit, c) with c = -(2^23 + 512) unit - l_i,
-    // so the body sees the home's low part as 0
+    // FMA per axis, fma(2^23 + code, unit, c) with c = -(2^23 + 512) unit - l_i
     float cx = 0.f, cy = 0.f, cz = 0.f;
     const float unit = pl.lo_unit;
     if (kCompact) {
@@ -148,46 +173,55 @@ force_list_kernel(Body body, DevGeom g, PairList pl, ForceOut out) {
         hh = pl.pos[2 * (size_t)s];
         hl = pl.pos[2 * (size_t)s + 1];
     }
-    // the body reads the home's low part as cv.posl[i]
-    CellView cv{};
-    cv.posl = &hl;
-    typename Body::Home home;
-    body.load_home(cv, 0, home);
-    typename Body::Shifted hs;
-    body.shift(home, hh, 0, 0, 0, g, hs);
+    const float usize = 2.0f * pl.radius, us2 = usize * usize;
     typename Body::Acc acc;
     body.init(acc);
     uint32_t err = 0;
+    float rmin = 3.0e38f;
     const int cnt = pl.count[s];   // a multiple of kListFold
     const uint32_t* lp = pl.list + s;
-    for (int k0 = 0; k0 < cnt; k0 += kListFold) {
+    using Rec = ListRec<kCompact>;
+    const Rec none{};
+    uint32_t e[kBatch];
+    Rec r[kBatch], rn[kBatch];
+    // prologue: the first batch's records, the second batch's entries
 #pragma unroll
-        for (int b = 0; b < kListFold; b += kBatch) {
-            uint32_t e[kBatch];
-            float4 nh[kBatch], nl[kBatch];
+    for (int u = 0; u < kBatch; ++u) e[u] = cnt > 0 ? __ldg(lp + (size_t)u * pl.stride) : 0u;
 #pragma unroll
-            for (int u = 0; u < kBatch; ++u) e[u] = __ldg(lp + (size_t)(k0 + b + u) * pl.stride);
-            if (kCompact) {
-                float4 c[kBatch];   // 16-byte records: all loads first
+    for (int u = 0; u < kBatch; ++u) r[u] = cnt > 0 ? load_rec(pl.pos, e[u], none) : none;
 #pragma unroll
-                for (int u = 0; u < kBatch; ++u) c[u] = __ldg(pl.pos + e[u]);
+    for (int u = 0; u < kBatch; ++u)
+        e[u] = cnt > kBatch ? __ldg(lp + (size_t)(kBatch + u) * pl.stride) : 0u;
+    for (int k0 = 0; k0 < cnt; k0 += kBatch) {
+        // entries of batch k0 + kBatch are in e (when it exists): its records,
+        // then the entries of the batch after it, then batch k0's terms
+        const bool next = k0 + kBatch < cnt, after = k0 + 2 * kBatch < cnt;
 #pragma unroll
-                for (int u = 0; u < kBatch; ++u) {
-                    const uint32_t w = __float_as_uint(c[u].w);
-                    nh[u] = make_float4(c[u].x, c[u].y, c[u].z, pl.radius);
-                    nl[u] = make_float4(fmaf(lo_magic(w & 1023u), unit, cx),
-                                        fmaf(lo_magic((w >> 10) & 1023u), unit, cy),
-                                        fmaf(lo_magic((w >> 20) & 1023u), unit, cz), 0.f);
-                }
+        for (int u = 0; u < kBatch; ++u) rn[u] = next ? load_rec(pl.pos, e[u], none) : none;
+#pragma unroll
+        for (int u = 0; u < kBatch; ++u)
+            e[u] = after ? __ldg(lp + (size_t)(k0 + 2 * kBatch + u) * pl.stride) : 0u;
+#pragma unroll
+        for (int u = 0; u < kBatch; ++u) {
+            if constexpr (kCompact) {
+                const uint32_t w = __float_as_uint(r[u].h.w);
+                const float d0 = (r[u].h.x - hh.x) + fmaf(lo_magic(w & 1023u), unit, cx);
+                const float d1 = (r[u].h.y - hh.y) + fmaf(lo_magic((w >> 10) & 1023u), unit, cy);
+                const float d2 = (r[u].h.z - hh.z) + fmaf(lo_magic((w >> 20) & 1023u), unit, cz);
+                body.template eval_list<true>(d0, d1, d2, usize, us2, acc, rmin, err);
             } else {
-#pragma unroll
-                for (int u = 0; u < kBatch; ++u) load_record(pl.pos, e[u], nh[u], nl[u]);
+                const float d0 = (r[u].h.x - hh.x) + (r[u].l.x - hl.x);
+                const float d1 = (r[u].h.y - hh.y) + (r[u].l.y - hl.y);
+                const float d2 = (r[u].h.z - hh.z) + (r[u].l.z - hl.z);
+                const float size = hh.w + r[u].h.w;
+                body.template eval_list<false>(d0, d1, d2, size, size * size, acc, rmin, err);
             }
-#pragma unroll
-            for (int u = 0; u < kBatch; ++u) body.eval_masked(nh[u], nl[u], hs, acc, err);
         }
-        body.fold(acc);
+        if ((k0 + kBatch) % kListFold == 0) body.fold(acc);
+#pragma unroll
+        for (int u = 0; u < kBatch; ++u) r[u] = rn[u];
     }
+    if (kCompact) body.list_overlap(rmin, us2, err);
     body.store(out, f, acc);
     if (err) atomicOr(out.err, err);
 }

@@ -23,6 +23,7 @@ struct ForceSetup {
     double rc_max;     // largest cutoff: cell_size must be >= rc_max
     float pre_rc2f;    // conservative FP32 prefilter bound on r^2 (FP64 form)
     int tile;          // 0: a warp per 32 consecutive particles; 1: a block per home cell
+    int lj_pure;       // LennardJones with yukawaStrength 0 in every replica
 };
 
 // Positions and cell ranges in sorted (cell) order, as the force kernels read them.

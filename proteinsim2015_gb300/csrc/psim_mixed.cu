@@ -105,26 +105,28 @@ struct MixedBody {
             a.p2 += f * d2;
         }
     }
-    // eval without a branch on the cutoff (the pair-list pass, where most
-    // candidates are in range): out-of-range terms are computed at r^2 = 1
-    // and dropped
-    __device__ __forceinline__ void eval_masked(const float4& hj, const float4& lj,
-                                                const Shifted& hs, Acc& a, uint32_t& err) const {
-        const float d0 = (hj.x - hs.h.x) + (lj.x - hs.lx);
-        const float d1 = (hj.y - hs.h.y) + (lj.y - hs.ly);
-        const float d2 = (hj.z - hs.h.z) + (lj.z - hs.lz);
+    // the pair-list pass: one entry at separation d (the float-pair difference
+    // already formed), masked by the cutoff.  kUniform: every pair has the
+    // contact diameter `size` (s2 = size^2), and the overlap test runs once
+    // per particle on the smallest r^2 (rmin); otherwise per pair.
+    template <bool kUniform>
+    __device__ __forceinline__ void eval_list(float d0, float d1, float d2, float size, float s2,
+                                              Acc& a, float& rmin, uint32_t& err) const {
         const float r2 = d0 * d0 + d1 * d1 + d2 * d2;
         const bool in = r2 < rc2f;
-        const float r2s = in ? r2 : 1.0f;
-        const float rinv = rsqrtf(r2s);
-        const float r = r2s * rinv;
-        const float size = hs.h.w + hj.w;
-        if (in && r < 0.8f * size) err |= EBIT_OVERLAP;
-        const float fr = pf.fnet32(r2s, r, rinv, size) * rinv;
+        const float fr = list_fr32(pf, r2, size, s2);
+        if (kUniform)
+            rmin = fminf(rmin, r2);
+        else if (in && r2 < 0.64f * s2)
+            err |= EBIT_OVERLAP;
         const float f = in ? fr : 0.0f;
         a.p0 += f * d0;
         a.p1 += f * d1;
         a.p2 += f * d2;
+    }
+    // the overlap test of eval_list<true>: r < 0.8 size for an in-range pair
+    __device__ __forceinline__ void list_overlap(float rmin, float s2, uint32_t& err) const {
+        if (rmin < fminf(0.64f * s2, rc2f)) err |= EBIT_OVERLAP;
     }
     __device__ __forceinline__ void fold(Acc& a) const {
         kahan_add(a.s0, a.k0, a.p0);
@@ -174,8 +176,10 @@ struct MixedBody {
     }
 };
 
-// The plugin's pair functor (LennardJones with its exponent fixed at compile
-// time for the common ljNum values) handed to run(pair, rc2f).
+// The plugin's pair functor handed to run(pair, rc2f): LennardJones without
+// a Yukawa term gets its exponent fixed at compile time for the common ljNum
+// values 6, 12 and 18, the pure Yukawa form (ljNum 0) likewise; other
+// LennardJones settings run the general functor.
 template <class Run>
 static cudaError_t with_pair(const ForceSetup& fs, Run&& run) {
     switch (fs.kind) {
@@ -185,13 +189,15 @@ static cudaError_t with_pair(const ForceSetup& fs, Run&& run) {
             static_cast<LJPair&>(p) = fs.lj;
             return run(p, fs.lj.rc2f);
         };
-        switch (fs.lj.n) {
-        case 0: return fixed(LJFixed<0>{});
-        case 6: return fixed(LJFixed<6>{});
-        case 12: return fixed(LJFixed<12>{});
-        case 18: return fixed(LJFixed<18>{});
-        default: return run(fs.lj, fs.lj.rc2f);
+        if (fs.lj_pure) {
+            switch (fs.lj.n) {
+            case 6: return fixed(LJPure<6>{});
+            case 12: return fixed(LJPure<12>{});
+            case 18: return fixed(LJPure<18>{});
+            }
         }
+        if (fs.lj.n == 0) return fixed(LJFixed<0>{});
+        return run(fs.lj, fs.lj.rc2f);
     }
     case 3: return run(fs.cal, fs.cal.rc2f);
     case 4: {
