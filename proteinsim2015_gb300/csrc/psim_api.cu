@@ -849,7 +849,7 @@ cudaError_t enqueue_list_build(psim_system* s, int cb, const int* gate) {
     CellView cv{nullptr, s->posh.as<float4>(), s->posl.as<float4>(), s->cellid.as<int>(),
                 s->start.as<int>(), s->count[cb].as<int>()};
     ListBuild lb{s->list.as<uint32_t>(), s->lcount.as<int>(), s->n, s->lcap, s->lpre, gate,
-                 s->lhalo.as<int>()};
+                 s->lhalo.as<int>(), s->n};
     return launch_list_build(s->g, cv, lb, s->err.as<uint32_t>(), s->st);
 }
 

@@ -202,6 +202,13 @@ __device__ __forceinline__ void halo_write(float4* pos, float inv_unit, int base
 // Neighbour cell index wrapped into [0, s) as the reference does
 // ((c % s) + s when negative, AOPotential.cpp:154-160), and the periodic
 // image it implies (-1, 0 or +1 boxes).
+// The spacing of floats at x (x > 0 and normal, 2^(e-23) for x in [2^e, 2^(e+1))),
+// from the exponent bits; the smallest normal float when that is smaller.
+__device__ __forceinline__ float ulp_of(float x) {
+    const int eb = (int)((__float_as_uint(x) >> 23) & 0xffu) - 23;
+    return __uint_as_float((uint32_t)(eb > 1 ? eb : 1) << 23);
+}
+
 __device__ __forceinline__ int wrap_cell(int c, int s, int& shift) {
     int w = c % s;
     if (w < 0) w += s;

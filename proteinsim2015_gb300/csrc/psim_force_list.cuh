@@ -32,80 +32,148 @@
 
 namespace psim {
 
-// Appends the candidates the warp kernel selects to the home particle's
-// list, then pads the list to a multiple of kListFold with the ghost record
-// (a far-away dummy particle), so the force pass reads whole batches.  The
-// neighbour's slot travels in the .w lane of its low-part float4; a pair
+// The pair-list build, a thread per particle i (sorted order of the build
+// step, whose list slots are the sorted positions).  It walks the 27
+// neighbour cells as 9 rows of x-adjacent cells -- one contiguous run of the
+// sorted list per row, plus a one-cell run where the row wraps in x -- and
+// appends every candidate within the list radius (rc + skin, widened by the
+// FP32 test's rounding margin).  A neighbour cell beyond that radius from
+// the particle (by its distance to the cell's faces) is not read: about a
+// quarter of the 27 cells on average when cellSize ~ rc + skin.  A pair
 // across the box edge refers to the neighbour's halo record for that image.
-struct ListBody {
-    uint32_t* list;
-    int* count;
-    int stride;
-    int cap;           // a multiple of kListFold
-    int ghost;         // the ghost record (n); halo records follow it
-    const int* lhalo;
-    using Aux = float4;
-    static constexpr bool kBatchable = false;   // pair lists are built for one system only
-    struct Home {
-        int i;
-    };
-    struct Shifted {
-        int i;
-        int sx, sy, sz;   // the neighbour image x_j + s L of this row
-    };
-    struct Acc {
-        int n;
-    };
-    __device__ __forceinline__ const Aux* aux(const CellView& cv) const { return cv.posl; }
-    __device__ __forceinline__ void init(Acc& a) const { a.n = 0; }
-    __device__ __forceinline__ void load_home(const CellView&, int i, Home& h) const { h.i = i; }
-    __device__ __forceinline__ void shift(const Home& h, const float4&, int sx, int sy, int sz,
-                                          const DevGeom&, Shifted& o) const {
-        o.i = h.i;
-        o.sx = sx;
-        o.sy = sy;
-        o.sz = sz;
-    }
-    __device__ __forceinline__ void eval(const float4&, const float4& lj, const Shifted& hs,
-                                         Acc& a, uint32_t& err) const {
-        uint32_t j = __float_as_uint(lj.w);
-        if ((hs.sx | hs.sy | hs.sz) != 0) {
-            // image number: one bit per flagged axis, set where this row shifts
-            const int hal = lhalo[j];
-            const uint32_t fl = (uint32_t)(hal & 63);
-            const int s[3] = {hs.sx, hs.sy, hs.sz};
-            int num = 0, bit = 0;
-            bool ok = true;
+// Lists are padded to a multiple of kListFold with the ghost record, a
+// far-away dummy particle, so the force pass reads whole batches.
+// st.global of v at p when w holds; no branch around it
+__device__ __forceinline__ void store_if(uint32_t* p, uint32_t v, bool w) {
+    asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %2, 0;\n\t@q st.global.u32 [%0], %1;\n\t}"
+                 :: "l"(p), "r"(v), "r"((uint32_t)w) : "memory");
+}
+
+// Appends the candidates of one run [a, a + len) of the sorted list within
+// the list radius of the home position (hx, hy, hz) (the home particle i
+// minus the run's image s L) to i's list, n entries so far.  Unshifted runs,
+// almost all of them, append the candidate's own slot branch-free; a shifted
+// run appends the neighbour's halo record for that image.
+template <bool kShifted>
+__device__ __forceinline__ void list_run(const CellView& cv, const ListBuild& lb, int i, int a,
+                                         int len, float hx, float hy, float hz, int sx, int sy,
+                                         int sz, int& n, uint32_t& err) {
+    const float R2 = lb.pre_r2;
+    for (int t0 = 0; t0 < len; t0 += 4) {
+        float4 hj[4];
 #pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                const int fk = halo_axis(fl, k);
-                if (s[k] != 0) {
-                    ok = ok && fk == s[k];
-                    num |= 1 << bit;
+        for (int u = 0; u < 4; ++u) hj[u] = __ldg(&cv.posh[a + min(t0 + u, len - 1)]);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int j = a + t0 + u;
+            const float ex = hj[u].x - hx, ey = hj[u].y - hy, ez = hj[u].z - hz;
+            const float r2 = ex * ex + ey * ey + ez * ez;
+            const bool in = (t0 + u < len) & (r2 < R2) & (j != i);
+            if (!kShifted) {
+                store_if(lb.list + (size_t)n * lb.stride + i, (uint32_t)j, in & (n < lb.cap));
+                n += in ? 1 : 0;
+            } else if (in) {
+                // image number: one bit per flagged axis, set where this run shifts
+                const int hal = lb.lhalo[j];
+                const uint32_t fl = (uint32_t)(hal & 63);
+                const int sh[3] = {sx, sy, sz};
+                int num = 0, bit = 0;
+                bool ok = true;
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const int fk = halo_axis(fl, k);
+                    if (sh[k] != 0) {
+                        ok = ok && fk == sh[k];
+                        num |= 1 << bit;
+                    }
+                    if (fk != 0) ++bit;
                 }
-                if (fk != 0) ++bit;
+                if (!ok) {   // no record of that image: the margin failed
+                    err |= EBIT_LIST;
+                } else {
+                    if (n < lb.cap)
+                        lb.list[(size_t)n * lb.stride + i] = (uint32_t)(lb.ghost + 1 + (hal >> 6) + num - 1);
+                    ++n;
+                }
             }
-            if (!ok) {          // no record of that image: the margin failed
-                err |= EBIT_LIST;
-                return;
+        }
+    }
+}
+
+__device__ __forceinline__ void list_build_one(const DevGeom& g, const CellView& cv,
+                                               const ListBuild& lb, int i, uint32_t& err) {
+    const float4 hi = cv.posh[i];
+    const int c = cv.cellid[i] - g.c0;
+    const int cx = c % g.s, cy = (c / g.s) % g.s, cz = c / g.s2;
+    const int ghost = g.n;
+    const float R2 = lb.pre_r2;
+    // distances to the lower and upper faces of the home cell, less a margin
+    // for the FP32 rounding of the position and of the cell bounds
+    const float csf = (float)g.cs;
+    const float m = 8.0f * ulp_of(g.Lhi);
+    const float fx = hi.x - (float)cx * csf, fy = hi.y - (float)cy * csf,
+                fz = hi.z - (float)cz * csf;
+    const float lo[3] = {fmaxf(fx - m, 0.f), fmaxf(fy - m, 0.f), fmaxf(fz - m, 0.f)};
+    const float up[3] = {fmaxf(csf - fx - m, 0.f), fmaxf(csf - fy - m, 0.f),
+                         fmaxf(csf - fz - m, 0.f)};
+    int n = 0;
+    for (int row = 0; row < 9; ++row) {
+        const int dz = row / 3 - 1, dy = row % 3 - 1;
+        const float ey = dy < 0 ? lo[1] : (dy > 0 ? up[1] : 0.f);
+        const float ez = dz < 0 ? lo[2] : (dz > 0 ? up[2] : 0.f);
+        const float e2 = ey * ey + ez * ez;
+        if (e2 >= R2) continue;
+        int sy, sz;
+        const int y = wrap_cell(cy + dy, g.s, sy);
+        const int z = wrap_cell(cz + dz, g.s, sz);
+        const int base = g.c0 + g.s * y + g.s2 * z;
+        const bool left = e2 + lo[0] * lo[0] < R2, right = e2 + up[0] * up[0] < R2;
+#pragma unroll 1
+        for (int part = 0; part < 2; ++part) {
+            // part 0: the reachable cells of [cx-1, cx+1] inside the grid;
+            // part 1: the one cell that wraps around in x (if reachable)
+            int a = 0, len = 0, sx = 0;
+            if (part == 0) {
+                const int xa = (left && cx > 0) ? cx - 1 : cx;
+                const int xb = (right && cx < g.s - 1) ? cx + 1 : cx;
+                a = cv.cstart[base + xa];
+                len = cv.cstart[base + xb] + cv.ccount[base + xb] - a;
+            } else if ((cx == 0 && left) || (cx == g.s - 1 && right)) {
+                const int xw = cx == 0 ? g.s - 1 : 0;
+                sx = cx == 0 ? -1 : 1;
+                a = cv.cstart[base + xw];
+                len = cv.ccount[base + xw];
             }
-            j = (uint32_t)(ghost + 1 + (hal >> 6) + num - 1);
+            if (len <= 0) continue;
+            // the row's image is applied to the home position
+            const float hx = hi.x - (float)sx * g.Lhi;
+            const float hy = hi.y - (float)sy * g.Lhi;
+            const float hz = hi.z - (float)sz * g.Lhi;
+            if ((sx | sy | sz) == 0)
+                list_run<false>(cv, lb, i, a, len, hx, hy, hz, 0, 0, 0, n, err);
+            else
+                list_run<true>(cv, lb, i, a, len, hx, hy, hz, sx, sy, sz, n, err);
         }
-        if (a.n < cap) list[(size_t)a.n * stride + hs.i] = j;
-        a.n++;
     }
-    __device__ __forceinline__ void fold(Acc&) const {}
-    __device__ __forceinline__ void store(const ForceOut& out, int i, const Acc& a) const {
-        if (a.n > cap) {
-            atomicOr(out.err, EBIT_LIST);
-            count[i] = cap;
-            return;
-        }
-        const int padded = (a.n + kListFold - 1) / kListFold * kListFold;
-        for (int k = a.n; k < padded; ++k) list[(size_t)k * stride + i] = (uint32_t)ghost;
-        count[i] = padded;
+    if (n > lb.cap) {
+        err |= EBIT_LIST;
+        n = lb.cap;
     }
-};
+    const int padded = (n + kListFold - 1) / kListFold * kListFold;
+    for (int k = n; k < padded; ++k) lb.list[(size_t)k * lb.stride + i] = (uint32_t)ghost;
+    lb.count[i] = padded;
+}
+
+// A grid of a few blocks per SM striding over the particles, so that a step
+// whose rebuild gate is closed costs one short launch.
+__global__ void __launch_bounds__(128)
+list_build_kernel(DevGeom g, CellView cv, ListBuild lb, uint32_t* errp) {
+    if (*errp != 0 || (lb.gate && *lb.gate == 0)) return;
+    uint32_t err = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += gridDim.x * blockDim.x)
+        list_build_one(g, cv, lb, i, err);
+    if (err) atomicOr(errp, err);
+}
 
 // One 32-byte record (high and low float4 halves) in a single 256-bit load
 // through the read-only path; the records are 32-byte aligned.

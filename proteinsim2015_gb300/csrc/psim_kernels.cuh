@@ -94,6 +94,7 @@ struct ListBuild {
     float pre_r2;
     const int* gate;
     const int* lhalo;      // per list slot: first halo record << 6 | halo_flags
+    int ghost;             // the ghost record (n); halo records follow it
 };
 cudaError_t launch_list_build(const DevGeom& g, const CellView& cv, const ListBuild& lb,
                               uint32_t* err, cudaStream_t st);

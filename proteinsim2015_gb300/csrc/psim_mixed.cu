@@ -10,6 +10,7 @@
 // where the first difference is exact for nearby values (Sterbenz), so d
 // carries one FP32 rounding of a number of size <= rc, not of the box.
 // The pair loop itself is force_pass_kernel (psim_force.cuh).
+#include <algorithm>
 #include <cmath>
 
 #include "psim_force.cuh"
@@ -227,9 +228,17 @@ cudaError_t launch_forces_list(const ForceSetup& fs, const DevGeom& g, const Pai
 
 cudaError_t launch_list_build(const DevGeom& g, const CellView& cv, const ListBuild& lb,
                               uint32_t* err, cudaStream_t st) {
-    const ListBody body{lb.list, lb.count, lb.stride, lb.cap, g.n, lb.lhalo};
-    const ForceOut out{nullptr, nullptr, nullptr, err, lb.gate};
-    return launch_force_pass(body, g, cv, out, lb.pre_r2, st);
+    if (g.n == 0) return cudaSuccess;
+    static int blocks = 0;   // 32 blocks per SM of the current device
+    if (blocks == 0) {
+        int dev = 0, sms = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            sms = 152;
+        blocks = 32 * sms;
+    }
+    list_build_kernel<<<std::min(blocks, (g.n + 127) / 128), 128, 0, st>>>(g, cv, lb, err);
+    return cudaGetLastError();
 }
 
 // The update of the mixed form: the same FP64 arithmetic as psim_exact.cu's
