@@ -340,6 +340,8 @@ int make_vgb_params(const psim_integrator_config* ic, VgbParams* p) {
     p->corrf = (float)c.corr;
     p->devf = (float)c.dev;
     p->coeff0f = (float)c.coeff0;
+    p->dt2c1f = (float)p->dt2c1;
+    p->dt2c2f = (float)p->dt2c2;
     p->vel_freq = ic->vel_freq;
     p->seed = (uint32_t)ic->seed;
     return PSIM_OK;

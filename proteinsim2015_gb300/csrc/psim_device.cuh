@@ -85,6 +85,20 @@ __device__ __forceinline__ float f32_trunc(double x) {
                : 0.f;
 }
 
+// x cut to FP32 toward zero like f32_trunc, except that a value beyond the
+// FP32 range becomes an infinity and a NaN stays a NaN.
+__device__ __forceinline__ float f32_cut(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const uint32_t top = (uint32_t)(b >> 32);
+    const uint32_t sign = top & 0x80000000u;
+    const int e = (int)((top >> 20) & 0x7FFu);
+    const uint32_t m23 = (uint32_t)(b >> 29) & 0x7FFFFFu;
+    const bool nan = e == 2047 && (b << 12) != 0ull;
+    const uint32_t big = sign | 0x7F800000u | (nan ? 0x400000u : 0u);
+    return __uint_as_float(e >= 1151 ? big
+                                     : (e > 896 ? sign | ((uint32_t)(e - 896) << 23) | m23 : sign));
+}
+
 // A float widened to double exactly, by integer operations (FP32 subnormals,
 // which the noise never produces, become zero).
 __device__ __forceinline__ double widen_f32(float f) {

@@ -107,7 +107,7 @@ struct VgbParams {
     // the mixed form's normal step: dt^2 coeff1, dt^2 coeff2, and the noise
     // coefficients in FP32
     double dt2c1, dt2c2;
-    float sig1f, sig2f, corrf, devf, coeff0f;
+    float sig1f, sig2f, corrf, devf, coeff0f, dt2c1f, dt2c2f;
     int vel_freq;
     uint32_t seed;
 };

@@ -129,28 +129,38 @@ __device__ __forceinline__ void vgb_particle(const VgbParams& p, double L, doubl
     }
 }
 
-// normalStep of the mixed form (brownianIntegrator.cpp:225-296): the
-// position terms in FP64 (FMA-contracted), the noise terms -- random numbers
-// drawn in FP32 -- summed in FP32 and added to the position once.  The wrap
-// is normalStep's; the previous position's re-image test runs in FP32 with
-// a wide margin and falls back to FP64 near L/2.  xf: the 6 Gaussians.
+// normalStep of the mixed form (brownianIntegrator.cpp:225-296), written as
+//   x_new = x + [coEff0 (x - x0) + dt^2 coEff1 F/m + dt^2 coEff2 (F - F0)/m + noise]
+// (c0 = 1 + coEff0): the bracket -- a displacement of ~v dt -- is summed in
+// FP32 from FP32 cuts of its terms (the random numbers are drawn in FP32) and
+// added to the FP64 position once, so each step carries ~1e-10 of rounding
+// on top of the FP64 form's, four orders of magnitude below the step's own
+// noise.  GB300 runs FP64 at 1/64 of the FP32 rate: this leaves two FP64
+// additions per axis.  The wrap is normalStep's; the previous position's
+// re-image test runs in FP32 with a wide margin and falls back to FP64 near
+// L/2.  xf: the 6 Gaussians.  A NaN in any input reaches the position and
+// the bounds test.
 __device__ __forceinline__ void vgb_normal_fast(const VgbParams& p, double L, double half_L,
                                                 const double x[3], const double x0[3],
                                                 double mx[3], const double F[3],
                                                 const double F0[3], const float xf[6], double m,
                                                 double xn[3], double x0n[3], uint32_t& err) {
-    const double c1 = m * p.dt2c1;
-    const double c2 = m * p.dt2c2;
+    // explicit roundings (no contraction left to the compiler), so every
+    // instance of this update -- one system or a batch -- rounds alike
+    const float mf = f32_cut(m);
+    const float c1 = __fmul_rn(mf, p.dt2c1f);
+    const float c2 = __fmul_rn(mf, p.dt2c2f);
     double nw[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        const float mcf = p.sig2f * (p.corrf * f32_trunc(mx[k]) + p.devf * xf[k]);
-        const float noise = p.sig1f * xf[3 + k] + p.coeff0f * mcf;
-        double t = p.c0 * x[k];
-        t -= p.coeff0 * x0[k];
-        t += c1 * F[k];
-        t += c2 * (F[k] - F0[k]);
-        nw[k] = t + widen_f32(noise);
+        const float mcf =
+            __fmul_rn(p.sig2f, __fmaf_rn(p.corrf, f32_trunc(mx[k]), __fmul_rn(p.devf, xf[k])));
+        const float noise = __fmaf_rn(p.sig1f, xf[3 + k], __fmul_rn(p.coeff0f, mcf));
+        const float d = f32_cut(x[k] - x0[k]);
+        const float fk = f32_cut(F[k]), f0k = f32_cut(F0[k]);
+        const float step =
+            __fmaf_rn(p.coeff0f, d, __fmaf_rn(c1, fk, __fmaf_rn(c2, __fsub_rn(fk, f0k), noise)));
+        nw[k] = x[k] + widen_f32(step);
         mx[k] = widen_f32(xf[3 + k]);
     }
     bool lo[3], hi[3];
@@ -176,7 +186,8 @@ __device__ __forceinline__ void vgb_normal_fast(const VgbParams& p, double L, do
         bool far = df > 0.6f * Lf;
         if (df >= 0.4f * Lf && df <= 0.6f * Lf) far = abs_gt_d(xn[k] - x[k], half_L);
         x0n[k] = far ? ((xn[k] - x[k] < 0) ? x[k] - L : x[k] + L) : x[k];
-        const bool inside = !neg_d(xn[k]) && !ge_pos_d(xn[k], L) && (xn[k] == xn[k]);
+        // [0, L) as normalStep requires; a NaN (either sign) fails one of the two
+        const bool inside = !neg_d(xn[k]) && !ge_pos_d(xn[k], L);
         if (!inside) err |= EBIT_BOUNDS;
     }
 }
