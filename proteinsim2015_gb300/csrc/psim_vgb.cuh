@@ -261,10 +261,10 @@ __device__ __forceinline__ void load_noise_f(const NoiseView& nz, uint32_t seed,
 // The new position in pair-list order: the periodic image nearest the
 // position at the list build (|x - build| < L/2 picks it), as an exact float
 // pair; raises the rebuild flag when it has moved more than sqrt(ldisp2).
-__device__ __forceinline__ void list_position(const VgbSystemArgs& a, int f, const double xn[3],
-                                              const DevGeom& g) {
-    const int s = a.lslot[f];
-    const float4 b = a.lbuild[s];
+// s, b, hal: the particle's list slot, its position at the build and its halo
+// word, loaded before the update so that their latency overlaps it.
+__device__ __forceinline__ void list_position(const VgbSystemArgs& a, int s, const float4& b,
+                                              int hal, const double xn[3], const DevGeom& g) {
     const float bb[3] = {b.x, b.y, b.z};
     const float halff = 0.5f * g.Lhi;
     float h[3], l[3], d2 = 0.f;
@@ -279,7 +279,6 @@ __device__ __forceinline__ void list_position(const VgbSystemArgs& a, int f, con
     }
     const float4 hv = make_float4(h[0], h[1], h[2], b.w), lv = make_float4(l[0], l[1], l[2], 0.f);
     store_record(a.lpos, a.linv_unit, (size_t)s, hv, lv);
-    const int hal = a.lhalo[s];
     if (hal & 63)  // the particle's periodic images in the halo records
         halo_write(a.lpos + (a.linv_unit != 0.f ? 1 : 2) * ((size_t)a.n + 1), a.linv_unit,
                    hal >> 6, (uint32_t)(hal & 63), hv, lv, g.Lhi, g.Llo);
@@ -305,6 +304,13 @@ __device__ __forceinline__ void vgb_system_one(const VgbSystemArgs& a, const Vgb
     double mx[3] = {a.mx[o], a.my[o], a.mz[o]};
     const double F[3] = {a.fx[f], a.fy[f], a.fz[f]};
     const double F0[3] = {a.gx[o], a.gy[o], a.gz[o]};
+    int ls = 0, lhal = 0;
+    float4 lb = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (a.lslot) {
+        ls = __ldg(a.lslot + f);
+        lb = __ldg(a.lbuild + ls);
+        lhal = __ldg(a.lhalo + ls);
+    }
     double v[3] = {0.0, 0.0, 0.0};
     if (first || vel_step) {
         v[0] = a.vel[3 * (size_t)tag];
@@ -336,7 +342,7 @@ __device__ __forceinline__ void vgb_system_one(const VgbSystemArgs& a, const Vgb
         a.vel[3 * (size_t)tag + 1] = v[1];
         a.vel[3 * (size_t)tag + 2] = v[2];
     }
-    if (a.lslot) list_position(a, f, xn, g);
+    if (a.lslot) list_position(a, ls, lb, lhal, xn, g);
     if (f == 0 && a.lflag_clear) {
         *a.lflag_clear = 0;
         *a.lhcount = 0;   // halo records are handed out afresh at the next build
