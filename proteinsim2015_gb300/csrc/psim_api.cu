@@ -1193,6 +1193,14 @@ psim_system* system_new(const psim_system_config* cfg, const DevGeom& g) {
         s->list_on = true;
         s->skin = skin;
         s->lcap = ((int)(1.5 * mean) + 32 + 31) / 32 * 32;
+        if ((double)(s->lcap + kListFold) * (double)g.n >= 4294967296.0) {
+            // the list build addresses entries with 32-bit offsets
+            const int cap = s->lcap;
+            delete s;
+            fail(PSIM_ERR_INPUT, "the pair list of %d particles (%d entries each) is too large; "
+                 "use a smaller skin", g.n, cap);
+            return nullptr;
+        }
         s->lpre = prefilter_r2(rl, g.L);
         // the rebuild test compares FP32 roundings of the positions (each off
         // by ulp(L)/2): half the skin, less that error
@@ -1222,7 +1230,7 @@ psim_system* system_new(const psim_system_config* cfg, const DevGeom& g) {
     ok = ok && !s->cellid.ensure(4 * n) && !s->key.ensure(4 * n) && !s->rank.ensure(4 * n) &&
          !s->tmp.ensure(4 * n) && !s->start.ensure(4 * nc) &&
          !s->scratch.ensure(4 * scan_scratch_ints(g.ncell)) &&
-         !s->posh.ensure(16 * n) &&
+         !s->posh.ensure(16 * (n + 4)) &&   // + 4: the list build reads up to 3 past a run
          !s->vel.ensure(24 * n) && !s->err.ensure(4) && !s->state.ensure(sizeof(StepState)) &&
          !s->occ.ensure(4);
     if (ok && cfg->precision == PSIM_PRECISION_FP64) ok = !s->posd.ensure(32 * n);
@@ -1231,7 +1239,7 @@ psim_system* system_new(const psim_system_config* cfg, const DevGeom& g) {
     if (ok && list_on) {
         ok = !s->lslot[0].ensure(4 * n) && !s->lslot[1].ensure(4 * n) && !s->lbuild.ensure(16 * n) &&
              !s->lpos.ensure(32 * (n + 1 + (size_t)s->hcap)) &&
-             !s->list.ensure(4 * n * (size_t)s->lcap) && !s->lcount.ensure(4 * n) &&
+             !s->list.ensure(4 * n * (size_t)(s->lcap + kListFold)) && !s->lcount.ensure(4 * n) &&
              !s->lflag.ensure(8) && !s->lhalo.ensure(4 * n) && !s->lhcount.ensure(4) &&
              cudaMemset(s->lflag.p, 0, 8) == cudaSuccess &&
              cudaMemset(s->lhcount.p, 0, 4) == cudaSuccess;

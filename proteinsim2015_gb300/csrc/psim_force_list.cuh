@@ -49,31 +49,51 @@ __device__ __forceinline__ void store_if(uint32_t* p, uint32_t v, bool w) {
                  :: "l"(p), "r"(v), "r"((uint32_t)w) : "memory");
 }
 
+// A home's list is stored in groups of kListFold = 8 entries: group q of the
+// home in slot i is 32 contiguous bytes at element (q stride + i) 8, so the
+// force pass reads a group with one 32-byte load per thread.  The build
+// appends entry n of home i at element o = ((n / 8) stride + i) 8 + n % 8,
+// kept as a 32-bit offset (the host keeps (cap + 8) stride below 2^32);
+// entries past the cap go to the scratch group cap / 8 and are counted, so
+// that the overflow is reported.
+__device__ __forceinline__ void list_append(const ListBuild& lb, uint32_t ocap, uint32_t v,
+                                            bool in, int& n, uint32_t& o) {
+    store_if(lb.list + min(o, ocap), v, in);
+    n += in ? 1 : 0;
+    // next element: the following word, or the next group's first
+    const uint32_t step = (n & (kListFold - 1)) ? 1u : (uint32_t)lb.stride * kListFold - 7u;
+    o += in ? step : 0u;
+}
+
 // Appends the candidates of one run [a, a + len) of the sorted list within
 // the list radius of the home position (hx, hy, hz) (the home particle i
-// minus the run's image s L) to i's list, n entries so far.  Unshifted runs,
-// almost all of them, append the candidate's own slot branch-free; a shifted
-// run appends the neighbour's halo record for that image.
-template <bool kShifted>
+// minus the run's image s L) to i's list, n entries so far.  Candidates are
+// read four at a time, up to three past the run (the sorted positions are
+// padded by four), and masked.  Only the home row's run (kSelf) can hold i
+// itself; a shifted run appends the neighbour's halo record for that image.
+template <bool kShifted, bool kSelf>
 __device__ __forceinline__ void list_run(const CellView& cv, const ListBuild& lb, int i, int a,
                                          int len, float hx, float hy, float hz, int sx, int sy,
-                                         int sz, int& n, uint32_t& err) {
+                                         int sz, int& n, uint32_t& o, uint32_t& err) {
     const float R2 = lb.pre_r2;
-    for (int t0 = 0; t0 < len; t0 += 4) {
+    const uint32_t ocap = ((uint32_t)(lb.cap / kListFold) * (uint32_t)lb.stride + (uint32_t)i) *
+                          kListFold;
+    const float4* pp = cv.posh + a;
+    for (int t0 = 0; t0 < len; t0 += 4, pp += 4) {
         float4 hj[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) hj[u] = __ldg(&cv.posh[a + min(t0 + u, len - 1)]);
+        for (int u = 0; u < 4; ++u) hj[u] = __ldg(pp + u);
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-            const int j = a + t0 + u;
             const float ex = hj[u].x - hx, ey = hj[u].y - hy, ez = hj[u].z - hz;
             const float r2 = ex * ex + ey * ey + ez * ez;
-            const bool in = (t0 + u < len) & (r2 < R2) & (j != i);
+            bool in = (t0 + u < len) & (r2 < R2);
+            if (kSelf) in &= (a + t0 + u != i);
             if (!kShifted) {
-                store_if(lb.list + (size_t)n * lb.stride + i, (uint32_t)j, in & (n < lb.cap));
-                n += in ? 1 : 0;
+                list_append(lb, ocap, (uint32_t)(a + t0 + u), in, n, o);
             } else if (in) {
                 // image number: one bit per flagged axis, set where this run shifts
+                const int j = a + t0 + u;
                 const int hal = lb.lhalo[j];
                 const uint32_t fl = (uint32_t)(hal & 63);
                 const int sh[3] = {sx, sy, sz};
@@ -88,13 +108,11 @@ __device__ __forceinline__ void list_run(const CellView& cv, const ListBuild& lb
                     }
                     if (fk != 0) ++bit;
                 }
-                if (!ok) {   // no record of that image: the margin failed
+                if (!ok)   // no record of that image: the margin failed
                     err |= EBIT_LIST;
-                } else {
-                    if (n < lb.cap)
-                        lb.list[(size_t)n * lb.stride + i] = (uint32_t)(lb.ghost + 1 + (hal >> 6) + num - 1);
-                    ++n;
-                }
+                else
+                    list_append(lb, ocap, (uint32_t)(lb.ghost + 1 + (hal >> 6) + num - 1),
+                                true, n, o);
             }
         }
     }
@@ -117,6 +135,7 @@ __device__ __forceinline__ void list_build_one(const DevGeom& g, const CellView&
     const float up[3] = {fmaxf(csf - fx - m, 0.f), fmaxf(csf - fy - m, 0.f),
                          fmaxf(csf - fz - m, 0.f)};
     int n = 0;
+    uint32_t o = (uint32_t)i * kListFold;
     for (int row = 0; row < 9; ++row) {
         const int dz = row / 3 - 1, dy = row % 3 - 1;
         const float ey = dy < 0 ? lo[1] : (dy > 0 ? up[1] : 0.f);
@@ -149,19 +168,23 @@ __device__ __forceinline__ void list_build_one(const DevGeom& g, const CellView&
             const float hx = hi.x - (float)sx * g.Lhi;
             const float hy = hi.y - (float)sy * g.Lhi;
             const float hz = hi.z - (float)sz * g.Lhi;
-            if ((sx | sy | sz) == 0)
-                list_run<false>(cv, lb, i, a, len, hx, hy, hz, 0, 0, 0, n, err);
+            if ((sx | sy | sz) != 0)
+                list_run<true, false>(cv, lb, i, a, len, hx, hy, hz, sx, sy, sz, n, o, err);
+            else if (row == 4 && part == 0)
+                list_run<false, true>(cv, lb, i, a, len, hx, hy, hz, 0, 0, 0, n, o, err);
             else
-                list_run<true>(cv, lb, i, a, len, hx, hy, hz, sx, sy, sz, n, err);
+                list_run<false, false>(cv, lb, i, a, len, hx, hy, hz, 0, 0, 0, n, o, err);
         }
     }
+    // the open group padded with the ghost record
+    const uint32_t ocap = ((uint32_t)(lb.cap / kListFold) * (uint32_t)lb.stride + (uint32_t)i) *
+                          kListFold;
+    while (n & (kListFold - 1)) list_append(lb, ocap, (uint32_t)ghost, true, n, o);
     if (n > lb.cap) {
         err |= EBIT_LIST;
         n = lb.cap;
     }
-    const int padded = (n + kListFold - 1) / kListFold * kListFold;
-    for (int k = n; k < padded; ++k) lb.list[(size_t)k * lb.stride + i] = (uint32_t)ghost;
-    lb.count[i] = padded;
+    lb.count[i] = n;
 }
 
 // A grid of a few blocks per SM striding over the particles, so that a step
@@ -219,7 +242,7 @@ template <class Body, bool kCompact>
 __global__ void __launch_bounds__(128)
 force_list_kernel(Body body, DevGeom g, PairList pl, ForceOut out) {
     constexpr int kBatch = 4;
-    static_assert(kListFold % kBatch == 0, "batches tile a fold");
+    static_assert(kListFold == 2 * kBatch, "a fold is two batches");
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= g.n || *out.err) return;
     const int s = pl.lslot[f];
@@ -247,28 +270,9 @@ force_list_kernel(Body body, DevGeom g, PairList pl, ForceOut out) {
     uint32_t err = 0;
     float rmin = 3.0e38f;
     const int cnt = pl.count[s];   // a multiple of kListFold
-    const uint32_t* lp = pl.list + s;
     using Rec = ListRec<kCompact>;
     const Rec none{};
-    uint32_t e[kBatch];
-    Rec r[kBatch], rn[kBatch];
-    // prologue: the first batch's records, the second batch's entries
-#pragma unroll
-    for (int u = 0; u < kBatch; ++u) e[u] = cnt > 0 ? __ldg(lp + (size_t)u * pl.stride) : 0u;
-#pragma unroll
-    for (int u = 0; u < kBatch; ++u) r[u] = cnt > 0 ? load_rec(pl.pos, e[u], none) : none;
-#pragma unroll
-    for (int u = 0; u < kBatch; ++u)
-        e[u] = cnt > kBatch ? __ldg(lp + (size_t)(kBatch + u) * pl.stride) : 0u;
-    for (int k0 = 0; k0 < cnt; k0 += kBatch) {
-        // entries of batch k0 + kBatch are in e (when it exists): its records,
-        // then the entries of the batch after it, then batch k0's terms
-        const bool next = k0 + kBatch < cnt, after = k0 + 2 * kBatch < cnt;
-#pragma unroll
-        for (int u = 0; u < kBatch; ++u) rn[u] = next ? load_rec(pl.pos, e[u], none) : none;
-#pragma unroll
-        for (int u = 0; u < kBatch; ++u)
-            e[u] = after ? __ldg(lp + (size_t)(k0 + 2 * kBatch + u) * pl.stride) : 0u;
+    auto terms = [&](const Rec* r) {
 #pragma unroll
         for (int u = 0; u < kBatch; ++u) {
             if constexpr (kCompact) {
@@ -285,9 +289,38 @@ force_list_kernel(Body body, DevGeom g, PairList pl, ForceOut out) {
                 body.template eval_list<false>(d0, d1, d2, size, size * size, acc, rmin, err);
             }
         }
-        if ((k0 + kBatch) % kListFold == 0) body.fold(acc);
-#pragma unroll
-        for (int u = 0; u < kBatch; ++u) r[u] = rn[u];
+    };
+    // groups of 8 entries (one 32-byte load) one group ahead; records one
+    // batch of 4 ahead of their pair terms
+    const uint4* gp = reinterpret_cast<const uint4*>(pl.list + (size_t)s * kListFold);
+    const size_t gstride = (size_t)pl.stride * kListFold / 4;   // uint4 per group row
+    uint4 ea = make_uint4(0u, 0u, 0u, 0u), eb = ea;
+    Rec r[kBatch], rn[kBatch];
+    if (cnt > 0) {
+        ea = __ldg(gp);
+        eb = __ldg(gp + 1);
+    }
+    r[0] = cnt > 0 ? load_rec(pl.pos, ea.x, none) : none;
+    r[1] = cnt > 0 ? load_rec(pl.pos, ea.y, none) : none;
+    r[2] = cnt > 0 ? load_rec(pl.pos, ea.z, none) : none;
+    r[3] = cnt > 0 ? load_rec(pl.pos, ea.w, none) : none;
+    for (int k0 = 0; k0 < cnt; k0 += kListFold) {
+        const bool more = k0 + kListFold < cnt;
+        gp += gstride;
+        const uint4 na = more ? __ldg(gp) : make_uint4(0u, 0u, 0u, 0u);
+        const uint4 nb = more ? __ldg(gp + 1) : make_uint4(0u, 0u, 0u, 0u);
+        rn[0] = load_rec(pl.pos, eb.x, none);
+        rn[1] = load_rec(pl.pos, eb.y, none);
+        rn[2] = load_rec(pl.pos, eb.z, none);
+        rn[3] = load_rec(pl.pos, eb.w, none);
+        terms(r);
+        r[0] = more ? load_rec(pl.pos, na.x, none) : none;
+        r[1] = more ? load_rec(pl.pos, na.y, none) : none;
+        r[2] = more ? load_rec(pl.pos, na.z, none) : none;
+        r[3] = more ? load_rec(pl.pos, na.w, none) : none;
+        terms(rn);
+        body.fold(acc);
+        eb = nb;
     }
     if (kCompact) body.list_overlap(rmin, us2, err);
     body.store(out, f, acc);
