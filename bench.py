@@ -125,7 +125,7 @@ class ClockSampler:
 
 # the dominant kernel of the mixed step and the ncu summary that gives its
 # DRAM traffic per launch (a line "dram_bytes_per_launch: B")
-FORCE_KERNEL = "force_list_kernel<MixedBody<LJFixed<6>>>"
+FORCE_KERNEL = "force_list_kernel<MixedBody<LJPure<6>>, 1>"
 FORCE_PROFILE = os.path.join(ROOT, "profiles", "force_list_lj_rho0.8_n2e20.txt")
 
 
