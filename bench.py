@@ -421,8 +421,10 @@ def run_gpu(args):
     s.step(max(args.warmup, 3))          # W >= 3 untimed warm-up steps (melting the lattice)
     if dist:
         dist.barrier()
+    builds0 = s.list_builds()
     with ClockSampler(dev) as clk:
         ms = s.time_steps(args.steps)
+    builds_timed = s.list_builds() - builds0
     if dist:
         import torch
         t = torch.tensor([ms], dtype=torch.float64)
@@ -502,7 +504,7 @@ def run_gpu(args):
         "e2e": {"value": e2e_v, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "steps": e2e_steps,
                 "path": "force_evaluate -> next_system -> cells_build on pinned host arrays"},
-        "gpu_launches": args.steps * s.launches_per_step(),
+        "gpu_launches": args.steps * s.launches_per_step() + builds_timed * s.launches_per_rebuild(),
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak,
                      "unit": "TFLOP/s", "frac": achieved / fp32_peak,
                      "traffic": profiled_traffic(FORCE_PROFILE),

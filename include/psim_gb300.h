@@ -409,6 +409,10 @@ int psim_system_profile(psim_system* sys, int32_t n_steps, double* out_ms);
 
 /* Number of kernel launches one step issues (for launch accounting). */
 int psim_system_launches_per_step(psim_system* sys);
+/* Kernel launches of a step's pair-list rebuild (0 without a pair list): with
+ * a pair list a step launches psim_system_launches_per_step kernels, and the
+ * steps that rebuild the list this many more. */
+int psim_system_launches_per_rebuild(psim_system* sys);
 
 /* Occupancy of the current cell list: max and mean particles per cell. */
 int psim_system_cell_occupancy(psim_system* sys, int32_t* max_occ, double* mean_occ);

@@ -149,6 +149,7 @@ def lib():
             "psim_system_forces": ([P, P], C.c_int),
             "psim_system_profile": ([P, C.c_int32, P], C.c_int),
             "psim_system_launches_per_step": ([P], C.c_int),
+            "psim_system_launches_per_rebuild": ([P], C.c_int),
             "psim_system_cell_occupancy": ([P, C.POINTER(C.c_int32), C.POINTER(C.c_double)], C.c_int),
             "psim_system_time_steps": ([P, C.c_int32, C.POINTER(C.c_double)], C.c_int),
             "psim_system_pair_count": ([P, C.c_double, C.POINTER(C.c_double)], C.c_int),
@@ -503,6 +504,9 @@ class System:
 
     def launches_per_step(self):
         return lib().psim_system_launches_per_step(self._h)
+
+    def launches_per_rebuild(self):
+        return lib().psim_system_launches_per_rebuild(self._h)
 
     def cell_occupancy(self):
         m, a = C.c_int32(), C.c_double()

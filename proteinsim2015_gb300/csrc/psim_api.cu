@@ -794,6 +794,13 @@ struct psim_system {
     int lcap = 0, hcap = 0;
     float lpre = 0.f, ldisp2 = 0.f, hr = 0.f;
     DevBuf lslot[2], lbuild, lpos, list, lcount, lflag, lhalo, lhcount;
+    // With a pair list the cell list is rebuilt only with the list (the
+    // storage order then stays the list order between builds): the state is
+    // carried into the new order through pscratch (15 n doubles), and the
+    // per-slot arrays live in buffer 0 (buffer 1 receives a new order or the
+    // cell view of the current positions that refresh_cells computes).
+    DevBuf pscratch;
+    cudaGraphConditionalHandle cond = 0;   // the rebuild's conditional node (graph capture)
     // compact 16-byte records when every particle has one radius (set by the upload)
     int lcompact = 0;
     float lradius = 0.f, lunit = 0.f;
@@ -869,14 +876,150 @@ cudaError_t enqueue_force(psim_system* s, const Phase& ph, const ForceOut& fo) {
     }
     if (s->cfg.precision == PSIM_PRECISION_FP64) return launch_forces_fp64(s->fs, s->g, cv, fo, s->st);
     if (s->list_on) {
-        PairList pl{s->lslot[ph.ob].as<int>(), s->lpos.as<float4>(), s->lcount.as<int>(),
+        // the storage order is the list order: no slot table
+        PairList pl{nullptr, s->lpos.as<float4>(), s->lcount.as<int>(),
                     s->list.as<uint32_t>(), s->n, s->lcompact, s->lradius, s->lunit};
         return launch_forces_list(s->fs, s->g, pl, fo, s->st);
     }
     return launch_forces_mixed(s->fs, s->g, cv, fo, s->st);
 }
 
+// ---- the step with a pair list: the cell list is rebuilt with the list only
+//
+// force (list) -> vGB (no permutation, no hash) -> step end, then, on the
+// steps whose integrator raised the rebuild flag, the rebuild: hash + count,
+// scan, scatter, canonicalisation into the new cell order (list records and
+// halo images included), the state carried into that order, the list build.
+// In a graph the rebuild is the body of a conditional node that the step end
+// sets; so a step without a rebuild launches three kernels.  The forces and
+// the trajectory are those of the cell list rebuilt every step: the same
+// pair terms in the same list order, the same per-particle arithmetic.
+
+// The rebuild after step t (phase of t): the state the integrator wrote (in
+// the storage order) sorted into the new cell order.
+int enqueue_rebuild_lazy(psim_system* s, long long t) {
+    const Phase ph = phase_of(t);
+    const int n = s->n, nsb = 1 - ph.sb;
+    cudaStream_t st = s->st;
+    uint32_t* err = s->err.as<uint32_t>();
+    PSIM_CUDA(cudaMemsetAsync(s->count[0].p, 0, 4 * (size_t)s->ncell, st));
+    PSIM_CUDA(launch_hash_count(n, d3(s->pos[nsb], n, 0), d3(s->pos[nsb], n, 1),
+                                d3(s->pos[nsb], n, 2), s->g, s->key.as<int>(), s->rank.as<int>(),
+                                s->count[0].as<int>(), err, st));
+    PSIM_CUDA(launch_scan(s->count[0].as<int>(), s->start.as<int>(), s->ncell,
+                          s->scratch.as<int>(), st));
+    PSIM_CUDA(launch_scatter(n, s->key.as<int>(), s->rank.as<int>(), s->start.as<int>(),
+                             s->tmp.as<int>(), err, st));
+    CanonArgs ca{};
+    ca.n = n;
+    ca.tmp = s->tmp.as<int>();
+    ca.key = s->key.as<int>();
+    ca.start = s->start.as<int>();
+    ca.count = s->count[0].as<int>();
+    ca.tag_in = s->tag[0].as<int>();
+    ca.radius_in = s->radius[0].as<double>();
+    ca.inv_mass_in = s->inv_mass[0].as<double>();
+    ca.x = d3(s->pos[nsb], n, 0); ca.y = d3(s->pos[nsb], n, 1); ca.z = d3(s->pos[nsb], n, 2);
+    ca.perm = s->perm[0].as<int>();
+    ca.tag_out = s->tag[1].as<int>();
+    ca.radius_out = s->radius[1].as<double>();
+    ca.inv_mass_out = s->inv_mass[1].as<double>();
+    ca.cellid = s->cellid.as<int>();
+    ca.posh = s->posh.as<float4>();
+    ca.vel_freq = s->vp.vel_freq;
+    ca.err = err;
+    set_halo_args(s, ca);   // list records, build positions and halo images on the new order
+    PSIM_CUDA(launch_canonicalize(ca, st));
+    // the state into the new order: positions, previous positions, noise
+    // memory, and the forces of this step and the one before
+    DevBuf* arrs[5] = {&s->pos[nsb], &s->pos0[nsb], &s->mem[nsb], &s->frc[ph.fcur],
+                       &s->frc[ph.fprev]};
+    PermuteArgs pa{};
+    pa.n = n;
+    pa.perm = s->perm[0].as<int>();
+    pa.narr = 15;
+    double* scr = s->pscratch.as<double>();
+    for (int a = 0; a < 5; ++a)
+        for (int k = 0; k < 3; ++k) {
+            pa.src[3 * a + k] = d3(*arrs[a], n, k);
+            pa.dst[3 * a + k] = scr + (size_t)(3 * a + k) * n;
+        }
+    PSIM_CUDA(launch_permute(pa, err, st));
+    for (int a = 0; a < 5; ++a)
+        PSIM_CUDA(cudaMemcpyAsync(arrs[a]->p, scr + (size_t)3 * a * n, 24 * (size_t)n,
+                                  cudaMemcpyDeviceToDevice, st));
+    PSIM_CUDA(cudaMemcpyAsync(s->tag[0].p, s->tag[1].p, 4 * (size_t)n, cudaMemcpyDeviceToDevice, st));
+    PSIM_CUDA(cudaMemcpyAsync(s->radius[0].p, s->radius[1].p, 8 * (size_t)n,
+                              cudaMemcpyDeviceToDevice, st));
+    PSIM_CUDA(cudaMemcpyAsync(s->inv_mass[0].p, s->inv_mass[1].p, 8 * (size_t)n,
+                              cudaMemcpyDeviceToDevice, st));
+    PSIM_CUDA(enqueue_list_build(s, 0, nullptr));
+    return PSIM_OK;
+}
+
+// Step t with a pair list.  In a graph (evs null) this enqueues the force
+// pass, the integrator and the step end; the caller adds the conditional
+// rebuild.  Timed directly (evs: 4 events), the rebuild decision is read back.
+int enqueue_step_lazy(psim_system* s, long long t, cudaEvent_t* evs) {
+    const Phase ph = phase_of(t);
+    const int n = s->n, sb = ph.sb, nsb = 1 - ph.sb;
+    cudaStream_t st = s->st;
+    int* lflag = s->lflag.as<int>() + (t & 1);
+    if (evs) PSIM_CUDA(cudaEventRecord(evs[0], st));
+    ForceOut fo{d3(s->frc[ph.fcur], n, 0), d3(s->frc[ph.fcur], n, 1), d3(s->frc[ph.fcur], n, 2),
+                s->err.as<uint32_t>(), nullptr};
+    PSIM_CUDA(enqueue_force(s, ph, fo));
+    if (evs) PSIM_CUDA(cudaEventRecord(evs[1], st));
+    VgbSystemArgs a{};
+    a.n = n;
+    a.perm = nullptr;   // the storage order has not changed since the last rebuild
+    a.tag = s->tag[0].as<int>();
+    a.inv_mass = s->inv_mass[0].as<double>();
+    a.x = d3(s->pos[sb], n, 0); a.y = d3(s->pos[sb], n, 1); a.z = d3(s->pos[sb], n, 2);
+    a.x0 = d3(s->pos0[sb], n, 0); a.y0 = d3(s->pos0[sb], n, 1); a.z0 = d3(s->pos0[sb], n, 2);
+    a.mx = d3(s->mem[sb], n, 0); a.my = d3(s->mem[sb], n, 1); a.mz = d3(s->mem[sb], n, 2);
+    a.fx = fo.fx; a.fy = fo.fy; a.fz = fo.fz;
+    a.gx = d3(s->frc[ph.fprev], n, 0); a.gy = d3(s->frc[ph.fprev], n, 1);
+    a.gz = d3(s->frc[ph.fprev], n, 2);
+    a.vel = s->vel.as<double>();
+    a.ox = d3(s->pos[nsb], n, 0); a.oy = d3(s->pos[nsb], n, 1); a.oz = d3(s->pos[nsb], n, 2);
+    a.ox0 = d3(s->pos0[nsb], n, 0); a.oy0 = d3(s->pos0[nsb], n, 1); a.oz0 = d3(s->pos0[nsb], n, 2);
+    a.omx = d3(s->mem[nsb], n, 0); a.omy = d3(s->mem[nsb], n, 1); a.omz = d3(s->mem[nsb], n, 2);
+    a.count = nullptr;  // no hash: the cell list is rebuilt with the list
+    a.err = s->err.as<uint32_t>();
+    a.state = s->state.as<StepState>();
+    a.lslot = nullptr;  // list slot = storage slot
+    a.lbuild = s->lbuild.as<float4>();
+    a.lpos = s->lpos.as<float4>();
+    a.linv_unit = s->lcompact ? 1.0f / s->lunit : 0.f;
+    a.lflag_set = lflag;
+    a.lflag_clear = s->lflag.as<int>() + (1 - (t & 1));
+    a.ldisp2 = s->ldisp2;
+    a.lhalo = s->lhalo.as<int>();
+    a.lhcount = s->lhcount.as<int>();
+    a.img = s->img.as<int>();
+    NoiseView nz{s->cfg.noise_mode, s->noise.as<double>(), s->noise_first, s->noise_steps};
+    PSIM_CUDA(launch_vgb_system_fast(a, s->vp, s->g, nz, st));
+    if (evs) PSIM_CUDA(cudaEventRecord(evs[2], st));
+    PSIM_CUDA(launch_step_end(s->state.as<StepState>(), lflag, s->err.as<uint32_t>(),
+                              s->vp.vel_freq, s->cond, evs ? 0 : 1, st));
+    if (evs) {
+        int flag = 0;
+        uint32_t bits = 0;
+        PSIM_CUDA(cudaMemcpyAsync(&flag, lflag, 4, cudaMemcpyDeviceToHost, st));
+        PSIM_CUDA(cudaMemcpyAsync(&bits, s->err.p, 4, cudaMemcpyDeviceToHost, st));
+        PSIM_CUDA(cudaStreamSynchronize(st));
+        if (flag && !bits) {
+            const int rc = enqueue_rebuild_lazy(s, t);
+            if (rc) return rc;
+        }
+        PSIM_CUDA(cudaEventRecord(evs[3], st));
+    }
+    return PSIM_OK;
+}
+
 int enqueue_step(psim_system* s, long long t, cudaEvent_t* evs) {
+    if (s->list_on) return enqueue_step_lazy(s, t, evs);
     const Phase ph = phase_of(t);
     const int n = s->n;
     cudaStream_t st = s->st;
@@ -973,8 +1116,67 @@ int enqueue_step(psim_system* s, long long t, cudaEvent_t* evs) {
     return PSIM_OK;
 }
 
+// The step graph with a pair list: the step, then a conditional node (set by
+// the step end) whose body is the rebuild.
+int graph_for_lazy(psim_system* s, int phase, cudaGraphExec_t* out) {
+    cudaGraph_t g = nullptr;
+    PSIM_CUDA(cudaGraphCreate(&g, 0));
+    auto done = [&](int rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    };
+    cudaError_t e = cudaGraphConditionalHandleCreate(&s->cond, g, 0, cudaGraphCondAssignDefault);
+    if (e != cudaSuccess)
+        return done(fail(PSIM_ERR_CUDA, "conditional handle: %s", cudaGetErrorString(e)));
+    e = cudaStreamBeginCaptureToGraph(s->st, g, nullptr, nullptr, 0,
+                                      cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return done(fail(PSIM_ERR_CUDA, "capture: %s", cudaGetErrorString(e)));
+    int rc = enqueue_step_lazy(s, phase, nullptr);
+    cudaGraphNodeParams cp{};
+    if (!rc) {
+        cudaStreamCaptureStatus cs;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t nd = 0;
+        cudaGraph_t cg = nullptr;
+        e = cudaStreamGetCaptureInfo(s->st, &cs, nullptr, &cg, &deps, nullptr, &nd);
+        cudaGraphNode_t cn = nullptr;
+        if (e == cudaSuccess) {
+            cp.type = cudaGraphNodeTypeConditional;
+            cp.conditional.handle = s->cond;
+            cp.conditional.type = cudaGraphCondTypeIf;
+            cp.conditional.size = 1;
+            std::vector<cudaGraphNode_t> dv(deps, deps + nd);
+            e = cudaGraphAddNode(&cn, cg, dv.data(), nullptr, dv.size(), &cp);
+        }
+        if (e == cudaSuccess)
+            e = cudaStreamUpdateCaptureDependencies(s->st, &cn, nullptr, 1,
+                                                    cudaStreamSetCaptureDependencies);
+        if (e != cudaSuccess) rc = fail(PSIM_ERR_CUDA, "conditional node: %s", cudaGetErrorString(e));
+    }
+    cudaGraph_t captured = g;
+    e = cudaStreamEndCapture(s->st, &captured);
+    if (rc) return done(rc);
+    if (e != cudaSuccess) return done(fail(PSIM_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e)));
+    // the body: the rebuild, captured into the node's own graph
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    e = cudaStreamBeginCaptureToGraph(s->st, body, nullptr, nullptr, 0,
+                                      cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return done(fail(PSIM_ERR_CUDA, "capture: %s", cudaGetErrorString(e)));
+    rc = enqueue_rebuild_lazy(s, phase);
+    cudaGraph_t bcap = body;
+    e = cudaStreamEndCapture(s->st, &bcap);
+    if (rc) return done(rc);
+    if (e != cudaSuccess) return done(fail(PSIM_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e)));
+    e = cudaGraphInstantiate(&s->graph[phase], g, 0);
+    if (e != cudaSuccess)
+        return done(fail(PSIM_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e)));
+    *out = s->graph[phase];
+    return done(PSIM_OK);
+}
+
 int graph_for(psim_system* s, int phase, cudaGraphExec_t* out) {
     if (s->graph[phase]) { *out = s->graph[phase]; return PSIM_OK; }
+    if (s->list_on) return graph_for_lazy(s, phase, out);
     cudaGraph_t g = nullptr;
     PSIM_CUDA(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal));
     int rc = enqueue_step(s, phase, nullptr);
@@ -1012,6 +1214,72 @@ int settle(psim_system* s) {
         s->latched = bits;
         return fail(code_from_bits(bits), "step %lld: %s", ss.step, bits_text(bits));
     }
+    return PSIM_OK;
+}
+
+// The tags of the storage order (the order of the state arrays) after the
+// steps taken: the previous cell order, or with a pair list the order of the
+// last rebuild.
+const int* store_tags(psim_system* s) {
+    if (s->list_on) return s->tag[0].as<int>();
+    return s->tag[1 - phase_of(s->total).ob].as<int>();
+}
+// The permutation from the storage order to the order of the force two steps
+// back (null: the same order).
+const int* prev_perm(psim_system* s) {
+    return s->list_on ? nullptr : s->perm[1 - phase_of(s->total).pb].as<int>();
+}
+
+// A cell list of the current positions: per cell-order slot its storage slot,
+// tag and radius, and the counts per cell (with start and cellid in the
+// system's buffers).
+struct CellRefs {
+    const int* perm;
+    const int* tag;
+    const double* radius;
+    const int* count;
+};
+// Without a pair list: the one the last step built.  With one, the stored cell
+// list is that of the last rebuild, so it is computed afresh into buffer 1
+// from the current positions; the system's order, list and state are left
+// alone (the float positions posh it rewrites are read only by a rebuild,
+// after rewriting them).
+int cell_refs(psim_system* s, CellRefs& c) {
+    const Phase ph = phase_of(s->total);
+    if (!s->list_on) {
+        c = CellRefs{s->perm[ph.pb].as<int>(), s->tag[ph.ob].as<int>(),
+                     s->radius[ph.ob].as<double>(), s->count[ph.cb].as<int>()};
+        return PSIM_OK;
+    }
+    const int n = s->n;
+    cudaStream_t st = s->st;
+    uint32_t* err = s->err.as<uint32_t>();
+    PSIM_CUDA(cudaMemsetAsync(s->count[0].p, 0, 4 * (size_t)s->ncell, st));
+    PSIM_CUDA(launch_hash_count(n, d3(s->pos[ph.sb], n, 0), d3(s->pos[ph.sb], n, 1),
+                                d3(s->pos[ph.sb], n, 2), s->g, s->key.as<int>(), s->rank.as<int>(),
+                                s->count[0].as<int>(), err, st));
+    PSIM_CUDA(launch_scan(s->count[0].as<int>(), s->start.as<int>(), s->ncell,
+                          s->scratch.as<int>(), st));
+    PSIM_CUDA(launch_scatter(n, s->key.as<int>(), s->rank.as<int>(), s->start.as<int>(),
+                             s->tmp.as<int>(), err, st));
+    CanonArgs ca{};
+    ca.n = n;
+    ca.tmp = s->tmp.as<int>();
+    ca.key = s->key.as<int>();
+    ca.start = s->start.as<int>();
+    ca.count = s->count[0].as<int>();
+    ca.tag_in = s->tag[0].as<int>();
+    ca.radius_in = s->radius[0].as<double>();
+    ca.x = d3(s->pos[ph.sb], n, 0); ca.y = d3(s->pos[ph.sb], n, 1); ca.z = d3(s->pos[ph.sb], n, 2);
+    ca.perm = s->perm[1].as<int>();
+    ca.tag_out = s->tag[1].as<int>();
+    ca.radius_out = s->radius[1].as<double>();
+    ca.cellid = s->cellid.as<int>();
+    ca.posh = s->posh.as<float4>();
+    ca.err = err;
+    PSIM_CUDA(launch_canonicalize(ca, st));
+    c = CellRefs{s->perm[1].as<int>(), s->tag[1].as<int>(), s->radius[1].as<double>(),
+                 s->count[0].as<int>()};
     return PSIM_OK;
 }
 
@@ -1241,6 +1509,7 @@ psim_system* system_new(const psim_system_config* cfg, const DevGeom& g) {
              !s->lpos.ensure(32 * (n + 1 + (size_t)s->hcap)) &&
              !s->list.ensure(4 * n * (size_t)(s->lcap + kListFold)) && !s->lcount.ensure(4 * n) &&
              !s->lflag.ensure(8) && !s->lhalo.ensure(4 * n) && !s->lhcount.ensure(4) &&
+             !s->pscratch.ensure(15 * 8 * (size_t)n) &&
              cudaMemset(s->lflag.p, 0, 8) == cudaSuccess &&
              cudaMemset(s->lhcount.p, 0, 4) == cudaSuccess;
     }
@@ -1267,7 +1536,7 @@ void psim_system_destroy(psim_system* s) {
     DevBuf* arrs[] = {&s->cellid, &s->key, &s->rank, &s->tmp, &s->start, &s->scratch, &s->posd,
                       &s->posh, &s->posl, &s->vel, &s->err, &s->state, &s->occ, &s->noise,
                       &s->snap, &s->lslot[0], &s->lslot[1], &s->lbuild, &s->lpos, &s->list,
-                      &s->lcount, &s->lflag, &s->lhalo, &s->lhcount, &s->b_tasks,
+                      &s->lcount, &s->lflag, &s->lhalo, &s->lhcount, &s->pscratch, &s->b_tasks,
                       &s->b_geoms, &s->b_pairs, &s->b_pre, &s->b_rep, &s->b_seeds,
                       &s->img, &s->track_start};
     for (DevBuf* b : arrs) b->release();
@@ -1377,20 +1646,32 @@ int psim_system_upload(psim_system* s, const double* pos, const double* pos0, co
         PSIM_CUDA(cudaMemcpyAsync(grec, ghost, compact ? 16 : 32, cudaMemcpyHostToDevice, st));
     }
     if (s->list_on) {
-        // the first list, on the first cell order: flag 0 raised for the
-        // build, lowered for step 0 (whose integrator raises it when needed)
-        const int one = 1;
+        // the first list, on the first cell order (the list slots are the
+        // storage slots: the state is carried into that order below)
         PSIM_CUDA(cudaMemsetAsync(s->lflag.p, 0, 8, st));
-        PSIM_CUDA(cudaMemcpyAsync(s->lflag.p, &one, 4, cudaMemcpyHostToDevice, st));
-        ca.rebuild = s->lflag.as<int>();
-        ca.lslot_out = s->lslot[ob].as<int>();
         set_halo_args(s, ca);
         PSIM_CUDA(cudaMemsetAsync(s->lhcount.p, 0, 4, st));
     }
     PSIM_CUDA(launch_canonicalize(ca, st));
     if (s->list_on) {
-        PSIM_CUDA(enqueue_list_build(s, ph.cb, s->lflag.as<int>()));
-        PSIM_CUDA(cudaMemsetAsync(s->lflag.p, 0, 8, st));
+        // the uploaded state (original order) into the first cell order
+        DevBuf* arrs[5] = {&s->pos[sb], &s->pos0[sb], &s->mem[sb], &s->frc[ph.fprev],
+                           &s->frc[(ph.fprev + 2) % 3]};
+        PermuteArgs pa{};
+        pa.n = n;
+        pa.perm = s->perm[pb].as<int>();
+        pa.narr = 15;
+        double* scr = s->pscratch.as<double>();
+        for (int a = 0; a < 5; ++a)
+            for (int k = 0; k < 3; ++k) {
+                pa.src[3 * a + k] = d3(*arrs[a], n, k);
+                pa.dst[3 * a + k] = scr + (size_t)(3 * a + k) * n;
+            }
+        PSIM_CUDA(launch_permute(pa, s->err.as<uint32_t>(), st));
+        for (int a = 0; a < 5; ++a)
+            PSIM_CUDA(cudaMemcpyAsync(arrs[a]->p, scr + (size_t)3 * a * n, 24 * (size_t)n,
+                                      cudaMemcpyDeviceToDevice, st));
+        PSIM_CUDA(enqueue_list_build(s, ph.cb, nullptr));
     }
     uint32_t bits = 0;
     PSIM_CUDA(cudaMemcpyAsync(&bits, s->err.p, 4, cudaMemcpyDeviceToHost, st));
@@ -1471,7 +1752,7 @@ int psim_system_download(psim_system* s, double* pos, double* pos0, double* vel,
     const size_t b = 24 * (size_t)n;
     cudaStream_t st = s->st;
     // storage order is the previous cell order: its tags are tag[1 - ob]
-    const int* tg = s->tag[1 - ph.ob].as<int>();
+    const int* tg = store_tags(s);
     ScopedBuf stage;
     PSIM_CUDA(stage.ensure(b));
     auto get3 = [&](DevBuf& src, const int* perm, double* dst) -> int {
@@ -1486,7 +1767,7 @@ int psim_system_download(psim_system* s, double* pos, double* pos0, double* vel,
     if ((rc = get3(s->pos0[ph.sb], nullptr, pos0))) return rc;
     if ((rc = get3(s->frc[ph.fprev], nullptr, frc))) return rc;
     // frc0 is the force of two orders back, reached through the previous permutation
-    if ((rc = get3(s->frc[(ph.fprev + 2) % 3], s->perm[1 - ph.pb].as<int>(), frc0))) return rc;
+    if ((rc = get3(s->frc[(ph.fprev + 2) % 3], prev_perm(s), frc0))) return rc;
     if (vel) {
         PSIM_CUDA(cudaMemcpyAsync(vel, s->vel.p, b, cudaMemcpyDeviceToHost, st));
         PSIM_CUDA(cudaStreamSynchronize(st));
@@ -1509,17 +1790,18 @@ int psim_system_download_cells(psim_system* s, int32_t* hash_index, uint32_t* cs
     PSIM_CUDA(hb.ensure(8 * (size_t)n));
     PSIM_CUDA(cb.ensure(8 * (size_t)s->ncell));
     PSIM_CUDA(sb.ensure(32 * (size_t)n));
+    CellRefs c;
+    if ((rc = cell_refs(s, c))) return rc;
     const double4_32a* posd = s->posd.as<double4_32a>();
     if (s->cfg.precision != PSIM_PRECISION_FP64) {
         // the mixed form keeps no FP64 sorted copy: gather one from the storage order
         PSIM_CUDA(pd.ensure(32 * (size_t)n));
-        PSIM_CUDA(launch_gather_posd(n, s->perm[ph.pb].as<int>(), d3(s->pos[ph.sb], n, 0),
-                                     d3(s->pos[ph.sb], n, 1), d3(s->pos[ph.sb], n, 2),
-                                     s->radius[ph.ob].as<double>(), pd.as<double4_32a>(), st));
+        PSIM_CUDA(launch_gather_posd(n, c.perm, d3(s->pos[ph.sb], n, 0), d3(s->pos[ph.sb], n, 1),
+                                     d3(s->pos[ph.sb], n, 2), c.radius, pd.as<double4_32a>(), st));
         posd = pd.as<double4_32a>();
     }
-    PSIM_CUDA(launch_export_cells(n, s->ncell, s->cellid.as<int>(), s->tag[ph.ob].as<int>(), posd,
-                                  s->start.as<int>(), s->count[ph.cb].as<int>(),
+    PSIM_CUDA(launch_export_cells(n, s->ncell, s->cellid.as<int>(), c.tag, posd,
+                                  s->start.as<int>(), c.count,
                                   hb.as<int32_t>(), cb.as<uint32_t>(), sb.as<double>(), st));
     if (hash_index)
         PSIM_CUDA(cudaMemcpyAsync(hash_index, hb.p, 8 * (size_t)n, cudaMemcpyDeviceToHost, st));
@@ -1540,7 +1822,7 @@ int psim_system_snapshot_async(psim_system* s, double* host_pos) {
     // the previous snapshot's copy must have left the staging buffer
     if (s->snap_pending) PSIM_CUDA(cudaStreamWaitEvent(s->st, s->ev_snap_done, 0));
     PSIM_CUDA(launch_merge_xyz(n, d3(s->pos[ph.sb], n, 0), d3(s->pos[ph.sb], n, 1),
-                               d3(s->pos[ph.sb], n, 2), s->tag[1 - ph.ob].as<int>(), nullptr,
+                               d3(s->pos[ph.sb], n, 2), store_tags(s), nullptr,
                                s->snap.as<double>(), s->st));
     PSIM_CUDA(cudaEventRecord(s->ev_snap_ready, s->st));
     PSIM_CUDA(cudaStreamWaitEvent(s->side, s->ev_snap_ready, 0));
@@ -1583,7 +1865,10 @@ int psim_system_forces(psim_system* s, double* force) {
     ForceOut fo{f3.as<double>(), f3.as<double>() + n, f3.as<double>() + 2 * (size_t)n,
                 s->err.as<uint32_t>(), nullptr};
     PSIM_CUDA(enqueue_force(s, ph, fo));
-    PSIM_CUDA(launch_unsort_force(n, s->tag[ph.ob].as<int>(), fo.fx, fo.fy, fo.fz,
+    // the pass writes in its order: the next cell order, or with a pair list
+    // the storage order
+    PSIM_CUDA(launch_unsort_force(n, s->list_on ? store_tags(s) : s->tag[ph.ob].as<int>(),
+                                  fo.fx, fo.fy, fo.fz,
                                   out.as<double>(), s->st));
     PSIM_CUDA(cudaMemcpyAsync(force, out.p, 24 * (size_t)n, cudaMemcpyDeviceToHost, s->st));
     return settle(s);
@@ -1611,8 +1896,8 @@ int reduce(psim_system* s, ObserveArgs& a, double* out) {
     a.fz = d3(s->frc[ph.fprev], n, 2);
     const int fb = (ph.fprev + 2) % 3;
     a.gx = d3(s->frc[fb], n, 0); a.gy = d3(s->frc[fb], n, 1); a.gz = d3(s->frc[fb], n, 2);
-    a.perm_prev = s->perm[1 - ph.pb].as<int>();
-    a.tag = s->tag[1 - ph.ob].as<int>();   // the storage order's tags (as download)
+    a.perm_prev = prev_perm(s);
+    a.tag = store_tags(s);   // the storage order's tags (as download)
     a.L = s->g.L;
     ScopedBuf scratch, res;
     PSIM_CUDA(scratch.ensure(8 * (size_t)observe_scratch_doubles()));
@@ -1629,15 +1914,17 @@ int sorted_view(psim_system* s, ScopedBuf& pd, PairScanArgs& a) {
     if (s->n_reps) return fail(PSIM_ERR_INPUT, "pair observables are per system, not per batch");
     const Phase ph = phase_of(s->total);
     PSIM_CUDA(pd.ensure(32 * (size_t)s->n));
-    PSIM_CUDA(launch_gather_posd(s->n, s->perm[ph.pb].as<int>(), d3(s->pos[ph.sb], s->n, 0),
+    CellRefs c;
+    if (int rc = cell_refs(s, c)) return rc;
+    PSIM_CUDA(launch_gather_posd(s->n, c.perm, d3(s->pos[ph.sb], s->n, 0),
                                  d3(s->pos[ph.sb], s->n, 1), d3(s->pos[ph.sb], s->n, 2),
-                                 s->radius[ph.ob].as<double>(), pd.as<double4_32a>(), s->st));
+                                 c.radius, pd.as<double4_32a>(), s->st));
     a.g = s->g;
     a.posd = pd.as<double4_32a>();
     a.cellid = s->cellid.as<int>();
     a.cstart = s->start.as<int>();
-    a.ccount = s->count[ph.cb].as<int>();
-    a.tag = s->tag[ph.ob].as<int>();
+    a.ccount = c.count;
+    a.tag = c.tag;
     return PSIM_OK;
 }
 
@@ -1710,7 +1997,7 @@ int psim_system_track_start(psim_system* s) {
     const Phase ph = phase_of(s->total);
     PSIM_CUDA(cudaMemsetAsync(s->img.p, 0, 12 * (size_t)s->n, s->st));
     PSIM_CUDA(launch_merge_xyz(s->n, d3(s->pos[ph.sb], s->n, 0), d3(s->pos[ph.sb], s->n, 1),
-                               d3(s->pos[ph.sb], s->n, 2), s->tag[1 - ph.ob].as<int>(), nullptr,
+                               d3(s->pos[ph.sb], s->n, 2), store_tags(s), nullptr,
                                s->track_start.as<double>(), s->st));
     PSIM_CUDA(cudaStreamSynchronize(s->st));
     return PSIM_OK;
@@ -1862,9 +2149,16 @@ int psim_system_profile(psim_system* s, int32_t n_steps, double* out_ms) {
 }
 
 int psim_system_launches_per_step(psim_system* s) {
-    // force, vGB, scan x3, scatter, canonicalise (+1 memset node); the
-    // pair-list build (which returns at once unless the list is due)
-    return (s && s->list_on) ? 8 : 7;
+    // force, vGB, scan x3, scatter, canonicalise (+1 memset node); with a
+    // pair list: force, vGB, step end (the rebuild's kernels run on the
+    // steps that rebuild: psim_system_launches_per_rebuild)
+    return (s && s->list_on) ? 3 : 7;
+}
+
+int psim_system_launches_per_rebuild(psim_system* s) {
+    // hash + count, scan x3, scatter, canonicalise, state permutation, list
+    // build (+ memset and copy nodes)
+    return (s && s->list_on) ? 8 : 0;
 }
 
 int psim_system_cell_occupancy(psim_system* s, int32_t* max_occ, double* mean_occ) {
@@ -1874,7 +2168,9 @@ int psim_system_cell_occupancy(psim_system* s, int32_t* max_occ, double* mean_oc
     if (rc && rc != code_from_bits(s->latched)) return rc;
     const Phase ph = phase_of(s->total);
     PSIM_CUDA(cudaMemsetAsync(s->occ.p, 0, 4, s->st));
-    PSIM_CUDA(launch_occupancy(s->ncell, s->count[ph.cb].as<int>(), s->occ.as<int>(), s->st));
+    CellRefs c;
+    if ((rc = cell_refs(s, c))) return rc;
+    PSIM_CUDA(launch_occupancy(s->ncell, c.count, s->occ.as<int>(), s->st));
     int mx = 0;
     PSIM_CUDA(cudaMemcpyAsync(&mx, s->occ.p, 4, cudaMemcpyDeviceToHost, s->st));
     PSIM_CUDA(cudaStreamSynchronize(s->st));
@@ -1921,11 +2217,13 @@ int psim_system_pair_count(psim_system* s, double cutoff, double* mean_pairs) {
     PSIM_CUDA(cudaMemsetAsync(tot.p, 0, 8, s->st));
     // sorted positions gathered from the FP64 state (with a pair list the
     // float copies are in list order)
-    PSIM_CUDA(launch_gather_posh(s->n, s->perm[ph.pb].as<int>(), d3(s->pos[ph.sb], s->n, 0),
+    CellRefs c;
+    if ((rc = cell_refs(s, c))) return rc;
+    PSIM_CUDA(launch_gather_posh(s->n, c.perm, d3(s->pos[ph.sb], s->n, 0),
                                  d3(s->pos[ph.sb], s->n, 1), d3(s->pos[ph.sb], s->n, 2),
-                                 s->radius[ph.ob].as<double>(), ph4.as<float4>(), s->st));
+                                 c.radius, ph4.as<float4>(), s->st));
     CellView cv{nullptr, ph4.as<float4>(), nullptr, s->cellid.as<int>(), s->start.as<int>(),
-                s->count[ph.cb].as<int>()};
+                c.count};
     PSIM_CUDA(launch_pair_count(s->g, cv, (float)(cutoff * cutoff), tot.as<unsigned long long>(),
                                 s->st));
     unsigned long long h = 0;

@@ -478,6 +478,41 @@ cudaError_t launch_pair_count(const DevGeom& g, const CellView& cv, float rc2,
     return cudaGetLastError();
 }
 
+__global__ void step_end_kernel(StepState* state, const int* lflag, const uint32_t* err,
+                                int vel_freq, cudaGraphConditionalHandle handle, int use_handle) {
+    const int rebuild = (*err == 0 && *lflag != 0) ? 1 : 0;
+    StepState s = *state;
+    if (*err == 0) {
+        // brownianIntegrator's velCounter bookkeeping (brownianIntegrator.cpp:291-292)
+        // runs only after normal steps
+        if (s.step > 0) s.vel_counter = (s.vel_counter == vel_freq) ? 0 : s.vel_counter + 1;
+        s.step += 1;
+        s.list_builds += rebuild;
+        *state = s;
+    }
+    if (use_handle) cudaGraphSetConditional(handle, (unsigned int)rebuild);
+}
+
+cudaError_t launch_step_end(StepState* state, const int* lflag, const uint32_t* err,
+                            int vel_freq, cudaGraphConditionalHandle handle, int use_handle,
+                            cudaStream_t st) {
+    step_end_kernel<<<1, 1, 0, st>>>(state, lflag, err, vel_freq, handle, use_handle);
+    return cudaGetLastError();
+}
+
+__global__ void __launch_bounds__(256) permute_kernel(PermuteArgs a, const uint32_t* err) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= a.n || *err) return;
+    const int o = a.perm[g];
+    for (int k = 0; k < a.narr; ++k) a.dst[k][g] = a.src[k][o];
+}
+
+cudaError_t launch_permute(const PermuteArgs& a, const uint32_t* err, cudaStream_t st) {
+    if (a.n == 0 || a.narr == 0) return cudaSuccess;
+    permute_kernel<<<(a.n + 255) / 256, 256, 0, st>>>(a, err);
+    return cudaGetLastError();
+}
+
 __global__ void __launch_bounds__(256) fma_probe_kernel(int iters, float* sink) {
     float a[8];
 #pragma unroll

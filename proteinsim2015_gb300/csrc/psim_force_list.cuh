@@ -245,7 +245,7 @@ force_list_kernel(Body body, DevGeom g, PairList pl, ForceOut out) {
     static_assert(kListFold == 2 * kBatch, "a fold is two batches");
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= g.n || *out.err) return;
-    const int s = pl.lslot[f];
+    const int s = pl.lslot ? pl.lslot[f] : f;   // no slot table: storage order is list order
     float4 hh, hl;
     // compact records: a neighbour's low part minus the home's comes out of one
     // FMA per axis, fma(2^23 + code, unit, c) with c = -(2^23 + 512) unit - l_i

@@ -69,7 +69,7 @@ cudaError_t launch_forces_mixed(const ForceSetup& fs, const DevGeom& g, const Ce
 constexpr int kListFold = 8;   // pair terms per Kahan fold
 constexpr int kHaloBaseMax = (1 << 25) - 1;   // halo records per system
 struct PairList {
-    const int* lslot;      // list slot of each current storage slot
+    const int* lslot;      // list slot of each current storage slot (null: the same slot)
     // list order, unwrapped, one record per slot (+ the ghost slot n and the
     // halo records): full, pos[2 s] = {x, y, z, R} high parts and pos[2 s + 1]
     // the low parts; or compact (one float4, compact_record, low parts in
@@ -132,7 +132,7 @@ struct NoiseView {
 // and counts them into the next grid.
 struct VgbSystemArgs {
     int n;
-    const int* perm;            // current slot -> previous-order slot
+    const int* perm;            // current slot -> previous-order slot (null: the same)
     const int* tag;             // original index of each current slot
     const double* inv_mass;     // 1/m, current order
     const double* x; const double* y; const double* z;       // previous order
@@ -146,14 +146,15 @@ struct VgbSystemArgs {
     double* omx; double* omy; double* omz;
     int* key;                   // new cell hash, current order
     int* rank;                  // slot inside the new cell (atomic order)
-    int* count;                 // per-cell counts of the next grid (zeroed)
+    int* count;                 // per-cell counts of the next grid (zeroed; null: no hash)
     uint32_t* err;
     const StepState* state;
-    // mixed form with a pair list (lslot null: none).  The new position is
+    // mixed form with a pair list (lbuild null: none).  The new position is
     // also written in list order as the image nearest the list-build position
     // (an exact float pair), and *lflag_set is raised when it lies more than
     // sqrt(ldisp2) from that position; *lflag_clear (the other step parity's
-    // flag) is cleared.
+    // flag) is cleared.  lslot: the list slot of each storage slot (null: the
+    // same slot, when the storage order is the list order).
     const int* lslot;
     const float4* lbuild;       // list order: positions at the build, .w radius
     float4* lpos;               // PairList::pos
@@ -255,6 +256,25 @@ struct CanonArgs {
     float hr, Lf, Lhi, Llo;
 };
 cudaError_t launch_canonicalize(const CanonArgs& a, cudaStream_t st);
+
+// End of a step whose cell list is rebuilt only with its pair list: advances
+// the step state (canonicalize_kernel's bookkeeping) and decides the rebuild
+// -- the flag the integrator raised, unless an error is latched.  In a graph
+// (use_handle) the decision sets the conditional node that runs the rebuild.
+cudaError_t launch_step_end(StepState* state, const int* lflag, const uint32_t* err,
+                            int vel_freq, cudaGraphConditionalHandle handle, int use_handle,
+                            cudaStream_t st);
+
+// dst[k][g] = src[k][perm[g]] for the first narr arrays (the state carried
+// into a new cell order).
+struct PermuteArgs {
+    int n;
+    const int* perm;
+    int narr;
+    const double* src[16];
+    double* dst[16];
+};
+cudaError_t launch_permute(const PermuteArgs& a, const uint32_t* err, cudaStream_t st);
 
 // Reference layout exports.
 cudaError_t launch_export_cells(int n, int ncell, const int* cellid, const int* tag,

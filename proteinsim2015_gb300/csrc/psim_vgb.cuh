@@ -294,7 +294,8 @@ __device__ __forceinline__ void vgb_system_one(const VgbSystemArgs& a, const Vgb
     const int vc = a.state->vel_counter;
     const bool first = (step == 0);
     const bool vel_step = !first && (p.vel_freq == 0 || vc == p.vel_freq);
-    const int o = a.perm[f];
+    // the previous order's slot (no permutation: the order has not changed)
+    const int o = a.perm ? a.perm[f] : f;
     const int tag = a.tag[f];
     const int ntag = tag - g.p0;   // the index within the replica keys its Philox noise
     const double m = a.inv_mass[f];
@@ -306,8 +307,10 @@ __device__ __forceinline__ void vgb_system_one(const VgbSystemArgs& a, const Vgb
     const double F0[3] = {a.gx[o], a.gy[o], a.gz[o]};
     int ls = 0, lhal = 0;
     float4 lb = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (a.lslot) {
-        ls = __ldg(a.lslot + f);
+    if (a.lbuild) {
+        // list slot: carried with the particle, or its storage slot when the
+        // storage order is the list order
+        ls = a.lslot ? __ldg(a.lslot + f) : f;
         lb = __ldg(a.lbuild + ls);
         lhal = __ldg(a.lhalo + ls);
     }
@@ -342,14 +345,16 @@ __device__ __forceinline__ void vgb_system_one(const VgbSystemArgs& a, const Vgb
         a.vel[3 * (size_t)tag + 1] = v[1];
         a.vel[3 * (size_t)tag + 2] = v[2];
     }
-    if (a.lslot) list_position(a, ls, lb, lhal, xn, g);
+    if (a.lbuild) list_position(a, ls, lb, lhal, xn, g);
     if (f == 0 && a.lflag_clear) {
         *a.lflag_clear = 0;
         *a.lhcount = 0;   // halo records are handed out afresh at the next build
     }
-    const int key = hash_pos(xn, g, err);
-    a.key[f] = key;
-    a.rank[f] = atomicAdd(&a.count[key], 1);
+    if (a.count) {   // the next cell list (not when it is rebuilt only with the pair list)
+        const int key = hash_pos(xn, g, err);
+        a.key[f] = key;
+        a.rank[f] = atomicAdd(&a.count[key], 1);
+    }
     if (err) atomicOr(a.err, err);
 }
 
