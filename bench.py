@@ -261,9 +261,9 @@ def cpu_baseline(budget_s=15.0):
             "error": "child failed rc=%d: %s" % (p.returncode, p.stderr[-500:])}
 
 
-def pinned(n):
+def pinned(n, dtype=None):
     import torch
-    return torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+    return torch.empty(n, dtype=dtype or torch.float64, pin_memory=True).numpy()
 
 
 def e2e_dropin(psim, w, state, n_steps):
@@ -281,15 +281,20 @@ def e2e_dropin(psim, w, state, n_steps):
     rad = pinned(n)
     rad[:] = 0.5
     it = psim.Integrator(n, gamma=GAMMA, dt=DT, kT=KT, vel_freq=1000)
-    hi, cse, srt = psim.cells_build(g, buf["pos"], rad)
-    t_cur = DT  # continue as a normal step
+    import torch
     ncell = scale ** 3
+    # the reference's arrays in pinned host memory, written in place each step
+    cells = (pinned(2 * n, torch.int32), pinned(2 * ncell, torch.int32).view(np.uint32),
+             pinned(4 * n))
+    f = pinned(3 * n)
+    hi, cse, srt = psim.cells_build(g, buf["pos"], rad, out=cells)
+    t_cur = DT  # continue as a normal step
     t0 = time.perf_counter()
     for _ in range(n_steps):
-        f = psim.force_evaluate(p, g, srt, hi, cse, precision=psim.PRECISION_MIXED)
+        psim.force_evaluate(p, g, srt, hi, cse, precision=psim.PRECISION_MIXED, out=f)
         it.next_system(t_cur, box, buf["pos"], buf["pos0"], buf["vel"], buf["frc"], buf["frc0"],
                        mass, particle_force=f)
-        hi, cse, srt = psim.cells_build(g, buf["pos"], rad)
+        psim.cells_build(g, buf["pos"], rad, out=cells)
         t_cur += DT
     el = time.perf_counter() - t0
     h2d = (32 * n + 8 * n + 8 * ncell) + (24 * n * 6 + 8 * n) + (24 * n + 8 * n)

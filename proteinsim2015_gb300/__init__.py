@@ -282,29 +282,41 @@ def ao_coefficients(kT, well_depth, cutoff):
 
 # ---------------------------------------------------------------- drop-ins
 
-def cells_build(geom, pos, radius):
+def _out(arr, dtype, size):
+    """A caller's output array (e.g. in pinned memory, which the copies read at
+    full speed), checked, or a new one."""
+    if arr is None:
+        return np.empty(size, dtype)
+    if arr.dtype != dtype or not arr.flags.c_contiguous or arr.size != size:
+        raise PsimError(ERR_INPUT, "output array must be contiguous %s[%d]" % (np.dtype(dtype), size))
+    return arr.reshape(-1)
+
+
+def cells_build(geom, pos, radius, out=None):
     """hashParticles + sortParticles + clearCells + reorderParticles on the GPU.
     Returns (particle_hash_index[2n] int32, cell_start_end[2 s^3] uint32,
-    sorted_particles[4n] float64)."""
+    sorted_particles[4n] float64), written into `out` (the same three arrays)
+    when given."""
     n = geom.n_particles
     pos = _f64(pos, 3 * n)
     radius = _f64(radius, n)
-    hi = np.empty(2 * n, np.int32)
-    cse = np.empty(2 * geom.cell_scale ** 3, np.uint32)
-    srt = np.empty(4 * n, np.float64)
+    o = out if out is not None else (None, None, None)
+    hi = _out(o[0], np.int32, 2 * n)
+    cse = _out(o[1], np.uint32, 2 * geom.cell_scale ** 3)
+    srt = _out(o[2], np.float64, 4 * n)
     _check(lib().psim_cells_build(C.byref(geom), _p(pos), _p(radius), _p(hi), _p(cse), _p(srt)))
     return hi, cse, srt
 
 
 def force_evaluate(params, geom, sorted_particles, hash_index, cell_start_end,
-                   precision=PRECISION_FP64):
+                   precision=PRECISION_FP64, out=None):
     """defaultForceManager::getAcceleration on the reference's arrays; returns
-    particle_force[3n] in original order."""
+    particle_force[3n] in original order (written into `out` when given)."""
     n = geom.n_particles
     srt = _f64(sorted_particles, 4 * n)
     hi = np.ascontiguousarray(hash_index, np.int32).reshape(-1)
     cse = np.ascontiguousarray(cell_start_end, np.uint32).reshape(-1)
-    out = np.empty(3 * n, np.float64)
+    out = _out(out, np.float64, 3 * n)
     _check(lib().psim_force_evaluate(C.byref(params), C.byref(geom), precision, _p(srt), _p(hi),
                                      _p(cse), _p(out)))
     return out
