@@ -10,6 +10,9 @@
     SnapshotWriter   the snapshot directory layout of writeSystemState
                      (analysisOutput.cpp:99-114), with the positions copied to
                      the host on a side stream while the steps go on
+    post_analysis    analysisManager::postAnalysis (analysisPost.cpp:26-52): the
+                     coordination, cluster-size and cluster-coordination
+                     histograms (analysisCluster.cpp:135-203) of the device state
 
 The reference writes doubles with the stream's default format (6 significant
 digits, as printf's %g), so its recovery files hold 6 digits; ``exact=True``
@@ -129,3 +132,51 @@ class SnapshotWriter:
         if self._thread is not None:
             self._thread.join()
             self._thread = None
+
+
+def histogram_text(values):
+    """The reference's histogram file: "key count" per line for every value
+    that occurs, keys ascending (a std::map<int, int> written in order)."""
+    keys, counts = np.unique(np.asarray(values, dtype=np.int64), return_counts=True)
+    return "".join("%d %d\n" % (k, c) for k, c in zip(keys, counts))
+
+
+POST_TESTS = {
+    "--coorhist": "coordinationHistogram.txt", "-CH": "coordinationHistogram.txt",
+    "--clusthist": "clusterSizeHistogram.txt", "-CLH": "clusterSizeHistogram.txt",
+    "--clustcoor": "clusterCoorHistogram.txt", "-CLC": "clusterCoorHistogram.txt",
+}
+
+
+def post_analysis(system, trial_name, tests, r_contact=1.2):
+    """analysisManager::postAnalysis (analysisPost.cpp:26-52) on a System: the
+    clusters of more than 4 particles in contact (findClusters,
+    analysisCluster.cpp:26-83), then for each test flag in order
+      --coorhist  / -CH   coordinationHistogram.txt: particles per
+                          coordination number (analysisCluster.cpp:184-203)
+      --clusthist / -CLH  clusterSizeHistogram.txt: clusters per size
+                          (analysisCluster.cpp:135-156)
+      --clustcoor / -CLC  clusterCoorHistogram.txt: the clustered particles
+                          per coordination number (analysisCluster.cpp:158-182)
+    Coordination numbers are those of updateInteractions (contacts closer than
+    r_contact, systemHandling.cpp:94-161).  Returns the files written."""
+    _, groups, _ = system.clusters(r_contact, 4)
+    coor, _ = system.interactions(r_contact)
+    coor = np.asarray(coor)
+    written = []
+    for t in tests:
+        name = POST_TESTS.get(t)
+        if name is None:
+            continue
+        if name == "coordinationHistogram.txt":
+            text = histogram_text(coor)
+        elif name == "clusterSizeHistogram.txt":
+            text = histogram_text([len(g) for g in groups])
+        else:
+            members = np.concatenate(groups) if groups else np.empty(0, np.int64)
+            text = histogram_text(coor[members])
+        path = os.path.join(trial_name, name)
+        with open(path, "w") as fh:
+            fh.write(text)
+        written.append(path)
+    return written

@@ -47,3 +47,24 @@ def test_frame_overlaps_steps_and_recovery_restarts(psim, tmp_path):
     assert np.all(np.isfinite(c.download()["pos"]))
     for s in (a, b, c):
         s.close()
+
+
+def test_post_analysis_histograms_match_all_pairs(psim, tmp_path):
+    n, box = 1500, 14.0   # phi ~ 0.29: clusters of many contacts closer than 1.2
+    pos, rad = rsa_state(n, box, seed=81)
+    s = make(psim, pos, rad, n, box=box, scale=4)
+    s.step(5)
+    p = s.download()["pos"].reshape(-1, 3)
+    d = p[:, None, :] - p[None, :, :]
+    a = np.abs(d)
+    d = np.where(a > box / 2, a - box, a)      # pbcDist (utilities.cpp:79-104)
+    r = np.sqrt(np.sum(d * d, axis=2))
+    np.fill_diagonal(r, np.inf)
+    coor = np.sum(r < 1.2, axis=1)
+    files = io.post_analysis(s, str(tmp_path), ["-CH", "-CLH", "-CLC"])
+    assert len(files) == 3
+    assert open(files[0]).read() == io.histogram_text(coor)
+    _, groups, _ = s.clusters(1.2, 4)
+    assert open(files[1]).read() == io.histogram_text([len(g) for g in groups])
+    assert open(files[2]).read() == io.histogram_text(coor[np.concatenate(groups)])
+    s.close()

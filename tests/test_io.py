@@ -1,4 +1,6 @@
 """Recovery and XYZ files in the reference's formats (host side, no GPU)."""
+import os
+
 import numpy as np
 
 from proteinsim2015_gb300 import io
@@ -38,3 +40,33 @@ def test_xyz_frame(tmp_path):
     io.write_series(tmp_path / "s.txt", 10.0, 0.25)
     io.write_series(tmp_path / "s.txt", 20.0, 0.5)
     assert (tmp_path / "s.txt").read_text() == "10 0.25\n20 0.5\n"
+
+
+class _FakeSystem:
+    """Stands in for a System: fixed coordination numbers and clusters."""
+
+    def __init__(self, coor, groups):
+        self.coor = np.asarray(coor, np.int32)
+        self.groups = [np.asarray(g) for g in groups]
+
+    def clusters(self, r_contact=1.2, min_size=4):
+        return None, self.groups, 0
+
+    def interactions(self, r_contact=1.2):
+        return self.coor, int(self.coor.sum())
+
+
+def test_post_analysis_histograms(tmp_path):
+    from proteinsim2015_gb300 import io
+    coor = [0, 2, 2, 3, 1, 2, 5, 2, 3, 3, 1, 0]
+    groups = [[1, 2, 3, 5, 6], [7, 8, 9, 10, 11, 0]]
+    files = io.post_analysis(_FakeSystem(coor, groups), str(tmp_path), ["-CH", "--clusthist",
+                                                                        "-CLC", "--other"])
+    names = [os.path.basename(f) for f in files]
+    assert names == ["coordinationHistogram.txt", "clusterSizeHistogram.txt",
+                     "clusterCoorHistogram.txt"]
+    read = {n: open(os.path.join(str(tmp_path), n)).read() for n in names}
+    assert read["coordinationHistogram.txt"] == "0 2\n1 2\n2 4\n3 3\n5 1\n"
+    assert read["clusterSizeHistogram.txt"] == "5 1\n6 1\n"
+    # members 1 2 3 5 6 7 8 9 10 11 0 -> coor 2 2 3 2 5 2 3 3 1 0 0
+    assert read["clusterCoorHistogram.txt"] == "0 2\n1 1\n2 4\n3 3\n5 1\n"
