@@ -300,10 +300,19 @@ typedef struct {
  * integ.seed replaced by the replica's seed, and steps bit for bit like it.
  * The returned handle takes every psim_system_* call; its arrays are the
  * replicas' arrays concatenated in replica order (original order within
- * each).  No pair-list skin. */
+ * each).  No pair-list skin (see psim_batch_create_list). */
 psim_system* psim_batch_create(const psim_replica* reps, int32_t n_reps,
                                const psim_integrator_config* integ, int32_t precision,
                                int32_t noise_mode, int32_t device);
+
+/* A batch whose force pass reads a Verlet pair list (mixed precision form):
+ * every replica's cellSize must be >= its cutOff + skin.  The list is built
+ * for all replicas together, on the step after a particle of any replica has
+ * moved skin / 2; each replica keeps its own box, grid, pair parameters and
+ * noise.  skin 0 is psim_batch_create. */
+psim_system* psim_batch_create_list(const psim_replica* reps, int32_t n_reps,
+                                    const psim_integrator_config* integ, int32_t precision,
+                                    int32_t noise_mode, int32_t device, double skin);
 
 /* Creates the system and its device buffers (the role of system::system,
  * system.cpp:69-103, without the random initialisation: states are uploaded). */

@@ -124,6 +124,8 @@ def lib():
             "psim_system_create": ([C.POINTER(SystemConfig)], P),
             "psim_batch_create": ([C.POINTER(Replica), C.c_int32, C.POINTER(IntegratorConfig),
                                    C.c_int32, C.c_int32, C.c_int32], P),
+            "psim_batch_create_list": ([C.POINTER(Replica), C.c_int32, C.POINTER(IntegratorConfig),
+                                        C.c_int32, C.c_int32, C.c_int32, C.c_double], P),
             "psim_system_destroy": ([P], None),
             "psim_system_upload": ([P] * 8, C.c_int),
             "psim_system_set_noise": ([P, P, C.c_int32, C.c_int32], C.c_int),
@@ -551,10 +553,12 @@ class System:
 class Batch(System):
     """Independent replicas stepped together, one launch per phase.  Each
     replica is (geometry, force params, seed); arrays are the replicas'
-    arrays concatenated in replica order.  Every System method applies."""
+    arrays concatenated in replica order.  Every System method applies.  A
+    skin > 0 gives the mixed form a pair list (every replica's cellSize >=
+    its cutOff + skin)."""
 
     def __init__(self, replicas, gamma=1.0, dt=0.001, kT=1.0, vel_freq=1000,
-                 precision=PRECISION_MIXED, noise_mode=NOISE_PHILOX, device=0):
+                 precision=PRECISION_MIXED, noise_mode=NOISE_PHILOX, device=0, skin=0.0):
         arr = (Replica * len(replicas))()
         for k, (g, f, seed) in enumerate(replicas):
             arr[k] = Replica(geom=g, force=f, seed=int(seed))
@@ -564,9 +568,9 @@ class Batch(System):
         self.offsets = np.concatenate([[0], np.cumsum(self.sizes)]).astype(int)
         self.n = int(self.offsets[-1])
         self.ncell = sum(g.cell_scale ** 3 for g, _, _ in replicas)
-        self.skin = 0.0
-        self._h = lib().psim_batch_create(arr, len(replicas), C.byref(self.integ), precision,
-                                          noise_mode, device)
+        self.skin = float(skin)
+        self._h = lib().psim_batch_create_list(arr, len(replicas), C.byref(self.integ), precision,
+                                               noise_mode, device, self.skin)
         if not self._h:
             _raise_last(ERR_INPUT)
 

@@ -28,9 +28,10 @@ def ao_params(psim, contact_kT, q, kT=1.0):
     return psim.make_force("AO", rc, kT=kT, well_depth=contact_kT * q / (1.5 + q))
 
 
-def geometry_for(psim, n, box, cutoff, factor=1.0):
-    """The finest grid with cellSize >= factor * cutoff (at least 3 cells a side)."""
-    scale = max(3, int(math.floor(box / (factor * cutoff))))
+def geometry_for(psim, n, box, cutoff, factor=1.0, skin=0.0):
+    """The finest grid with cellSize >= factor * cutoff and >= cutoff + skin
+    (at least 3 cells a side)."""
+    scale = max(3, int(math.floor(box / max(factor * cutoff, cutoff + skin))))
     return psim.geometry(n, box, box / scale, scale)
 
 
@@ -48,13 +49,14 @@ def c2_draws(n_reps=512, seed=2015):
     return out
 
 
-def replicas(psim, draws, factors=None):
-    """(geometry, force, seed) per draw; factors: cell-size factor per replica."""
+def replicas(psim, draws, factors=None, skin=0.0):
+    """(geometry, force, seed) per draw; factors: cell-size factor per replica;
+    skin: the pair-list skin the grids must allow."""
     reps = []
     for k, d in enumerate(draws):
         f = ao_params(psim, d["contact_kT"], d["q"])
         fac = 1.0 if factors is None else factors[k]
-        reps.append((geometry_for(psim, d["n"], d["box"], f.cutoff, fac), f, d["seed"]))
+        reps.append((geometry_for(psim, d["n"], d["box"], f.cutoff, fac, skin), f, d["seed"]))
     return reps
 
 

@@ -810,6 +810,10 @@ struct psim_system {
     // contiguous, so its particles keep their slot range in every cell order)
     int n_reps = 0, n_tasks = 0;
     DevBuf b_tasks, b_geoms, b_pairs, b_pre, b_rep, b_seeds;
+    // a batch with a pair list: per replica the list radius squared and the
+    // halo radius; the largest box and cutoff (the compact records' unit)
+    DevBuf b_lpre, b_hr;
+    double lmaxL = 0.0, lmaxrc = 0.0;
     // displacement tracker: box images crossed per particle and the start
     // positions (original order), counted by the integrator once started
     DevBuf img, track_start;
@@ -850,6 +854,11 @@ void set_halo_args(psim_system* s, CanonArgs& ca) {
     ca.Lf = (float)s->g.L;
     ca.Lhi = s->g.Lhi;
     ca.Llo = s->g.Llo;
+    if (s->n_reps) {   // each replica's own box and halo radius
+        ca.rep = s->b_rep.as<int>();
+        ca.geoms = s->b_geoms.as<DevGeom>();
+        ca.hr_rep = s->b_hr.as<float>();
+    }
 }
 
 // The pair-list build on the cell order just made (count buffer cb), run
@@ -859,6 +868,11 @@ cudaError_t enqueue_list_build(psim_system* s, int cb, const int* gate) {
                 s->start.as<int>(), s->count[cb].as<int>()};
     ListBuild lb{s->list.as<uint32_t>(), s->lcount.as<int>(), s->n, s->lcap, s->lpre, gate,
                  s->lhalo.as<int>(), s->n};
+    if (s->n_reps) {   // each replica's own grid and list radius
+        lb.rep = s->b_rep.as<int>();
+        lb.geoms = s->b_geoms.as<DevGeom>();
+        lb.pre = s->b_lpre.as<float>();
+    }
     return launch_list_build(s->g, cv, lb, s->err.as<uint32_t>(), s->st);
 }
 
@@ -867,6 +881,11 @@ cudaError_t enqueue_list_build(psim_system* s, int cb, const int* gate) {
 cudaError_t enqueue_force(psim_system* s, const Phase& ph, const ForceOut& fo) {
     CellView cv{s->posd.as<double4_32a>(), s->posh.as<float4>(), s->posl.as<float4>(),
                 s->cellid.as<int>(), s->start.as<int>(), s->count[ph.cb].as<int>()};
+    if (s->n_reps && s->list_on) {   // each particle with its replica's pair functor
+        PairList pl{nullptr, s->lpos.as<float4>(), s->lcount.as<int>(), s->list.as<uint32_t>(),
+                    s->n, s->lcompact, s->lradius, s->lunit, s->b_rep.as<int>(), s->b_pairs.p};
+        return launch_forces_list(s->fs, s->g, pl, fo, s->st);
+    }
     if (s->n_reps) {
         BatchView bv{s->b_tasks.as<int2>(), s->n_tasks, s->b_geoms.as<DevGeom>(),
                      s->b_pairs.p, s->b_pre.as<float>()};
@@ -905,7 +924,9 @@ int enqueue_rebuild_lazy(psim_system* s, long long t) {
     PSIM_CUDA(cudaMemsetAsync(s->count[0].p, 0, 4 * (size_t)s->ncell, st));
     PSIM_CUDA(launch_hash_count(n, d3(s->pos[nsb], n, 0), d3(s->pos[nsb], n, 1),
                                 d3(s->pos[nsb], n, 2), s->g, s->key.as<int>(), s->rank.as<int>(),
-                                s->count[0].as<int>(), err, st));
+                                s->count[0].as<int>(), err, st,
+                                s->n_reps ? s->b_rep.as<int>() : nullptr,
+                                s->n_reps ? s->b_geoms.as<DevGeom>() : nullptr));
     PSIM_CUDA(launch_scan(s->count[0].as<int>(), s->start.as<int>(), s->ncell,
                           s->scratch.as<int>(), st));
     PSIM_CUDA(launch_scatter(n, s->key.as<int>(), s->rank.as<int>(), s->start.as<int>(),
@@ -998,6 +1019,11 @@ int enqueue_step_lazy(psim_system* s, long long t, cudaEvent_t* evs) {
     a.lhalo = s->lhalo.as<int>();
     a.lhcount = s->lhcount.as<int>();
     a.img = s->img.as<int>();
+    if (s->n_reps) {
+        a.rep = s->b_rep.as<int>();
+        a.geoms = s->b_geoms.as<DevGeom>();
+        a.seeds = s->b_seeds.as<uint32_t>();
+    }
     NoiseView nz{s->cfg.noise_mode, s->noise.as<double>(), s->noise_first, s->noise_steps};
     PSIM_CUDA(launch_vgb_system_fast(a, s->vp, s->g, nz, st));
     if (evs) PSIM_CUDA(cudaEventRecord(evs[2], st));
@@ -1257,7 +1283,9 @@ int cell_refs(psim_system* s, CellRefs& c) {
     PSIM_CUDA(cudaMemsetAsync(s->count[0].p, 0, 4 * (size_t)s->ncell, st));
     PSIM_CUDA(launch_hash_count(n, d3(s->pos[ph.sb], n, 0), d3(s->pos[ph.sb], n, 1),
                                 d3(s->pos[ph.sb], n, 2), s->g, s->key.as<int>(), s->rank.as<int>(),
-                                s->count[0].as<int>(), err, st));
+                                s->count[0].as<int>(), err, st,
+                                s->n_reps ? s->b_rep.as<int>() : nullptr,
+                                s->n_reps ? s->b_geoms.as<DevGeom>() : nullptr));
     PSIM_CUDA(launch_scan(s->count[0].as<int>(), s->start.as<int>(), s->ncell,
                           s->scratch.as<int>(), st));
     PSIM_CUDA(launch_scatter(n, s->key.as<int>(), s->rank.as<int>(), s->start.as<int>(),
@@ -1287,6 +1315,34 @@ int cell_refs(psim_system* s, CellRefs& c) {
 
 namespace {
 psim_system* system_new(const psim_system_config* cfg, const DevGeom& g);
+
+// The pair list's sizes for cutoff rc, skin and grid g: the entries per
+// particle (room for 1.5x the mean number of neighbours within rc + skin,
+// + 32), the list radius squared (the FP32 test's widened bound), the
+// rebuild test's displacement squared (half the skin, less the FP32 rounding
+// of the positions, each off by ulp(L)/2), the halo radius (beyond the list
+// test's radius, so every pair the build finds across an edge has an image)
+// and the halo records to hold.
+struct ListSizes {
+    int cap;
+    float pre, disp2, hr;
+    int hcap;
+};
+ListSizes list_sizes(double rc, double skin, const DevGeom& g) {
+    ListSizes z{};
+    const double rl = rc + skin;
+    const double mean = 4.0 / 3.0 * M_PI * rl * rl * rl * g.n / (g.L * g.L * g.L);
+    z.cap = ((int)(1.5 * mean) + 32 + 31) / 32 * 32;
+    z.pre = prefilter_r2(rl, g.L);
+    const double ulpL = std::ldexp(1.0, std::ilogb(std::max(g.L, 1.0)) - 23);
+    const double dmax = 0.5 * skin * (1.0 - 1e-3) - 4.0 * ulpL;
+    z.disp2 = dmax > 0.0 ? (float)(dmax * dmax) : 0.f;
+    z.hr = (float)(std::sqrt((double)z.pre) + 1e-3 * rl + 16.0 * ulpL);
+    const double p = 2.0 * z.hr / g.L;   // a particle's chance of an image per axis
+    const double expect = g.n * ((1.0 + p) * (1.0 + p) * (1.0 + p) - 1.0);
+    z.hcap = (int)std::min(std::min(7.0 * g.n, 1.3 * expect + 1024.0), (double)kHaloBaseMax);
+    return z;
+}
 }
 
 extern "C" {
@@ -1310,9 +1366,27 @@ psim_system* psim_system_create(const psim_system_config* cfg) {
 psim_system* psim_batch_create(const psim_replica* reps, int32_t n_reps,
                                const psim_integrator_config* integ, int32_t precision,
                                int32_t noise_mode, int32_t device) {
+    return psim_batch_create_list(reps, n_reps, integ, precision, noise_mode, device, 0.0);
+}
+
+psim_system* psim_batch_create_list(const psim_replica* reps, int32_t n_reps,
+                                    const psim_integrator_config* integ, int32_t precision,
+                                    int32_t noise_mode, int32_t device, double skin) {
     if (!reps || n_reps <= 0 || !integ) {
         fail(PSIM_ERR_INPUT, "a batch needs at least one replica and an integrator config");
         return nullptr;
+    }
+    if (!(skin >= 0.0) || (skin > 0.0 && precision != PSIM_PRECISION_MIXED)) {
+        fail(PSIM_ERR_INPUT, "a pair-list skin needs the mixed precision form (skin %g)", skin);
+        return nullptr;
+    }
+    for (int r = 0; r < n_reps && skin > 0.0; ++r) {
+        const double need = max_cutoff(&reps[r].force) + skin;
+        if (reps[r].geom.cell_size < need) {
+            fail(PSIM_ERR_INPUT, "replica %d: pair-list skin %g needs cellSize >= cutOff + skin "
+                 "(%g < %g)", r, skin, reps[r].geom.cell_size, need);
+            return nullptr;
+        }
     }
     const int kind = reps[0].force.kind;
     if (kind == PSIM_FORCE_AO_YUKAWA) {
@@ -1356,7 +1430,7 @@ psim_system* psim_batch_create(const psim_replica* reps, int32_t n_reps,
     cfg.precision = precision;
     cfg.noise_mode = noise_mode;
     cfg.device = device;
-    cfg.skin = 0.0;
+    cfg.skin = skin;
     if (precision != PSIM_PRECISION_FP64 && precision != PSIM_PRECISION_MIXED) {
         fail(PSIM_ERR_INPUT, "unknown precision %d", precision);
         return nullptr;
@@ -1407,6 +1481,41 @@ psim_system* psim_batch_create(const psim_replica* reps, int32_t n_reps,
         psim_system_destroy(s);
         return nullptr;
     }
+    if (s->list_on) {
+        // the list's sizes per replica: entries and halo records for the
+        // densest, the rebuild test of the strictest, each radius its own
+        std::vector<float> lpre((size_t)n_reps), hr((size_t)n_reps);
+        int cap = 0;
+        long long hcap = 0;
+        float disp2 = 3.0e38f, pre_max = 0.f;
+        for (int r = 0; r < n_reps; ++r) {
+            const ListSizes z = list_sizes(max_cutoff(&reps[r].force), skin, geoms[r]);
+            cap = std::max(cap, z.cap);
+            hcap += z.hcap;
+            disp2 = std::min(disp2, z.disp2);
+            pre_max = std::max(pre_max, z.pre);
+            lpre[(size_t)r] = z.pre;
+            hr[(size_t)r] = z.hr;
+            s->lmaxL = std::max(s->lmaxL, geoms[r].L);
+            s->lmaxrc = std::max(s->lmaxrc, max_cutoff(&reps[r].force));
+        }
+        s->lcap = cap;
+        s->hcap = (int)std::min(hcap, (long long)kHaloBaseMax);
+        s->ldisp2 = disp2;
+        s->lpre = pre_max;
+        const size_t n = (size_t)P;
+        const bool ok2 = (double)(cap + kListFold) * (double)P < 4294967296.0 &&
+                         put(s->b_lpre, lpre.data(), lpre.size() * sizeof(float)) &&
+                         put(s->b_hr, hr.data(), hr.size() * sizeof(float)) &&
+                         !s->list.ensure(4 * n * (size_t)(cap + kListFold)) &&
+                         !s->lpos.ensure(32 * (n + 1 + (size_t)s->hcap));
+        if (!ok2) {
+            fail(PSIM_ERR_INPUT, "the batch's pair list does not fit (%lld particles, %d entries "
+                 "each)", (long long)P, cap);
+            psim_system_destroy(s);
+            return nullptr;
+        }
+    }
     return s;
 }
 
@@ -1455,12 +1564,10 @@ psim_system* system_new(const psim_system_config* cfg, const DevGeom& g) {
     s->n = g.n;
     s->ncell = g.ncell;
     if (list_on) {
-        // room for 1.5x the mean number of neighbours within rc + skin, + 32
-        const double rl = rc + skin;
-        const double mean = 4.0 / 3.0 * M_PI * rl * rl * rl * g.n / (g.L * g.L * g.L);
+        const ListSizes z = list_sizes(rc, skin, g);
         s->list_on = true;
         s->skin = skin;
-        s->lcap = ((int)(1.5 * mean) + 32 + 31) / 32 * 32;
+        s->lcap = z.cap;
         if ((double)(s->lcap + kListFold) * (double)g.n >= 4294967296.0) {
             // the list build addresses entries with 32-bit offsets
             const int cap = s->lcap;
@@ -1469,18 +1576,10 @@ psim_system* system_new(const psim_system_config* cfg, const DevGeom& g) {
                  "use a smaller skin", g.n, cap);
             return nullptr;
         }
-        s->lpre = prefilter_r2(rl, g.L);
-        // the rebuild test compares FP32 roundings of the positions (each off
-        // by ulp(L)/2): half the skin, less that error
-        const double ulpL = std::ldexp(1.0, std::ilogb(std::max(g.L, 1.0)) - 23);
-        const double dmax = 0.5 * skin * (1.0 - 1e-3) - 4.0 * ulpL;
-        s->ldisp2 = dmax > 0.0 ? (float)(dmax * dmax) : 0.f;
-        // halo images for the particles within hr of a face: beyond the list
-        // test's radius, so every pair the build finds across an edge has one
-        s->hr = (float)(std::sqrt((double)s->lpre) + 1e-3 * rl + 16.0 * ulpL);
-        const double p = 2.0 * s->hr / g.L;   // a particle's chance of an image per axis
-        const double expect = g.n * ((1.0 + p) * (1.0 + p) * (1.0 + p) - 1.0);
-        s->hcap = (int)std::min(std::min(7.0 * g.n, 1.3 * expect + 1024.0), (double)kHaloBaseMax);
+        s->lpre = z.pre;
+        s->ldisp2 = z.disp2;
+        s->hr = z.hr;
+        s->hcap = z.hcap;
     }
     const size_t n = (size_t)g.n, nc = (size_t)g.ncell;
     bool ok = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) == cudaSuccess &&
@@ -1538,7 +1637,7 @@ void psim_system_destroy(psim_system* s) {
                       &s->snap, &s->lslot[0], &s->lslot[1], &s->lbuild, &s->lpos, &s->list,
                       &s->lcount, &s->lflag, &s->lhalo, &s->lhcount, &s->pscratch, &s->b_tasks,
                       &s->b_geoms, &s->b_pairs, &s->b_pre, &s->b_rep, &s->b_seeds,
-                      &s->img, &s->track_start};
+                      &s->img, &s->track_start, &s->b_lpre, &s->b_hr};
     for (DevBuf* b : arrs) b->release();
     for (int k = 0; k < 2; ++k) {
         s->pos[k].release(); s->pos0[k].release(); s->mem[k].release(); s->tag[k].release();
@@ -1638,7 +1737,8 @@ int psim_system_upload(psim_system* s, const double* pos, const double* pos0, co
         s->lradius = R;
         // low-part unit: |lo| of a record stays below the last place of its
         // high part, or ~2x that after a halo shift; M bounds every coordinate
-        const double M = s->g.L + 2.0 * (max_cutoff(&s->cfg.force) + s->skin) + 1.0;
+        const double M = s->n_reps ? s->lmaxL + 2.0 * (s->lmaxrc + s->skin) + 1.0
+                                   : s->g.L + 2.0 * (max_cutoff(&s->cfg.force) + s->skin) + 1.0;
         s->lunit = (float)std::ldexp(1.0, std::ilogb(M) - 31);
         const float4 ghost[2] = {make_float4(1e18f, 1e18f, 1e18f, compact ? 0.f : R),
                                  make_float4(0.f, 0.f, 0.f, 0.f)};

@@ -162,8 +162,16 @@ __global__ void __launch_bounds__(256) canonicalize_kernel(CanonArgs a, int vel_
             if (a.lpos) {
                 l.w = 0.f;
                 store_record(a.lpos, a.linv_unit, (size_t)g, h, l);
-                // images of a particle near a face, as halo records
-                uint32_t fl = halo_flags(h, a.hr, a.Lf);
+                // images of a particle near a face, as halo records (in a
+                // batch, of its replica's box)
+                float hr = a.hr, Lf = a.Lf, Lhi = a.Lhi, Llo = a.Llo;
+                if (a.rep) {
+                    const int r = a.rep[g];
+                    hr = a.hr_rep[r];
+                    Lf = Lhi = a.geoms[r].Lhi;
+                    Llo = a.geoms[r].Llo;
+                }
+                uint32_t fl = halo_flags(h, hr, Lf);
                 const int m = halo_copies(fl);
                 int base = 0;
                 if (m > 0) {
@@ -174,7 +182,7 @@ __global__ void __launch_bounds__(256) canonicalize_kernel(CanonArgs a, int vel_
                         base = 0;
                     } else {
                         halo_write(a.lpos + (a.linv_unit != 0.f ? 1 : 2) * ((size_t)a.n + 1),
-                                   a.linv_unit, base, fl, h, l, a.Lhi, a.Llo);
+                                   a.linv_unit, base, fl, h, l, Lhi, Llo);
                     }
                 }
                 a.lhalo[g] = (base << 6) | (int)fl;

@@ -72,10 +72,9 @@ __device__ __forceinline__ void list_append(const ListBuild& lb, uint32_t ocap, 
 // padded by four), and masked.  Only the home row's run (kSelf) can hold i
 // itself; a shifted run appends the neighbour's halo record for that image.
 template <bool kShifted, bool kSelf>
-__device__ __forceinline__ void list_run(const CellView& cv, const ListBuild& lb, int i, int a,
-                                         int len, float hx, float hy, float hz, int sx, int sy,
-                                         int sz, int& n, uint32_t& o, uint32_t& err) {
-    const float R2 = lb.pre_r2;
+__device__ __forceinline__ void list_run(const CellView& cv, const ListBuild& lb, float R2, int i,
+                                         int a, int len, float hx, float hy, float hz, int sx,
+                                         int sy, int sz, int& n, uint32_t& o, uint32_t& err) {
     const uint32_t ocap = ((uint32_t)(lb.cap / kListFold) * (uint32_t)lb.stride + (uint32_t)i) *
                           kListFold;
     const float4* pp = cv.posh + a;
@@ -119,12 +118,12 @@ __device__ __forceinline__ void list_run(const CellView& cv, const ListBuild& lb
 }
 
 __device__ __forceinline__ void list_build_one(const DevGeom& g, const CellView& cv,
-                                               const ListBuild& lb, int i, uint32_t& err) {
+                                               const ListBuild& lb, float R2, int i,
+                                               uint32_t& err) {
     const float4 hi = cv.posh[i];
     const int c = cv.cellid[i] - g.c0;
     const int cx = c % g.s, cy = (c / g.s) % g.s, cz = c / g.s2;
-    const int ghost = g.n;
-    const float R2 = lb.pre_r2;
+    const int ghost = lb.ghost;
     // distances to the lower and upper faces of the home cell, less a margin
     // for the FP32 rounding of the position and of the cell bounds
     const float csf = (float)g.cs;
@@ -169,11 +168,11 @@ __device__ __forceinline__ void list_build_one(const DevGeom& g, const CellView&
             const float hy = hi.y - (float)sy * g.Lhi;
             const float hz = hi.z - (float)sz * g.Lhi;
             if ((sx | sy | sz) != 0)
-                list_run<true, false>(cv, lb, i, a, len, hx, hy, hz, sx, sy, sz, n, o, err);
+                list_run<true, false>(cv, lb, R2, i, a, len, hx, hy, hz, sx, sy, sz, n, o, err);
             else if (row == 4 && part == 0)
-                list_run<false, true>(cv, lb, i, a, len, hx, hy, hz, 0, 0, 0, n, o, err);
+                list_run<false, true>(cv, lb, R2, i, a, len, hx, hy, hz, 0, 0, 0, n, o, err);
             else
-                list_run<false, false>(cv, lb, i, a, len, hx, hy, hz, 0, 0, 0, n, o, err);
+                list_run<false, false>(cv, lb, R2, i, a, len, hx, hy, hz, 0, 0, 0, n, o, err);
         }
     }
     // the open group padded with the ghost record
@@ -193,8 +192,14 @@ __global__ void __launch_bounds__(128)
 list_build_kernel(DevGeom g, CellView cv, ListBuild lb, uint32_t* errp) {
     if (*errp != 0 || (lb.gate && *lb.gate == 0)) return;
     uint32_t err = 0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += gridDim.x * blockDim.x)
-        list_build_one(g, cv, lb, i, err);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += gridDim.x * blockDim.x) {
+        if (lb.rep) {   // a batch: the particle's replica's grid and list radius
+            const int r = lb.rep[i];
+            list_build_one(lb.geoms[r], cv, lb, lb.pre[r], i, err);
+        } else {
+            list_build_one(g, cv, lb, lb.pre_r2, i, err);
+        }
+    }
     if (err) atomicOr(errp, err);
 }
 
@@ -238,13 +243,16 @@ __device__ __forceinline__ ListRec<false> load_rec(const float4* pos, uint32_t j
 // is d = (x_j,hi - x_i,hi) + (x_j,lo - x_i,lo): the first difference is exact
 // for nearby values and the second comes out of the record's decode
 // (compact) or one subtraction (full), so d carries one FP32 rounding.
-template <class Body, bool kCompact>
+template <class Body, bool kCompact, bool kReplicas>
 __global__ void __launch_bounds__(128)
-force_list_kernel(Body body, DevGeom g, PairList pl, ForceOut out) {
+force_list_kernel(Body body0, DevGeom g, PairList pl, ForceOut out) {
     constexpr int kBatch = 4;
     static_assert(kListFold == 2 * kBatch, "a fold is two batches");
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= g.n || *out.err) return;
+    // a batch: the pair functor of the particle's replica (its neighbours are
+    // all of the same replica)
+    const Body body = kReplicas ? body0.for_replica(pl.pairs, pl.rep[f], g) : body0;
     const int s = pl.lslot ? pl.lslot[f] : f;   // no slot table: storage order is list order
     float4 hh, hl;
     // compact records: a neighbour's low part minus the home's comes out of one
@@ -331,10 +339,21 @@ template <class Body>
 cudaError_t launch_force_list(const Body& body, const DevGeom& g, const PairList& pl,
                               const ForceOut& out, cudaStream_t st) {
     if (g.n == 0) return cudaSuccess;
+    const int blocks = (g.n + 127) / 128;
+    if (pl.rep) {
+        if constexpr (Body::kBatchable) {
+            if (pl.compact)
+                force_list_kernel<Body, true, true><<<blocks, 128, 0, st>>>(body, g, pl, out);
+            else
+                force_list_kernel<Body, false, true><<<blocks, 128, 0, st>>>(body, g, pl, out);
+            return cudaGetLastError();
+        }
+        return cudaErrorInvalidValue;
+    }
     if (pl.compact)
-        force_list_kernel<Body, true><<<(g.n + 127) / 128, 128, 0, st>>>(body, g, pl, out);
+        force_list_kernel<Body, true, false><<<blocks, 128, 0, st>>>(body, g, pl, out);
     else
-        force_list_kernel<Body, false><<<(g.n + 127) / 128, 128, 0, st>>>(body, g, pl, out);
+        force_list_kernel<Body, false, false><<<blocks, 128, 0, st>>>(body, g, pl, out);
     return cudaGetLastError();
 }
 

@@ -81,6 +81,10 @@ struct PairList {
     int compact;
     float radius;
     float lo_unit;
+    // a batch of replicas (rep null: one system): each storage slot's replica
+    // and the replicas' pair functors
+    const int* rep;
+    const void* pairs;
 };
 cudaError_t launch_forces_list(const ForceSetup& fs, const DevGeom& g, const PairList& pl,
                                const ForceOut& out, cudaStream_t st);
@@ -95,6 +99,11 @@ struct ListBuild {
     const int* gate;
     const int* lhalo;      // per list slot: first halo record << 6 | halo_flags
     int ghost;             // the ghost record (n); halo records follow it
+    // a batch of replicas (rep null: one system): each slot's replica, the
+    // replicas' geometries and list radii squared (pre_r2 per replica)
+    const int* rep;
+    const DevGeom* geoms;
+    const float* pre;
 };
 cudaError_t launch_list_build(const DevGeom& g, const CellView& cv, const ListBuild& lb,
                               uint32_t* err, cudaStream_t st);
@@ -254,6 +263,11 @@ struct CanonArgs {
     int* lhcount;
     int hcap;
     float hr, Lf, Lhi, Llo;
+    // a batch of replicas (rep null: one system): the halo radius and the box
+    // of each slot's replica
+    const int* rep;
+    const DevGeom* geoms;
+    const float* hr_rep;
 };
 cudaError_t launch_canonicalize(const CanonArgs& a, cudaStream_t st);
 

@@ -63,3 +63,54 @@ def test_batch_refuses_mixed_plugins(psim):
                          yukawa_strength=1.0, debye_length=0.25, lj_num=0)
     with pytest.raises(psim.PsimError):
         psim.Batch([(g1, f3, 1)])
+
+
+def test_batch_with_pair_list_follows_batch_without(psim):
+    # the same replicas with grids that allow a 0.2 skin.  After steps across
+    # list rebuilds (all replicas rebuild together), the list pass and the cell
+    # walk give the same forces on the list run's state, and one more step
+    # from that state moves both alike (the steep AO core makes longer
+    # trajectories diverge from FP32 summation order alone)
+    skin = 0.2
+    reps, states = [], []
+    for k, (n, phi, a, q) in enumerate(REPLICAS):
+        g0, f, pos = ao_replica(psim, n, phi, a, q, seed=60 + k)
+        box = g0.box_size
+        scale = max(3, int(np.floor(box / (f.cutoff + skin))))
+        reps.append((psim.geometry(n, box, box / scale, scale), f, 1000 + 17 * k))
+        states.append(pos)
+    rng = np.random.default_rng(63)
+    vel = np.concatenate([rng.standard_normal(3 * g.n_particles) for g, _, _ in reps])
+    lst = psim.Batch(reps, gamma=1.0, dt=0.002, kT=1.0, vel_freq=7, skin=skin)
+    lst.upload(np.concatenate(states), np.full(lst.n, 0.5), vel=vel)
+    for k in (1, 5, 13, 41):
+        lst.step(k)
+    assert lst.list_builds() >= 1
+    st = lst.download()
+    walk = psim.Batch(reps, gamma=1.0, dt=0.002, kT=1.0, vel_freq=7)
+    walk.upload(st["pos"], np.full(walk.n, 0.5), vel=st["vel"], pos0=st["pos0"], frc=st["frc"],
+                frc0=st["frc0"])
+    lst.upload(st["pos"], np.full(lst.n, 0.5), vel=st["vel"], pos0=st["pos0"], frc=st["frc"],
+               frc0=st["frc0"])
+    fl, fw = lst.forces(), walk.forces()
+    assert np.linalg.norm(fl - fw) < 1e-5 * np.linalg.norm(fw)
+    lst.step(1)
+    walk.step(1)
+    a, b = lst.download(), walk.download()
+    for k, (g, _, _) in enumerate(reps):
+        d = lst.split(a["pos"])[k] - walk.split(b["pos"])[k]
+        d -= g.box_size * np.round(d / g.box_size)   # a wrap at the box edge
+        # dt^2 times the FP32 force difference (~1e-5 of the steep cores' forces)
+        assert np.max(np.abs(d)) < 1e-7, k
+    # the cell list exported for the current positions is the same
+    assert all(np.array_equal(x, y) for x, y in zip(lst.download_cells()[:2],
+                                                     walk.download_cells()[:2]))
+    lst.close()
+    walk.close()
+
+
+def test_batch_pair_list_needs_room(psim):
+    g, f, _ = ao_replica(psim, 500, 0.1, 2.0, 0.1, seed=64)
+    with pytest.raises(psim.PsimError) as e:
+        psim.Batch([(g, f, 1)], skin=g.cell_size)   # cellSize < cutOff + skin
+    assert e.value.code == psim.ERR_INPUT
