@@ -303,33 +303,49 @@ def e2e_dropin(psim, w, state, n_steps):
     return n * n_steps / el, h2d, d2h
 
 
-def run_batched(psim, dev, steps=2000, n_reps=512, tune=True):
+def run_batched(psim, dev, steps=2000, n_reps=512, tune=True, skin=0.3):
     """The batched-replica workload: 512 independent AO systems (N, phi,
     contact attraction and q drawn per replica), gamma = 1, dt = 1e-3, mixed
-    form, every step one launch per phase over all replicas; each replica's
-    cell size chosen by the autotuner per size bucket."""
+    form, every step one set of launches over all replicas.  `value`: with a
+    pair list (skin 0.3; each replica's grid the finest with cellSize >= cutOff
+    + skin).  `cell_walk`: the 27-cell walk every step, each replica's cell size
+    chosen by the autotuner per size bucket."""
     from proteinsim2015_gb300 import batch
     draws = batch.c2_draws(n_reps)
+    pos, vel = batch.states(draws)
+
+    def timed(reps, sk):
+        b = psim.Batch(reps, gamma=1.0, dt=0.001, kT=1.0, vel_freq=1000,
+                       precision=psim.PRECISION_MIXED, device=dev, skin=sk)
+        b.upload(pos, np.full(b.n, 0.5), vel=vel)
+        b.step(3)
+        b0 = b.list_builds()
+        ms = b.time_steps(steps)
+        builds = b.list_builds() - b0
+        prof = b.profile(5)
+        out = {"value": b.n * steps / (ms * 1e-3), "ms_per_step": ms / steps,
+               "phases_ms": {k: round(v, 5) for k, v in prof.items()},
+               "launches": steps * b.launches_per_step() + builds * b.launches_per_rebuild()}
+        if sk > 0:
+            out["list_builds"] = builds
+        n = b.n
+        b.close()
+        return out, n
+
+    listed, n = timed(batch.replicas(psim, draws, skin=skin), skin)
     t0 = time.time()
     factors, report = batch.autotune(psim, draws, device=dev) if tune else ([1.0] * n_reps, {})
     t_tune = time.time() - t0
-    pos, vel = batch.states(draws)
-    b = psim.Batch(batch.replicas(psim, draws, factors), gamma=1.0, dt=0.001, kT=1.0,
-                   vel_freq=1000, precision=psim.PRECISION_MIXED, device=dev)
-    b.upload(pos, np.full(b.n, 0.5), vel=vel)
-    b.step(3)
-    ms = b.time_steps(steps)
-    prof = b.profile(5)
-    value = b.n * steps / (ms * 1e-3)
-    b.close()
-    return {"workload": "c2_%d_ao_replicas" % n_reps, "value": value, "unit": UNIT,
-            "n_particles": int(b.n), "replicas": n_reps, "steps": steps,
-            "ms_per_step": ms / steps, "launches_per_step": 7,
-            "phases_ms": {k: round(v, 5) for k, v in prof.items()},
-            "autotune": {"seconds": round(t_tune, 1),
-                         "buckets": {str(k): {"factor": v[0],
-                                              "rates": {str(f): r for f, r in v[1].items()}}
-                                     for k, v in report.items()}}}
+    walk, _ = timed(batch.replicas(psim, draws, factors), 0.0)
+    walk["autotune"] = {"seconds": round(t_tune, 1),
+                        "buckets": {str(k): {"factor": v[0],
+                                             "rates": {str(f): r for f, r in v[1].items()}}
+                                    for k, v in report.items()}}
+    out = {"workload": "c2_%d_ao_replicas" % n_reps, "unit": UNIT, "n_particles": int(n),
+           "replicas": n_reps, "steps": steps, "skin": skin}
+    out.update(listed)
+    out["cell_walk"] = walk
+    return out
 
 
 def run_differentiable(psim, dev, steps=2000):

@@ -1314,7 +1314,7 @@ int cell_refs(psim_system* s, CellRefs& c) {
 }  // namespace
 
 namespace {
-psim_system* system_new(const psim_system_config* cfg, const DevGeom& g);
+psim_system* system_new(const psim_system_config* cfg, const DevGeom& g, bool batch = false);
 
 // The pair list's sizes for cutoff rc, skin and grid g: the entries per
 // particle (room for 1.5x the mean number of neighbours within rc + skin,
@@ -1439,7 +1439,7 @@ psim_system* psim_batch_create_list(const psim_replica* reps, int32_t n_reps,
         fail(PSIM_ERR_INPUT, "unknown noise mode %d", noise_mode);
         return nullptr;
     }
-    psim_system* s = system_new(&cfg, gt);
+    psim_system* s = system_new(&cfg, gt, true);
     if (!s) return nullptr;
     DeviceGuard dg(s->device);
     s->fs.tile = 0;
@@ -1525,7 +1525,7 @@ namespace {
 
 // The system's streams, events and buffers for grid g (the whole batch's
 // particles and cells for a batch); validates the rest of cfg.
-psim_system* system_new(const psim_system_config* cfg, const DevGeom& g) {
+psim_system* system_new(const psim_system_config* cfg, const DevGeom& g, bool batch) {
     VgbParams vp;
     if (make_vgb_params(&cfg->integ, &vp)) return nullptr;
     const double rc = max_cutoff(&cfg->force);
@@ -1564,7 +1564,8 @@ psim_system* system_new(const psim_system_config* cfg, const DevGeom& g) {
     s->n = g.n;
     s->ncell = g.ncell;
     if (list_on) {
-        const ListSizes z = list_sizes(rc, skin, g);
+        // (a batch sizes its list per replica once its tables are made)
+        const ListSizes z = batch ? ListSizes{0, 0.f, 0.f, 0.f, 0} : list_sizes(rc, skin, g);
         s->list_on = true;
         s->skin = skin;
         s->lcap = z.cap;
