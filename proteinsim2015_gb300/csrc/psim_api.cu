@@ -646,10 +646,16 @@ int psim_force_evaluate(const psim_force_params* params, const psim_geometry* gm
 
 // ------------------------------------------------------------ integrator
 
+constexpr int kAosChunks = 8;   // chunks of the drop-in integrator's copies
+
 struct psim_integrator {
     int device = 0;
     int n = 0;
     cudaStream_t st = nullptr;
+    // the copies in and out run on their own streams, chunk by chunk, so that
+    // they overlap each other and the update of the chunks before
+    cudaStream_t st_in = nullptr, st_out = nullptr;
+    cudaEvent_t ev_in[kAosChunks] = {}, ev_run[kAosChunks] = {};
     VgbParams vp{};
     int vel_counter = 0;
     long long steps = 0;
@@ -668,7 +674,12 @@ psim_integrator* psim_integrator_create(const psim_integrator_config* cfg, int32
     it->vp = vp;
     cudaGetDevice(&it->device);
     const size_t b = 24 * (size_t)n;
-    if (cudaStreamCreateWithFlags(&it->st, cudaStreamNonBlocking) != cudaSuccess ||
+    bool ev_ok = cudaStreamCreateWithFlags(&it->st_in, cudaStreamNonBlocking) == cudaSuccess &&
+                 cudaStreamCreateWithFlags(&it->st_out, cudaStreamNonBlocking) == cudaSuccess;
+    for (int k = 0; k < kAosChunks && ev_ok; ++k)
+        ev_ok = cudaEventCreateWithFlags(&it->ev_in[k], cudaEventDisableTiming) == cudaSuccess &&
+                cudaEventCreateWithFlags(&it->ev_run[k], cudaEventDisableTiming) == cudaSuccess;
+    if (!ev_ok || cudaStreamCreateWithFlags(&it->st, cudaStreamNonBlocking) != cudaSuccess ||
         it->mem.ensure(b) || it->mem_corr.ensure(b) || it->pos.ensure(b) || it->pos0.ensure(b) ||
         it->vel.ensure(b) || it->frc.ensure(b) || it->frc0.ensure(b) ||
         it->mass.ensure(8 * (size_t)n) || it->err.ensure(4) ||
@@ -688,6 +699,12 @@ void psim_integrator_destroy(psim_integrator* it) {
     DevBuf* all[] = {&it->mem, &it->mem_corr, &it->pos, &it->pos0, &it->vel, &it->frc,
                      &it->frc0, &it->mass, &it->noise, &it->err};
     for (DevBuf* b : all) b->release();
+    for (int k = 0; k < kAosChunks; ++k) {
+        if (it->ev_in[k]) cudaEventDestroy(it->ev_in[k]);
+        if (it->ev_run[k]) cudaEventDestroy(it->ev_run[k]);
+    }
+    if (it->st_in) cudaStreamDestroy(it->st_in);
+    if (it->st_out) cudaStreamDestroy(it->st_out);
     if (it->st) cudaStreamDestroy(it->st);
     cudaSetDevice(prev);
     delete it;
@@ -706,53 +723,81 @@ int psim_integrator_next_system(psim_integrator* it, double current_time, double
     int prev = 0;
     PSIM_CUDA(cudaGetDevice(&prev));
     PSIM_CUDA(cudaSetDevice(it->device));
-    const size_t n = (size_t)it->n, b = 24 * n;
+    const size_t n = (size_t)it->n;
     cudaStream_t st = it->st;
-    PSIM_CUDA(cudaMemcpyAsync(it->pos.p, pos, b, cudaMemcpyHostToDevice, st));
-    PSIM_CUDA(cudaMemcpyAsync(it->pos0.p, pos0, b, cudaMemcpyHostToDevice, st));
-    PSIM_CUDA(cudaMemcpyAsync(it->vel.p, vel, b, cudaMemcpyHostToDevice, st));
-    if (particle_force) {  // pushParticleForce: frc0 <- frc, frc <- particleForce
-        PSIM_CUDA(cudaMemcpyAsync(it->frc0.p, frc, b, cudaMemcpyHostToDevice, st));
-        PSIM_CUDA(cudaMemcpyAsync(it->frc.p, particle_force, b, cudaMemcpyHostToDevice, st));
-    } else {
-        PSIM_CUDA(cudaMemcpyAsync(it->frc.p, frc, b, cudaMemcpyHostToDevice, st));
-        PSIM_CUDA(cudaMemcpyAsync(it->frc0.p, frc0, b, cudaMemcpyHostToDevice, st));
-    }
-    PSIM_CUDA(cudaMemcpyAsync(it->mass.p, mass, 8 * n, cudaMemcpyHostToDevice, st));
-    const double* dnoise = nullptr;
-    if (noise_mode == PSIM_NOISE_INJECTED) {
-        PSIM_CUDA(it->noise.ensure(48 * n));
-        PSIM_CUDA(cudaMemcpyAsync(it->noise.p, noise, 48 * n, cudaMemcpyHostToDevice, st));
-        dnoise = it->noise.as<double>();
-    }
-    PSIM_CUDA(cudaMemsetAsync(it->err.p, 0, 4, st));
     const bool first = (current_time == 0);  // nextSystem, brownianIntegrator.cpp:183
-    VgbAosArgs a{};
-    a.n = it->n;
-    a.first = first ? 1 : 0;
-    a.vel_step = (!first && (it->vp.vel_freq == 0 || it->vel_counter == it->vp.vel_freq)) ? 1 : 0;
-    a.pos = it->pos.as<double>();
-    a.pos0 = it->pos0.as<double>();
-    a.vel = it->vel.as<double>();
-    a.frc = it->frc.as<double>();
-    a.frc0 = it->frc0.as<double>();
-    a.mass = it->mass.as<double>();
-    a.mem = it->mem.as<double>();
-    a.mem_corr = it->mem_corr.as<double>();
-    a.noise = dnoise;
-    a.seed = it->vp.seed;
-    a.philox_step = it->steps;
-    a.err = it->err.as<uint32_t>();
-    PSIM_CUDA(launch_vgb_aos(a, it->vp, box, st));
+    const bool vel_step = !first && (it->vp.vel_freq == 0 || it->vel_counter == it->vp.vel_freq);
+    // the previous force and this one on the device (pushParticleForce:
+    // frc0 <- frc, frc <- particleForce)
+    const double* F0 = particle_force ? frc : frc0;
+    const double* F = particle_force ? particle_force : frc;
+    if (noise_mode == PSIM_NOISE_INJECTED) PSIM_CUDA(it->noise.ensure(48 * n));
+    PSIM_CUDA(cudaMemsetAsync(it->err.p, 0, 4, st));
+    cudaEvent_t ev0 = it->ev_run[0];
+    PSIM_CUDA(cudaEventRecord(ev0, st));   // the error word is cleared before any chunk runs
+    PSIM_CUDA(cudaStreamWaitEvent(it->st_in, ev0, 0));
+    // chunks of whole particles: copies in (st_in), the update (st), copies out
+    // (st_out); velocities move only when the step reads (firstStep) or writes
+    // (velocityStep) them
+    const size_t chunk = (n + kAosChunks - 1) / kAosChunks;
+    for (int k = 0; k < kAosChunks; ++k) {
+        const size_t a0 = std::min(n, (size_t)k * chunk), a1 = std::min(n, a0 + chunk);
+        const size_t m = a1 - a0;
+        if (m == 0) continue;
+        const size_t o3 = 3 * a0, b3 = 24 * m;
+        auto in = [&](DevBuf& d, const double* h, size_t off, size_t bytes) {
+            return cudaMemcpyAsync(d.as<double>() + off, h + off, bytes, cudaMemcpyHostToDevice,
+                                   it->st_in);
+        };
+        PSIM_CUDA(in(it->pos, pos, o3, b3));
+        PSIM_CUDA(in(it->pos0, pos0, o3, b3));
+        PSIM_CUDA(in(it->frc0, F0, o3, b3));
+        PSIM_CUDA(in(it->frc, F, o3, b3));
+        PSIM_CUDA(in(it->mass, mass, a0, 8 * m));
+        if (first || vel_step) PSIM_CUDA(in(it->vel, vel, o3, b3));
+        if (noise_mode == PSIM_NOISE_INJECTED) PSIM_CUDA(in(it->noise, noise, 6 * a0, 48 * m));
+        PSIM_CUDA(cudaEventRecord(it->ev_in[k], it->st_in));
+        PSIM_CUDA(cudaStreamWaitEvent(st, it->ev_in[k], 0));
+        VgbAosArgs a{};
+        a.n = (int)m;
+        a.offset = (int)a0;
+        a.first = first ? 1 : 0;
+        a.vel_step = vel_step ? 1 : 0;
+        a.pos = it->pos.as<double>() + o3;
+        a.pos0 = it->pos0.as<double>() + o3;
+        a.vel = it->vel.as<double>() + o3;
+        a.frc = it->frc.as<double>() + o3;
+        a.frc0 = it->frc0.as<double>() + o3;
+        a.mass = it->mass.as<double>() + a0;
+        a.mem = it->mem.as<double>() + o3;
+        a.mem_corr = it->mem_corr.as<double>() + o3;
+        a.noise = noise_mode == PSIM_NOISE_INJECTED ? it->noise.as<double>() + 6 * a0 : nullptr;
+        a.seed = it->vp.seed;
+        a.philox_step = it->steps;
+        a.err = it->err.as<uint32_t>();
+        PSIM_CUDA(launch_vgb_aos(a, it->vp, box, st));
+        PSIM_CUDA(cudaEventRecord(it->ev_run[k], st));
+        // the pushed forces back to the host arrays as soon as they are in
+        if (particle_force) {
+            PSIM_CUDA(cudaStreamWaitEvent(it->st_out, it->ev_in[k], 0));
+            PSIM_CUDA(cudaMemcpyAsync(frc0 + o3, it->frc0.as<double>() + o3, b3,
+                                      cudaMemcpyDeviceToHost, it->st_out));
+            PSIM_CUDA(cudaMemcpyAsync(frc + o3, it->frc.as<double>() + o3, b3,
+                                      cudaMemcpyDeviceToHost, it->st_out));
+        }
+        PSIM_CUDA(cudaStreamWaitEvent(it->st_out, it->ev_run[k], 0));
+        PSIM_CUDA(cudaMemcpyAsync(pos + o3, it->pos.as<double>() + o3, b3,
+                                  cudaMemcpyDeviceToHost, it->st_out));
+        PSIM_CUDA(cudaMemcpyAsync(pos0 + o3, it->pos0.as<double>() + o3, b3,
+                                  cudaMemcpyDeviceToHost, it->st_out));
+        if (vel_step)
+            PSIM_CUDA(cudaMemcpyAsync(vel + o3, it->vel.as<double>() + o3, b3,
+                                      cudaMemcpyDeviceToHost, it->st_out));
+    }
     uint32_t bits = 0;
     PSIM_CUDA(cudaMemcpyAsync(&bits, it->err.p, 4, cudaMemcpyDeviceToHost, st));
-    PSIM_CUDA(cudaMemcpyAsync(pos, it->pos.p, b, cudaMemcpyDeviceToHost, st));
-    PSIM_CUDA(cudaMemcpyAsync(pos0, it->pos0.p, b, cudaMemcpyDeviceToHost, st));
-    PSIM_CUDA(cudaMemcpyAsync(vel, it->vel.p, b, cudaMemcpyDeviceToHost, st));
-    if (particle_force) {
-        PSIM_CUDA(cudaMemcpyAsync(frc0, it->frc0.p, b, cudaMemcpyDeviceToHost, st));
-        PSIM_CUDA(cudaMemcpyAsync(frc, it->frc.p, b, cudaMemcpyDeviceToHost, st));
-    }
+    PSIM_CUDA(cudaStreamSynchronize(it->st_in));
+    PSIM_CUDA(cudaStreamSynchronize(it->st_out));
     PSIM_CUDA(cudaStreamSynchronize(st));
     if (!first)  // brownianIntegrator.cpp:291-292
         it->vel_counter = (it->vel_counter == it->vp.vel_freq) ? 0 : it->vel_counter + 1;

@@ -193,6 +193,7 @@ cudaError_t launch_vgb_system_fast(const VgbSystemArgs& a, const VgbParams& p, c
 // in original order).  mem/mem_corr: 3n device arrays owned by the integrator.
 struct VgbAosArgs {
     int n;
+    int offset;             // index of the first particle (arrays start there): its noise key
     int first;
     int vel_step;
     double* pos; double* pos0; double* vel;

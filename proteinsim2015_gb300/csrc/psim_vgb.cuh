@@ -407,7 +407,7 @@ __global__ void __launch_bounds__(256) vgb_aos_kernel(VgbAosArgs a, VgbParams p,
 #pragma unroll
         for (int k = 0; k < 6; ++k) xi[k] = a.noise[6 * (size_t)i + k];
     } else {
-        philox_gaussians6(a.seed, (uint32_t)i, (uint32_t)a.philox_step, xi);
+        philox_gaussians6(a.seed, (uint32_t)(a.offset + i), (uint32_t)a.philox_step, xi);
     }
     const double m = 1.0 / a.mass[i];
     vgb_particle(p, L, L / 2, a.first != 0, a.vel_step != 0, x, x0, mx, mc, F, F0, v, xi, m, xn,

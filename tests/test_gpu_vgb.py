@@ -69,3 +69,20 @@ def test_gamma_zero_is_refused(psim):
     with pytest.raises(psim.PsimError) as e:
         psim.Integrator(10, gamma=0.0)
     assert e.value.code == psim.ERR_INPUT
+
+
+def test_philox_noise_is_keyed_by_particle(psim):
+    # the copies and the update run in chunks: every particle keeps its own
+    # Philox stream (no two particles move alike without forces)
+    n, box = 4096, 40.0
+    rng = np.random.default_rng(5)
+    pos = rng.uniform(5.0, 35.0, 3 * n)
+    z = np.zeros(3 * n)
+    it = psim.Integrator(n, gamma=1.0, dt=0.001, kT=1.0, vel_freq=1000, seed=77)
+    p, p0, v, f, f0 = pos.copy(), pos.copy(), z.copy(), z.copy(), z.copy()
+    for step in range(3):
+        it.next_system(step * 0.001, box, p, p0, v, f, f0, np.ones(n), particle_force=z)
+    d = (p - pos).reshape(-1, 3)
+    assert np.all(np.isfinite(d)) and np.unique(d, axis=0).shape[0] == n
+    assert 0.5 < np.var(d) / np.var(d[: n // 8]) < 2.0   # the same spread in every chunk
+    it.close()
