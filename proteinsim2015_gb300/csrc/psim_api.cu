@@ -206,6 +206,34 @@ float prefilter_r2(double r, double L) {
     return (float)(rpre * rpre * (1.0 + 1e-6));
 }
 
+// The pair list's sizes for cutoff rc, skin and grid g: the entries per
+// particle (room for 1.5x the mean number of neighbours within rc + skin,
+// + 32), the list radius squared (the FP32 test's widened bound), the
+// rebuild test's displacement squared (half the skin, less the FP32 rounding
+// of the positions, each off by ulp(L)/2), the halo radius (beyond the list
+// test's radius, so every pair the build finds across an edge has an image)
+// and the halo records to hold.
+struct ListSizes {
+    int cap;
+    float pre, disp2, hr;
+    int hcap;
+};
+ListSizes list_sizes(double rc, double skin, const DevGeom& g) {
+    ListSizes z{};
+    const double rl = rc + skin;
+    const double mean = 4.0 / 3.0 * M_PI * rl * rl * rl * g.n / (g.L * g.L * g.L);
+    z.cap = ((int)(1.5 * mean) + 32 + 31) / 32 * 32;
+    z.pre = prefilter_r2(rl, g.L);
+    const double ulpL = std::ldexp(1.0, std::ilogb(std::max(g.L, 1.0)) - 23);
+    const double dmax = 0.5 * skin * (1.0 - 1e-3) - 4.0 * ulpL;
+    z.disp2 = dmax > 0.0 ? (float)(dmax * dmax) : 0.f;
+    z.hr = (float)(std::sqrt((double)z.pre) + 1e-3 * rl + 16.0 * ulpL);
+    const double p = 2.0 * z.hr / g.L;   // a particle's chance of an image per axis
+    const double expect = g.n * ((1.0 + p) * (1.0 + p) * (1.0 + p) - 1.0);
+    z.hcap = (int)std::min(std::min(7.0 * g.n, 1.3 * expect + 1024.0), (double)kHaloBaseMax);
+    return z;
+}
+
 ForceSetup make_setup(const psim_force_params* p, double L) {
     ForceSetup fs{};
     fs.kind = p->kind;
@@ -393,6 +421,8 @@ struct Workspace {
     cudaStream_t st = nullptr;
     DevBuf pos, radius, xyz, key, rank, tmp, perm, tag_in, tag_out, radius_out, cellid, count,
         start, scratch, posd, posh, posl, hash_index, cse, sorted, force, fxyz, err;
+    // the mixed form's one-call pair list (records, halo words and count, entries)
+    DevBuf lpos, lhalo, lhcount, list, lcount;
 };
 Workspace g_ws;
 
@@ -404,7 +434,7 @@ int ws_begin(Workspace& w) {
         DevBuf* all[] = {&w.pos, &w.radius, &w.xyz, &w.key, &w.rank, &w.tmp, &w.perm, &w.tag_in,
                          &w.tag_out, &w.radius_out, &w.cellid, &w.count, &w.start, &w.scratch,
                          &w.posd, &w.posh, &w.posl, &w.hash_index, &w.cse, &w.sorted, &w.force,
-                         &w.fxyz, &w.err};
+                         &w.fxyz, &w.err, &w.lpos, &w.lhalo, &w.lhcount, &w.list, &w.lcount};
         for (DevBuf* b : all) { b->p = nullptr; b->bytes = 0; }
         w.st = nullptr;
     }
@@ -629,10 +659,46 @@ int psim_force_evaluate(const psim_force_params* params, const psim_geometry* gm
     CellView cv{w.posd.as<double4_32a>(), w.posh.as<float4>(), w.posl.as<float4>(),
                 w.cellid.as<int>(), w.start.as<int>(), w.count.as<int>()};
     ForceOut out{f, f + n, f + 2 * n, w.err.as<uint32_t>()};
-    if (precision == PSIM_PRECISION_FP64)
+    // the mixed form through a pair list of this call's pairs (radius rc, no
+    // skin): building it and walking it costs about half the 27-cell walk
+    const ListSizes z = list_sizes(max_cutoff(params), 0.0, g);
+    const bool one_list = precision == PSIM_PRECISION_MIXED &&
+                          (double)(z.cap + kListFold) * (double)g.n < 4294967296.0;
+    if (precision == PSIM_PRECISION_FP64) {
         PSIM_CUDA(launch_forces_fp64(fs, g, cv, out, st));
-    else
+    } else if (one_list) {
+        PSIM_CUDA(w.lpos.ensure(32 * (n + 1 + (size_t)z.hcap)));
+        PSIM_CUDA(w.lhalo.ensure(4 * n));
+        PSIM_CUDA(w.lhcount.ensure(4));
+        PSIM_CUDA(w.list.ensure(4 * n * (size_t)(z.cap + kListFold)));
+        PSIM_CUDA(w.lcount.ensure(4 * n));
+        PSIM_CUDA(cudaMemsetAsync(w.lhcount.p, 0, 4, st));
+        // the ghost record that pads the lists, far from every particle
+        static const float4 ghost[2] = {make_float4(1e18f, 1e18f, 1e18f, 0.f),
+                                        make_float4(0.f, 0.f, 0.f, 0.f)};
+        PSIM_CUDA(cudaMemcpyAsync(w.lpos.as<float4>() + 2 * n, ghost, 32, cudaMemcpyHostToDevice,
+                                  st));
+        PSIM_CUDA(launch_list_records(g.n, w.posh.as<float4>(), w.posl.as<float4>(),
+                                      w.lpos.as<float4>(), w.lhalo.as<int>(), w.lhcount.as<int>(),
+                                      z.hcap, z.hr, g, w.err.as<uint32_t>(), st));
+        ListBuild lb{w.list.as<uint32_t>(), w.lcount.as<int>(), g.n, z.cap, z.pre, nullptr,
+                     w.lhalo.as<int>(), g.n};
+        PSIM_CUDA(launch_list_build(g, cv, lb, w.err.as<uint32_t>(), st));
+        PSIM_CUDA(cudaMemcpyAsync(&bits, w.err.p, 4, cudaMemcpyDeviceToHost, st));
+        PSIM_CUDA(cudaStreamSynchronize(st));
+        if (bits == EBIT_LIST) {
+            // a denser neighbourhood than the list has room for: the cell walk
+            bits = 0;
+            PSIM_CUDA(cudaMemsetAsync(w.err.p, 0, 4, st));
+            PSIM_CUDA(launch_forces_mixed(fs, g, cv, out, st));
+        } else {
+            const PairList pl{nullptr, w.lpos.as<float4>(), w.lcount.as<int>(),
+                              w.list.as<uint32_t>(), g.n, 0, 0.f, 0.f};
+            PSIM_CUDA(launch_forces_list(fs, g, pl, out, st));
+        }
+    } else {
         PSIM_CUDA(launch_forces_mixed(fs, g, cv, out, st));
+    }
     PSIM_CUDA(launch_unsort_force(g.n, w.tag_out.as<int>(), f, f + n, f + 2 * n,
                                   w.force.as<double>(), st));
     PSIM_CUDA(cudaMemcpyAsync(&bits, w.err.p, 4, cudaMemcpyDeviceToHost, st));
@@ -1361,33 +1427,6 @@ int cell_refs(psim_system* s, CellRefs& c) {
 namespace {
 psim_system* system_new(const psim_system_config* cfg, const DevGeom& g, bool batch = false);
 
-// The pair list's sizes for cutoff rc, skin and grid g: the entries per
-// particle (room for 1.5x the mean number of neighbours within rc + skin,
-// + 32), the list radius squared (the FP32 test's widened bound), the
-// rebuild test's displacement squared (half the skin, less the FP32 rounding
-// of the positions, each off by ulp(L)/2), the halo radius (beyond the list
-// test's radius, so every pair the build finds across an edge has an image)
-// and the halo records to hold.
-struct ListSizes {
-    int cap;
-    float pre, disp2, hr;
-    int hcap;
-};
-ListSizes list_sizes(double rc, double skin, const DevGeom& g) {
-    ListSizes z{};
-    const double rl = rc + skin;
-    const double mean = 4.0 / 3.0 * M_PI * rl * rl * rl * g.n / (g.L * g.L * g.L);
-    z.cap = ((int)(1.5 * mean) + 32 + 31) / 32 * 32;
-    z.pre = prefilter_r2(rl, g.L);
-    const double ulpL = std::ldexp(1.0, std::ilogb(std::max(g.L, 1.0)) - 23);
-    const double dmax = 0.5 * skin * (1.0 - 1e-3) - 4.0 * ulpL;
-    z.disp2 = dmax > 0.0 ? (float)(dmax * dmax) : 0.f;
-    z.hr = (float)(std::sqrt((double)z.pre) + 1e-3 * rl + 16.0 * ulpL);
-    const double p = 2.0 * z.hr / g.L;   // a particle's chance of an image per axis
-    const double expect = g.n * ((1.0 + p) * (1.0 + p) * (1.0 + p) - 1.0);
-    z.hcap = (int)std::min(std::min(7.0 * g.n, 1.3 * expect + 1024.0), (double)kHaloBaseMax);
-    return z;
-}
 }
 
 extern "C" {

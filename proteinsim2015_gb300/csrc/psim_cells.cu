@@ -486,6 +486,45 @@ cudaError_t launch_pair_count(const DevGeom& g, const CellView& cv, float rc2,
     return cudaGetLastError();
 }
 
+// The pair-list records of a sorted order, one 32-byte float-pair record per
+// slot (radius in the high part), and the halo images of the particles within
+// hr of a face (the list records the canonicalisation writes, for positions
+// that are already sorted).
+__global__ void __launch_bounds__(256)
+list_records_kernel(int n, const float4* posh, const float4* posl, float4* lpos, int* lhalo,
+                    int* lhcount, int hcap, float hr, float Lf, float Lhi, float Llo,
+                    uint32_t* err) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n || *err) return;
+    const float4 h = posh[g];
+    float4 l = posl[g];
+    l.w = 0.f;
+    store_record(lpos, 0.f, (size_t)g, h, l);
+    uint32_t fl = halo_flags(h, hr, Lf);
+    const int m = halo_copies(fl);
+    int base = 0;
+    if (m > 0) {
+        base = atomicAdd(lhcount, m);
+        if (base + m > hcap) {
+            atomicOr(err, EBIT_LIST);
+            fl = 0;
+            base = 0;
+        } else {
+            halo_write(lpos + 2 * ((size_t)n + 1), 0.f, base, fl, h, l, Lhi, Llo);
+        }
+    }
+    lhalo[g] = (base << 6) | (int)fl;
+}
+
+cudaError_t launch_list_records(int n, const float4* posh, const float4* posl, float4* lpos,
+                                int* lhalo, int* lhcount, int hcap, float hr, const DevGeom& g,
+                                uint32_t* err, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    list_records_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, posh, posl, lpos, lhalo, lhcount, hcap,
+                                                         hr, (float)g.L, g.Lhi, g.Llo, err);
+    return cudaGetLastError();
+}
+
 __global__ void step_end_kernel(StepState* state, const int* lflag, const uint32_t* err,
                                 int vel_freq, cudaGraphConditionalHandle handle, int use_handle) {
     const int rebuild = (*err == 0 && *lflag != 0) ? 1 : 0;

@@ -272,6 +272,13 @@ struct CanonArgs {
 };
 cudaError_t launch_canonicalize(const CanonArgs& a, cudaStream_t st);
 
+// Full 32-byte pair-list records of the sorted positions (posh, posl) and
+// the halo images of the particles within hr of a face (lhalo per slot,
+// records n + 1 + [0, hcap) handed out by *lhcount, zeroed by the caller).
+cudaError_t launch_list_records(int n, const float4* posh, const float4* posl, float4* lpos,
+                                int* lhalo, int* lhcount, int hcap, float hr, const DevGeom& g,
+                                uint32_t* err, cudaStream_t st);
+
 // End of a step whose cell list is rebuilt only with its pair list: advances
 // the step state (canonicalize_kernel's bookkeeping) and decides the rebuild
 // -- the flag the integrator raised, unless an error is latched.  In a graph
