@@ -235,6 +235,14 @@ typedef struct {
 int psim_init_rsa(int32_t n, double box, double min_sep, uint64_t seed, int64_t max_trials,
                   double* pos);
 
+/* The same construction on a GPU: the same trials in the same order (a trial
+ * is kept when no earlier kept trial lies within min_sep), evaluated in
+ * chunks of trials in parallel; the result is psim_init_rsa's for the same
+ * arithmetic.  Falls back to psim_init_rsa for boxes of fewer than 3 cells of
+ * min_sep a side. */
+int psim_init_rsa_device(int32_t n, double box, double min_sep, uint64_t seed,
+                         int64_t max_trials, double* pos, int32_t device);
+
 /* ------------------------------------------- differentiable trajectory */
 
 /* Gradients of a trajectory loss with the noise held fixed (no reference

@@ -121,6 +121,8 @@ def lib():
             "psim_integrator_next_system": ([P, C.c_double, C.c_double, C.c_int32] + [P] * 8, C.c_int),
             "psim_init_rsa": ([C.c_int32, C.c_double, C.c_double, C.c_uint64, C.c_int64, P],
                               C.c_int),
+            "psim_init_rsa_device": ([C.c_int32, C.c_double, C.c_double, C.c_uint64, C.c_int64,
+                                      P, C.c_int32], C.c_int),
             "psim_system_create": ([C.POINTER(SystemConfig)], P),
             "psim_batch_create": ([C.POINTER(Replica), C.c_int32, C.POINTER(IntegratorConfig),
                                    C.c_int32, C.c_int32, C.c_int32], P),

@@ -27,7 +27,8 @@ SOURCES = {
     "psim_cells.cu": [],
     "psim_api.cu": [],
     "psim_noalloc.cu": [],
-    "psim_init.cu": [],
+    # host and device evaluate the RSA trials with the same IEEE operations
+    "psim_init.cu": ["--fmad=false", "-Xcompiler", "-ffp-contract=off"],
     "psim_observe.cu": [],
     "psim_adjoint.cu": ["--fmad=false"],
 }

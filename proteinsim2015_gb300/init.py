@@ -26,14 +26,22 @@ def reference_box(n, radius, conc, scale):
     return box, cell, vp / float(box) ** 3
 
 
-def rsa_native(n, box, min_sep=1.0, seed=90210, max_trials=0):
-    """Random sequential addition in the native library (host code, O(1) per
-    trial): the same construction as rsa() with its own random stream, fast
-    enough for batches of millions of particles."""
+def rsa_native(n, box, min_sep=1.0, seed=90210, max_trials=0, device=None):
+    """Random sequential addition in the native library (O(1) per trial): the
+    same construction as rsa() with its own random stream.  device: a GPU
+    that evaluates the trials in parallel chunks (the same result); None
+    picks GPU 0 for n >= 2^17 when one is present, else the host."""
     import proteinsim2015_gb300 as psim
     out = np.empty(3 * int(n))
-    rc = psim.lib().psim_init_rsa(int(n), float(box), float(min_sep), int(seed) & (2 ** 64 - 1),
-                                  int(max_trials), out.ctypes.data)
+    if device is None and int(n) >= (1 << 17) and psim.device_count() > 0:
+        device = 0
+    if device is not None:
+        rc = psim.lib().psim_init_rsa_device(int(n), float(box), float(min_sep),
+                                             int(seed) & (2 ** 64 - 1), int(max_trials),
+                                             out.ctypes.data, int(device))
+    else:
+        rc = psim.lib().psim_init_rsa(int(n), float(box), float(min_sep),
+                                      int(seed) & (2 ** 64 - 1), int(max_trials), out.ctypes.data)
     if rc != 0:
         raise psim.PsimError(rc, psim.lib().psim_last_error_string().decode())
     return out.reshape(-1, 3)

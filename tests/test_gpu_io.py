@@ -68,3 +68,18 @@ def test_post_analysis_histograms_match_all_pairs(psim, tmp_path):
     assert open(files[1]).read() == io.histogram_text([len(g) for g in groups])
     assert open(files[2]).read() == io.histogram_text(coor[np.concatenate(groups)])
     s.close()
+
+
+def test_device_rsa_is_the_host_rsa(psim):
+    # the same trials in the same order, kept by the same rule: chunks of
+    # trials evaluated in parallel give the host's sequence exactly
+    from proteinsim2015_gb300 import init
+    for n, phi, seed in ((20000, 0.30, 5), (3000, 0.05, 6), (5000, 0.34, 7)):
+        box = (n * np.pi / 6.0 / phi) ** (1.0 / 3.0)
+        host = init.rsa_native(n, box, 1.0, seed=seed)   # n < 2^17: on the host
+        dev = init.rsa_native(n, box, 1.0, seed=seed, device=0)
+        assert np.array_equal(host, dev), (n, phi)
+        d = dev[:, None, :] - dev[None, :200, :]
+        d -= box * np.round(d / box)
+        r = np.sqrt(np.sum(d * d, axis=2))
+        assert np.sum(r < 1.0 - 1e-12) == 200   # only the particles themselves
