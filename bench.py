@@ -297,8 +297,13 @@ def e2e_dropin(psim, w, state, n_steps):
         psim.cells_build(g, buf["pos"], rad, out=cells)
         t_cur += DT
     el = time.perf_counter() - t0
-    h2d = (32 * n + 8 * n + 8 * ncell) + (24 * n * 6 + 8 * n) + (24 * n + 8 * n)
-    d2h = 24 * n + 24 * n * 5 + (8 * n + 8 * ncell + 32 * n)
+    # per step: force_evaluate (sorted, hash index, cell ranges in; force out),
+    # next_system (positions, previous positions, the two forces, masses in;
+    # positions, previous positions and the pushed forces out -- velocities
+    # move only on the first and velocity steps), cells_build (positions,
+    # radii in; hash index, cell ranges, sorted out)
+    h2d = (32 * n + 8 * n + 8 * ncell) + (4 * 24 * n + 8 * n) + (24 * n + 8 * n)
+    d2h = 24 * n + 4 * 24 * n + (8 * n + 8 * ncell + 32 * n)
     it.close()
     return n * n_steps / el, h2d, d2h
 
