@@ -20,8 +20,9 @@ the CPU implementation of the path (oracle/_ref when present, else the
 oracle's restatement) on the host cores.  Sub-objects of the line report the
 other workloads on the same GPU: `batched` (512 AO replicas in one set of
 launches), `differentiable` (the adjoint of a 2,000-step AO + Yukawa
-trajectory, N = 32768) and `gel` (2^23 aggregating AO colloids, with the
-cell occupancy over time).
+trajectory, N = 32768), `gel` (2^23 aggregating AO colloids, with the
+cell occupancy over time) and `c0` (the reference's own 4000-particle AO
+case, with the CPU port beside it).
 """
 import argparse
 import json
@@ -426,6 +427,53 @@ def run_gel(psim, dev, steps=1000, skin=0.3, chunk=100):
     return out
 
 
+def run_c0(psim, dev, steps=10000, cpu_budget_s=3.0):
+    """The reference's own CPU-runnable case: N = 4000 AO colloids (cutOff 1.1,
+    wellDepth 0.25: -4 kT at contact) in the box the reference can represent,
+    L = 21 with 7 cells a side (phi = 0.226), gamma = 1, dt = 1e-3, kT = 1,
+    10,000 steps from a seeded RSA start with Maxwell-Boltzmann velocities: on
+    the GPU in the mixed form with a pair list and in the plain FP64 form, and
+    the oracle port (the CPU baseline) on all host cores over a few seconds."""
+    from proteinsim2015_gb300 import init
+    n, L, scale = 4000, 21.0, 7
+    g = psim.geometry(n, L, L / scale, scale)
+    f = psim.make_force("AO", 1.1, kT=1.0, well_depth=0.25)
+    pos = init.rsa_native(n, L, 1.0, seed=90210).reshape(-1)
+    vel = init.maxwell(n, 1.0, seed=90211).reshape(-1)
+    out = {"workload": "c0_ao_N4000_L21", "n_particles": n, "steps": steps, "unit": UNIT}
+    for name, prec, skin in (("mixed_list", psim.PRECISION_MIXED, psim.auto_skin(g, f)),
+                             ("plain_fp64", psim.PRECISION_FP64, 0.0)):
+        s = psim.System(g, f, gamma=1.0, dt=0.001, kT=1.0, vel_freq=1000, seed=7, precision=prec,
+                        device=dev, skin=skin)
+        s.upload(pos, np.full(n, 0.5), vel=vel)
+        s.step(3)
+        ms = s.time_steps(steps)
+        out[name] = {"value": n * steps / (ms * 1e-3), "ms_per_step": ms / steps, "skin": skin}
+        s.close()
+    from oracle import port
+    cores = os.cpu_count() or 1
+    port.set_threads(cores)
+    pg = port.geom(n, L, L / scale, scale)
+    pf = port.make_force(port.AO, 1.1, kT=1.0, well_depth=0.25)
+    c = port.vgb_coeffs(1.0, 0.001, 1.0)
+    st = port.State(pos, np.full(n, 0.5), vel=vel)
+    cells = None
+    done, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < cpu_budget_s:
+        err, hi, cse, srt, _ = port.run(pg, pf, c, 0.001, st, 50, None, vel_freq=1000,
+                                        cells=cells)
+        cells = (hi, cse, srt)
+        if err:
+            break
+        done += 50
+    el = time.perf_counter() - t0
+    out["cpu_baseline"] = {"value": n * done / el if done else None, "unit": UNIT, "cores": cores,
+                           "kind": "port",
+                           "sample": "N=4000, %d whole steps (%.1f s) of the same workload" % (
+                               done, el)}
+    return out
+
+
 def run_gpu(args):
     import proteinsim2015_gb300 as psim
     ws, rank, local = dist_env()
@@ -509,6 +557,7 @@ def run_gpu(args):
         batched["vs_single_system"] = batched["value"] / value
     differentiable = run_differentiable(psim, dev) if args.batched_steps > 0 and ws == 1 else None
     gel = run_gel(psim, dev, args.gel_steps) if args.gel_steps > 0 and ws == 1 else None
+    c0 = run_c0(psim, dev) if args.gel_steps > 0 and ws == 1 else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps, "higher_is_better": True,
@@ -543,6 +592,7 @@ def run_gpu(args):
         "batched": batched,
         "differentiable": differentiable,
         "gel": gel,
+        "c0": c0,
         "clocks": clk.summary(),
     }
     print(json.dumps(line))
