@@ -356,7 +356,9 @@ int psim_system_sync(psim_system* sys);
 /* Current state in original order.  Any pointer may be NULL. */
 int psim_system_download(psim_system* sys, double* pos, double* pos0, double* vel,
                          double* frc, double* frc0);
-/* Current cell list in the reference layout.  Any pointer may be NULL. */
+/* Current cell list in the reference layout.  Any pointer may be NULL.  With
+ * a pair list the system re-sorts its particles only when the list is
+ * rebuilt, so the cell list of the current positions is computed here. */
 int psim_system_download_cells(psim_system* sys, int32_t* particle_hash_index,
                                uint32_t* cell_start_end, double* sorted_particles);
 
