@@ -290,6 +290,7 @@ def e2e_dropin(psim, w, state, n_steps):
     f = pinned(3 * n)
     hi, cse, srt = psim.cells_build(g, buf["pos"], rad, out=cells)
     t_cur = DT  # continue as a normal step
+    calls0, builds0 = psim.force_list_stats()
     t0 = time.perf_counter()
     for _ in range(n_steps):
         psim.force_evaluate(p, g, srt, hi, cse, precision=psim.PRECISION_MIXED, out=f)
@@ -298,6 +299,7 @@ def e2e_dropin(psim, w, state, n_steps):
         psim.cells_build(g, buf["pos"], rad, out=cells)
         t_cur += DT
     el = time.perf_counter() - t0
+    calls1, builds1 = psim.force_list_stats()
     # per step: force_evaluate (sorted, hash index, cell ranges in; force out),
     # next_system (positions, previous positions, the two forces, masses in;
     # positions, previous positions and the pushed forces out -- velocities
@@ -306,7 +308,8 @@ def e2e_dropin(psim, w, state, n_steps):
     h2d = (32 * n + 8 * n + 8 * ncell) + (4 * 24 * n + 8 * n) + (24 * n + 8 * n)
     d2h = 24 * n + 4 * 24 * n + (8 * n + 8 * ncell + 32 * n)
     it.close()
-    return n * n_steps / el, h2d, d2h
+    lists = {"calls": calls1 - calls0, "builds": builds1 - builds0}
+    return n * n_steps / el, h2d, d2h, lists
 
 
 def run_batched(psim, dev, steps=2000, n_reps=512, tune=True, skin=0.3):
@@ -540,8 +543,8 @@ def run_gpu(args):
     fmax = float(np.max(np.abs(f32 - f64).reshape(-1, 3).max(1)) / rms)
     s64.close()
     # ---- end to end through the reference-layout drop-ins on pinned host buffers
-    e2e_steps = max(3, min(args.steps // 50, 10))
-    e2e_v, h2d, d2h = e2e_dropin(psim, w, state, e2e_steps)
+    e2e_steps = max(3, min(args.steps // 50, 30))
+    e2e_v, h2d, d2h, e2e_lists = e2e_dropin(psim, w, state, e2e_steps)
     # ---- roofline of the dominant kernel (the force pass)
     fp32_peak = psim.measure_fp32_peak(dev)
     f_ms = prof["force_ms"]
@@ -577,7 +580,7 @@ def run_gpu(args):
         "pair_list": {"skin": args.skin, "rebuilds": builds, "steps": steps_run,
                       "rebuild_every": (steps_run / builds) if builds else None},
         "e2e": {"value": e2e_v, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "steps": e2e_steps,
+                "d2h_bytes_per_step": d2h, "steps": e2e_steps, "force_lists": e2e_lists,
                 "path": "force_evaluate -> next_system -> cells_build on pinned host arrays"},
         "gpu_launches": args.steps * s.launches_per_step() + builds_timed * s.launches_per_rebuild(),
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak,

@@ -182,6 +182,21 @@ int psim_force_evaluate(const psim_force_params* params, const psim_geometry* ge
                         const int32_t* particle_hash_index, const uint32_t* cell_start_end,
                         double* particle_force);
 
+/* The pair list of psim_force_evaluate's mixed precision.  The call walks the
+ * pairs within cutOff + skin of a list it built on an earlier call, found
+ * from that call's cell list, and keeps doing so while no particle (by its
+ * original index) has moved skin/2 since that build; it builds a new list
+ * otherwise, and whenever n, the grid or the cutoff changed.  The forces are
+ * those of this call's positions either way (every pair within cutOff is in
+ * the list); only the FP32 summation order follows the list.  skin < 0
+ * (default): the smaller of 0.4 and cellSize - cutOff, if at least 0.1, else
+ * none; skin > 0: that skin, at most cellSize - cutOff; 0: a list of each
+ * call's own pairs, built every call.  No counterpart in the reference. */
+int psim_force_set_list_skin(double skin);
+/* Mixed-precision psim_force_evaluate calls so far, and the pair lists they
+ * built. */
+int psim_force_list_stats(int64_t* calls, int64_t* builds);
+
 /* The brownianIntegrator constructor's coefficient set-up
  * (brownianIntegrator.cpp:27-99).  gamma == 0 reproduces the reference's
  * non-finite noise widths; such coefficients are refused by the steppers. */

@@ -115,6 +115,8 @@ def lib():
             "psim_cells_build": ([C.POINTER(Geometry), P, P, P, P, P], C.c_int),
             "psim_cells_build_noalloc": ([C.POINTER(Geometry), P, P, P, P, P, P], C.c_int),
             "psim_force_evaluate": ([C.POINTER(ForceParams), C.POINTER(Geometry), C.c_int32, P, P, P, P], C.c_int),
+            "psim_force_set_list_skin": ([C.c_double], C.c_int),
+            "psim_force_list_stats": ([C.POINTER(C.c_int64), C.POINTER(C.c_int64)], C.c_int),
             "psim_vgb_coefficients": ([C.c_double] * 3 + [C.POINTER(VgbCoeffs)], C.c_int),
             "psim_integrator_create": ([C.POINTER(IntegratorConfig), C.c_int32], P),
             "psim_integrator_destroy": ([P], None),
@@ -324,6 +326,21 @@ def force_evaluate(params, geom, sorted_particles, hash_index, cell_start_end,
     _check(lib().psim_force_evaluate(C.byref(params), C.byref(geom), precision, _p(srt), _p(hi),
                                      _p(cse), _p(out)))
     return out
+
+
+def set_force_list_skin(skin=-1.0):
+    """The pair-list skin of force_evaluate's mixed precision: the list is kept
+    across calls while no particle has moved skin/2 since its build.  < 0:
+    automatic (the smaller of 0.4 and cellSize - cutOff, if at least 0.1);
+    0: a list of each call's own pairs, built every call."""
+    _check(lib().psim_force_set_list_skin(float(skin)))
+
+
+def force_list_stats():
+    """(mixed-precision force_evaluate calls, pair lists they built)."""
+    calls, builds = C.c_int64(0), C.c_int64(0)
+    _check(lib().psim_force_list_stats(C.byref(calls), C.byref(builds)))
+    return calls.value, builds.value
 
 
 def vgb_coefficients(gamma, dt, kT):

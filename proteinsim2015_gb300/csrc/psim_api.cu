@@ -234,6 +234,17 @@ ListSizes list_sizes(double rc, double skin, const DevGeom& g) {
     return z;
 }
 
+// The skin of the force drop-in's pair list on grid g: `want` (clamped to
+// the room the cell size leaves over cutOff), or with want < 0 the smaller of
+// 0.4 and that room, if at least 0.1; 0: no skin.
+double dropin_skin(double want, const DevGeom& g, double rc) {
+    const double room = (g.cs - rc) * (1.0 - 1e-9);
+    if (room <= 0.0 || want == 0.0) return 0.0;
+    if (want > 0.0) return std::min(want, room);
+    const double s = std::min(0.4, room);
+    return s >= 0.1 ? s : 0.0;
+}
+
 ForceSetup make_setup(const psim_force_params* p, double L) {
     ForceSetup fs{};
     fs.kind = p->kind;
@@ -421,8 +432,22 @@ struct Workspace {
     cudaStream_t st = nullptr;
     DevBuf pos, radius, xyz, key, rank, tmp, perm, tag_in, tag_out, radius_out, cellid, count,
         start, scratch, posd, posh, posl, hash_index, cse, sorted, force, fxyz, err;
-    // the mixed form's one-call pair list (records, halo words and count, entries)
-    DevBuf lpos, lhalo, lhcount, list, lcount;
+    // the mixed form's pair list (records, halo words and count, entries),
+    // kept across calls while no particle has moved skin/2 since its build:
+    // the build's slot of each original index and original index of each
+    // slot, the build positions (high parts), the displacement flag
+    DevBuf lpos, lhalo, lhcount, list, lcount, lslot_of, ltag, lbuild, lflag;
+    struct ListKey {
+        bool valid = false;
+        int n = 0, s = 0, cap = 0, hcap = 0;
+        double L = 0.0, cs = 0.0, rc = 0.0, skin = 0.0;
+        bool operator==(const ListKey& o) const {
+            return valid && o.valid && n == o.n && s == o.s && cap == o.cap && hcap == o.hcap &&
+                   L == o.L && cs == o.cs && rc == o.rc && skin == o.skin;
+        }
+    } lkey;
+    double lskin = -1.0;        // the list's skin: < 0 automatic, 0 none
+    long long lbuilds = 0, lcalls = 0;
 };
 Workspace g_ws;
 
@@ -434,8 +459,10 @@ int ws_begin(Workspace& w) {
         DevBuf* all[] = {&w.pos, &w.radius, &w.xyz, &w.key, &w.rank, &w.tmp, &w.perm, &w.tag_in,
                          &w.tag_out, &w.radius_out, &w.cellid, &w.count, &w.start, &w.scratch,
                          &w.posd, &w.posh, &w.posl, &w.hash_index, &w.cse, &w.sorted, &w.force,
-                         &w.fxyz, &w.err, &w.lpos, &w.lhalo, &w.lhcount, &w.list, &w.lcount};
+                         &w.fxyz, &w.err, &w.lpos, &w.lhalo, &w.lhcount, &w.list, &w.lcount,
+                         &w.lslot_of, &w.ltag, &w.lbuild, &w.lflag};
         for (DevBuf* b : all) { b->p = nullptr; b->bytes = 0; }
+        w.lkey.valid = false;
         w.st = nullptr;
     }
     if (!w.st) {
@@ -650,48 +677,104 @@ int psim_force_evaluate(const psim_force_params* params, const psim_geometry* gm
     PSIM_CUDA(launch_import_cse(g.ncell, g.n, w.cse.as<uint32_t>(), w.start.as<int>(),
                                 w.count.as<int>(), w.scratch.as<int>(), w.err.as<uint32_t>(),
                                 st));
+    // The mixed form walks a pair list: the pairs within cutOff + skin of a
+    // build, kept across calls while no particle has moved skin/2 since (every
+    // pair within cutOff is then in it), or, with no skin, a list of this
+    // call's pairs only.  Building a list and walking it costs about half the
+    // 27-cell walk; walking a kept one, about a fifth.
+    const double rcm = max_cutoff(params);
+    const double skin = precision == PSIM_PRECISION_MIXED ? dropin_skin(w.lskin, g, rcm) : 0.0;
+    const ListSizes z = list_sizes(rcm, skin, g);
+    const bool one_list = precision == PSIM_PRECISION_MIXED &&
+                          (double)(z.cap + kListFold) * (double)g.n < 4294967296.0;
+    Workspace::ListKey key;
+    key.valid = skin > 0.0;
+    key.n = g.n;
+    key.s = g.s;
+    key.cap = z.cap;
+    key.hcap = z.hcap;
+    key.L = g.L;
+    key.cs = g.cs;
+    key.rc = rcm;
+    key.skin = skin;
+    const bool kept = one_list && w.lkey == key;
+    int moved = 0;
+    if (kept) {   // this call's positions into the kept records, and the displacement test
+        PSIM_CUDA(cudaMemsetAsync(w.lflag.p, 0, 4, st));
+        PSIM_CUDA(launch_list_refresh(g.n, w.posd.as<double4_32a>(), w.tag_out.as<int>(),
+                                      w.lslot_of.as<int>(), w.lbuild.as<float4>(),
+                                      w.lhalo.as<int>(), w.lpos.as<float4>(), z.disp2, g,
+                                      w.lflag.as<int>(), st));
+        PSIM_CUDA(cudaMemcpyAsync(&moved, w.lflag.p, 4, cudaMemcpyDeviceToHost, st));
+    }
+    w.lcalls += precision == PSIM_PRECISION_MIXED ? 1 : 0;
     // a position outside the grid has no home cell: stop before the force pass
     uint32_t bits = 0;
     PSIM_CUDA(cudaMemcpyAsync(&bits, w.err.p, 4, cudaMemcpyDeviceToHost, st));
     PSIM_CUDA(cudaStreamSynchronize(st));
-    if (bits) return fail(code_from_bits(bits), "%s", bits_text(bits));
+    if (bits) {
+        w.lkey.valid = false;
+        return fail(code_from_bits(bits), "%s", bits_text(bits));
+    }
     double* f = w.fxyz.as<double>();
     CellView cv{w.posd.as<double4_32a>(), w.posh.as<float4>(), w.posl.as<float4>(),
                 w.cellid.as<int>(), w.start.as<int>(), w.count.as<int>()};
     ForceOut out{f, f + n, f + 2 * n, w.err.as<uint32_t>()};
-    // the mixed form through a pair list of this call's pairs (radius rc, no
-    // skin): building it and walking it costs about half the 27-cell walk
-    const ListSizes z = list_sizes(max_cutoff(params), 0.0, g);
-    const bool one_list = precision == PSIM_PRECISION_MIXED &&
-                          (double)(z.cap + kListFold) * (double)g.n < 4294967296.0;
+    // forces come out in the list's order (the sorted order of its build)
+    const int* order = w.tag_out.as<int>();
     if (precision == PSIM_PRECISION_FP64) {
         PSIM_CUDA(launch_forces_fp64(fs, g, cv, out, st));
     } else if (one_list) {
-        PSIM_CUDA(w.lpos.ensure(32 * (n + 1 + (size_t)z.hcap)));
-        PSIM_CUDA(w.lhalo.ensure(4 * n));
-        PSIM_CUDA(w.lhcount.ensure(4));
-        PSIM_CUDA(w.list.ensure(4 * n * (size_t)(z.cap + kListFold)));
-        PSIM_CUDA(w.lcount.ensure(4 * n));
-        PSIM_CUDA(cudaMemsetAsync(w.lhcount.p, 0, 4, st));
-        // the ghost record that pads the lists, far from every particle
-        static const float4 ghost[2] = {make_float4(1e18f, 1e18f, 1e18f, 0.f),
-                                        make_float4(0.f, 0.f, 0.f, 0.f)};
-        PSIM_CUDA(cudaMemcpyAsync(w.lpos.as<float4>() + 2 * n, ghost, 32, cudaMemcpyHostToDevice,
-                                  st));
-        PSIM_CUDA(launch_list_records(g.n, w.posh.as<float4>(), w.posl.as<float4>(),
-                                      w.lpos.as<float4>(), w.lhalo.as<int>(), w.lhcount.as<int>(),
-                                      z.hcap, z.hr, g, w.err.as<uint32_t>(), st));
-        ListBuild lb{w.list.as<uint32_t>(), w.lcount.as<int>(), g.n, z.cap, z.pre, nullptr,
-                     w.lhalo.as<int>(), g.n};
-        PSIM_CUDA(launch_list_build(g, cv, lb, w.err.as<uint32_t>(), st));
-        PSIM_CUDA(cudaMemcpyAsync(&bits, w.err.p, 4, cudaMemcpyDeviceToHost, st));
-        PSIM_CUDA(cudaStreamSynchronize(st));
-        if (bits == EBIT_LIST) {
-            // a denser neighbourhood than the list has room for: the cell walk
-            bits = 0;
-            PSIM_CUDA(cudaMemsetAsync(w.err.p, 0, 4, st));
-            PSIM_CUDA(launch_forces_mixed(fs, g, cv, out, st));
+        bool listed = kept && moved == 0;
+        if (!listed) {
+            w.lkey.valid = false;
+            PSIM_CUDA(w.lpos.ensure(32 * (n + 1 + (size_t)z.hcap)));
+            PSIM_CUDA(w.lhalo.ensure(4 * n));
+            PSIM_CUDA(w.lhcount.ensure(4));
+            PSIM_CUDA(w.list.ensure(4 * n * (size_t)(z.cap + kListFold)));
+            PSIM_CUDA(w.lcount.ensure(4 * n));
+            PSIM_CUDA(cudaMemsetAsync(w.lhcount.p, 0, 4, st));
+            // the ghost record that pads the lists, far from every particle
+            static const float4 ghost[2] = {make_float4(1e18f, 1e18f, 1e18f, 0.f),
+                                            make_float4(0.f, 0.f, 0.f, 0.f)};
+            PSIM_CUDA(cudaMemcpyAsync(w.lpos.as<float4>() + 2 * n, ghost, 32,
+                                      cudaMemcpyHostToDevice, st));
+            PSIM_CUDA(launch_list_records(g.n, w.posh.as<float4>(), w.posl.as<float4>(),
+                                          w.lpos.as<float4>(), w.lhalo.as<int>(),
+                                          w.lhcount.as<int>(), z.hcap, z.hr, g,
+                                          w.err.as<uint32_t>(), st));
+            ListBuild lb{w.list.as<uint32_t>(), w.lcount.as<int>(), g.n, z.cap, z.pre, nullptr,
+                         w.lhalo.as<int>(), g.n};
+            PSIM_CUDA(launch_list_build(g, cv, lb, w.err.as<uint32_t>(), st));
+            PSIM_CUDA(cudaMemcpyAsync(&bits, w.err.p, 4, cudaMemcpyDeviceToHost, st));
+            PSIM_CUDA(cudaStreamSynchronize(st));
+            w.lbuilds++;
+            if (bits == EBIT_LIST) {
+                // a denser neighbourhood than the list has room for: the cell walk
+                bits = 0;
+                PSIM_CUDA(cudaMemsetAsync(w.err.p, 0, 4, st));
+                PSIM_CUDA(launch_forces_mixed(fs, g, cv, out, st));
+            } else if (bits == 0) {
+                listed = true;
+                if (key.valid) {   // kept: the build's order and positions
+                    PSIM_CUDA(w.lslot_of.ensure(4 * n));
+                    PSIM_CUDA(w.ltag.ensure(4 * n));
+                    PSIM_CUDA(w.lbuild.ensure(16 * n));
+                    PSIM_CUDA(w.lflag.ensure(4));
+                    PSIM_CUDA(cudaMemcpyAsync(w.ltag.p, w.tag_out.p, 4 * n,
+                                              cudaMemcpyDeviceToDevice, st));
+                    PSIM_CUDA(cudaMemsetAsync(w.lslot_of.p, 0xff, 4 * n, st));
+                    PSIM_CUDA(launch_invert_tags(g.n, w.tag_out.as<int>(),
+                                                 w.lslot_of.as<int>(), st));
+                    PSIM_CUDA(cudaMemcpyAsync(w.lbuild.p, w.posh.p, 16 * n,
+                                              cudaMemcpyDeviceToDevice, st));
+                    w.lkey = key;
+                }
+            }
         } else {
+            order = w.ltag.as<int>();
+        }
+        if (listed) {
             const PairList pl{nullptr, w.lpos.as<float4>(), w.lcount.as<int>(),
                               w.list.as<uint32_t>(), g.n, 0, 0.f, 0.f};
             PSIM_CUDA(launch_forces_list(fs, g, pl, out, st));
@@ -699,12 +782,31 @@ int psim_force_evaluate(const psim_force_params* params, const psim_geometry* gm
     } else {
         PSIM_CUDA(launch_forces_mixed(fs, g, cv, out, st));
     }
-    PSIM_CUDA(launch_unsort_force(g.n, w.tag_out.as<int>(), f, f + n, f + 2 * n,
-                                  w.force.as<double>(), st));
+    PSIM_CUDA(launch_unsort_force(g.n, order, f, f + n, f + 2 * n, w.force.as<double>(), st));
     PSIM_CUDA(cudaMemcpyAsync(&bits, w.err.p, 4, cudaMemcpyDeviceToHost, st));
     PSIM_CUDA(cudaMemcpyAsync(force, w.force.p, 24 * n, cudaMemcpyDeviceToHost, st));
     PSIM_CUDA(cudaStreamSynchronize(st));
-    if (bits) return fail(code_from_bits(bits), "%s", bits_text(bits));
+    if (bits) {
+        w.lkey.valid = false;
+        return fail(code_from_bits(bits), "%s", bits_text(bits));
+    }
+    return PSIM_OK;
+}
+
+int psim_force_set_list_skin(double skin) {
+    if (!(skin == skin)) return fail(PSIM_ERR_INPUT, "skin is NaN");
+    Workspace& w = g_ws;
+    std::lock_guard<std::mutex> lk(w.mu);
+    w.lskin = skin;
+    w.lkey.valid = false;
+    return PSIM_OK;
+}
+
+int psim_force_list_stats(int64_t* calls, int64_t* builds) {
+    Workspace& w = g_ws;
+    std::lock_guard<std::mutex> lk(w.mu);
+    if (calls) *calls = w.lcalls;
+    if (builds) *builds = w.lbuilds;
     return PSIM_OK;
 }
 

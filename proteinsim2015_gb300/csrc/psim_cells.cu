@@ -525,6 +525,72 @@ cudaError_t launch_list_records(int n, const float4* posh, const float4* posl, f
     return cudaGetLastError();
 }
 
+// The drop-in force pass's kept pair list on a later call.  Each particle
+// (sorted slot k of this call, original index tag[k]) has its record at its
+// slot of the build rewritten from this call's position: the image nearest
+// its position at the build, as an exact float pair, with its halo images --
+// as the integrator of a system with a pair list writes them.  *flag is set
+// when a particle has moved more than sqrt(disp2) since the build, or when
+// its original index has no slot of the build.
+__global__ void __launch_bounds__(256)
+list_refresh_kernel(int n, const double4_32a* posd, const int* tag, const int* slot_of,
+                    const float4* lbuild, const int* lhalo, float4* lpos, float disp2, float Lhi,
+                    float Llo, double L, int* flag) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int s = slot_of[tag[k]];
+    if (s < 0 || s >= n) {
+        *flag = 1;
+        return;
+    }
+    const double4_32a p = posd[k];
+    const float4 b = lbuild[s];
+    const double x[3] = {p.x, p.y, p.z};
+    const float bb[3] = {b.x, b.y, b.z};
+    const float halff = 0.5f * Lhi;
+    float h[3], l[3], d2 = 0.f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        split_f64(x[a], h[a], l[a]);
+        const float da = h[a] - bb[a];
+        if (da > halff || da < -halff)  // wrapped since the build: the other image
+            split_f64(da > 0.f ? x[a] - L : x[a] + L, h[a], l[a]);
+        const float e = h[a] - bb[a];
+        d2 += e * e;
+    }
+    const float4 hv = make_float4(h[0], h[1], h[2], (float)p.w);
+    const float4 lv = make_float4(l[0], l[1], l[2], 0.f);
+    store_record(lpos, 0.f, (size_t)s, hv, lv);
+    const int hal = lhalo[s];
+    if (hal & 63)
+        halo_write(lpos + 2 * ((size_t)n + 1), 0.f, hal >> 6, (uint32_t)(hal & 63), hv, lv, Lhi,
+                   Llo);
+    if (d2 > disp2) *flag = 1;
+}
+
+cudaError_t launch_list_refresh(int n, const double4_32a* posd, const int* tag,
+                                const int* slot_of, const float4* lbuild, const int* lhalo,
+                                float4* lpos, float disp2, const DevGeom& g, int* flag,
+                                cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    list_refresh_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, posd, tag, slot_of, lbuild, lhalo,
+                                                         lpos, disp2, g.Lhi, g.Llo, g.L, flag);
+    return cudaGetLastError();
+}
+
+// slot_of[tag[k]] = k: the slot of each original index in a sorted order
+__global__ void __launch_bounds__(256)
+invert_tags_kernel(int n, const int* tag, int* slot_of) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) slot_of[tag[k]] = k;
+}
+
+cudaError_t launch_invert_tags(int n, const int* tag, int* slot_of, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    invert_tags_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, tag, slot_of);
+    return cudaGetLastError();
+}
+
 __global__ void step_end_kernel(StepState* state, const int* lflag, const uint32_t* err,
                                 int vel_freq, cudaGraphConditionalHandle handle, int use_handle) {
     const int rebuild = (*err == 0 && *lflag != 0) ? 1 : 0;

@@ -279,6 +279,18 @@ cudaError_t launch_list_records(int n, const float4* posh, const float4* posl, f
                                 int* lhalo, int* lhcount, int hcap, float hr, const DevGeom& g,
                                 uint32_t* err, cudaStream_t st);
 
+// The force drop-in's kept pair list on a later call: the records at the
+// build's slots (slot_of: original index -> slot) rewritten from this call's
+// sorted positions (tag: slot -> original index), each as the image nearest
+// its build position (lbuild), with its halo images (lhalo); *flag = 1 when
+// a particle has moved more than sqrt(disp2) since the build.
+cudaError_t launch_list_refresh(int n, const double4_32a* posd, const int* tag,
+                                const int* slot_of, const float4* lbuild, const int* lhalo,
+                                float4* lpos, float disp2, const DevGeom& g, int* flag,
+                                cudaStream_t st);
+// slot_of[tag[k]] = k (tag: every value in [0, n)).
+cudaError_t launch_invert_tags(int n, const int* tag, int* slot_of, cudaStream_t st);
+
 // End of a step whose cell list is rebuilt only with its pair list: advances
 // the step state (canonicalize_kernel's bookkeeping) and decides the rebuild
 // -- the flag the integrator raised, unless an error is latched.  In a graph
