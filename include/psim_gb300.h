@@ -215,7 +215,11 @@ void psim_integrator_destroy(psim_integrator* integ);
  * firstStep as the reference does.  noise: n*6 Gaussians in the reference
  * draw order (firstStep uses the first 3 per particle) for
  * PSIM_NOISE_INJECTED, ignored for PSIM_NOISE_PHILOX.  pos/pos0/vel/frc/frc0
- * are updated in place.  box_size: the box edge L. */
+ * are updated in place.  box_size: the box edge L.  On a device that can
+ * access pageable host memory (a Grace host's coherent link) the GPU reads
+ * and writes these arrays in place, so they must stay valid and untouched by
+ * other threads for the call; elsewhere (or with PSIM_DROPIN_COPIES=1 in the
+ * environment when the integrator is created) they are copied in and out. */
 int psim_integrator_next_system(psim_integrator* integ, double current_time, double box_size,
                                 int32_t noise_mode, const double* noise,
                                 const double* particle_force, double* pos, double* pos0,

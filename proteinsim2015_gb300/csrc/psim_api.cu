@@ -824,6 +824,10 @@ struct psim_integrator {
     // they overlap each other and the update of the chunks before
     cudaStream_t st_in = nullptr, st_out = nullptr;
     cudaEvent_t ev_in[kAosChunks] = {}, ev_run[kAosChunks] = {};
+    // the GPU reads and writes the caller's arrays in place (a device with
+    // access to pageable host memory: Grace's coherent link) instead of
+    // copying them; PSIM_DROPIN_COPIES=1 keeps the copies
+    bool direct = false;
     VgbParams vp{};
     int vel_counter = 0;
     long long steps = 0;
@@ -841,6 +845,12 @@ psim_integrator* psim_integrator_create(const psim_integrator_config* cfg, int32
     it->n = n;
     it->vp = vp;
     cudaGetDevice(&it->device);
+    int pageable = 0;
+    if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, it->device) !=
+        cudaSuccess)
+        pageable = 0;
+    const char* copies = std::getenv("PSIM_DROPIN_COPIES");
+    it->direct = pageable == 1 && !(copies && copies[0] == '1');
     const size_t b = 24 * (size_t)n;
     bool ev_ok = cudaStreamCreateWithFlags(&it->st_in, cudaStreamNonBlocking) == cudaSuccess &&
                  cudaStreamCreateWithFlags(&it->st_out, cudaStreamNonBlocking) == cudaSuccess;
@@ -899,6 +909,38 @@ int psim_integrator_next_system(psim_integrator* it, double current_time, double
     // frc0 <- frc, frc <- particleForce)
     const double* F0 = particle_force ? frc : frc0;
     const double* F = particle_force ? particle_force : frc;
+    if (it->direct) {
+        // one pass over the caller's arrays in place
+        PSIM_CUDA(cudaMemsetAsync(it->err.p, 0, 4, st));
+        VgbHostArgs a{};
+        a.n = (int)n;
+        a.first = first ? 1 : 0;
+        a.vel_step = vel_step ? 1 : 0;
+        a.pos = pos;
+        a.pos0 = pos0;
+        a.vel = vel;
+        a.F = F;
+        a.F0 = F0;
+        a.frc_out = particle_force ? frc : nullptr;
+        a.frc0_out = particle_force ? frc0 : nullptr;
+        a.mass = mass;
+        a.mem = it->mem.as<double>();
+        a.mem_corr = it->mem_corr.as<double>();
+        a.noise = noise_mode == PSIM_NOISE_INJECTED ? noise : nullptr;
+        a.seed = it->vp.seed;
+        a.philox_step = it->steps;
+        a.err = it->err.as<uint32_t>();
+        PSIM_CUDA(launch_vgb_host(a, it->vp, box, st));
+        uint32_t bits = 0;
+        PSIM_CUDA(cudaMemcpyAsync(&bits, it->err.p, 4, cudaMemcpyDeviceToHost, st));
+        PSIM_CUDA(cudaStreamSynchronize(st));
+        if (!first)  // brownianIntegrator.cpp:291-292
+            it->vel_counter = (it->vel_counter == it->vp.vel_freq) ? 0 : it->vel_counter + 1;
+        it->steps++;
+        cudaSetDevice(prev);
+        if (bits) return fail(code_from_bits(bits), "%s", bits_text(bits));
+        return PSIM_OK;
+    }
     if (noise_mode == PSIM_NOISE_INJECTED) PSIM_CUDA(it->noise.ensure(48 * n));
     PSIM_CUDA(cudaMemsetAsync(it->err.p, 0, 4, st));
     cudaEvent_t ev0 = it->ev_run[0];

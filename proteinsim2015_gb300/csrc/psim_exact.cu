@@ -190,6 +190,12 @@ cudaError_t launch_vgb_aos(const VgbAosArgs& a, const VgbParams& p, double L, cu
     return cudaGetLastError();
 }
 
+cudaError_t launch_vgb_host(const VgbHostArgs& a, const VgbParams& p, double L, cudaStream_t st) {
+    if (a.n == 0) return cudaSuccess;
+    vgb_host_kernel<VgbExact><<<(a.n + kHostBlock - 1) / kHostBlock, kHostBlock, 0, st>>>(a, p, L);
+    return cudaGetLastError();
+}
+
 // ------------------------------------------------------------------ hashing
 
 __global__ void __launch_bounds__(256)

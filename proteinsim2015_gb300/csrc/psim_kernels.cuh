@@ -207,6 +207,26 @@ struct VgbAosArgs {
 };
 cudaError_t launch_vgb_aos(const VgbAosArgs& a, const VgbParams& p, double L, cudaStream_t st);
 
+// nextSystem straight on the caller's host arrays (original order), which
+// the GPU reads and writes in place over the coherent host link -- no copies.
+// F/F0: this step's force and the previous one (host); with frc_out set the
+// pushed forces are written back (frc0_out <- F0, frc_out <- F).
+struct VgbHostArgs {
+    int n;
+    int first;
+    int vel_step;
+    double* pos; double* pos0; double* vel;   // host, read and written
+    const double* F; const double* F0;        // host
+    double* frc_out; double* frc0_out;        // host, or null: no push
+    const double* mass;                       // host
+    double* mem; double* mem_corr;            // device
+    const double* noise;                      // host n*6 (injected) or null
+    uint32_t seed;
+    long long philox_step;
+    uint32_t* err;
+};
+cudaError_t launch_vgb_host(const VgbHostArgs& a, const VgbParams& p, double L, cudaStream_t st);
+
 // Cell hash + atomic count of positions given as three coordinate arrays.
 // rep/geoms (may be null): a batch's replica of each particle and their grids.
 cudaError_t launch_hash_count(int n, const double* x, const double* y, const double* z,

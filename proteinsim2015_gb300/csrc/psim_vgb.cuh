@@ -423,4 +423,76 @@ __global__ void __launch_bounds__(256) vgb_aos_kernel(VgbAosArgs a, VgbParams p,
     if (err) atomicOr(a.err, err);
 }
 
+// nextSystem on the caller's host arrays in place.  A block of kHostBlock
+// particles stages the AoS spans it reads (positions, previous positions, the
+// two forces, velocities when the step reads them, injected noise) through
+// shared memory, so that every host access is one coalesced run of doubles,
+// updates its particles, and writes its spans back the same way.  The state
+// of a particle is read before anything of it is written, so the in/out
+// arrays may be the same (pos, pos0, vel) or overlap the push (F0 = frc).
+constexpr int kHostBlock = 128;
+template <class Tag>
+__global__ void __launch_bounds__(kHostBlock) vgb_host_kernel(VgbHostArgs a, VgbParams p,
+                                                               double L) {
+    __shared__ double sx[3 * kHostBlock], sx0[3 * kHostBlock], sf[3 * kHostBlock],
+        sf0[3 * kHostBlock], sv[3 * kHostBlock], sxi[6 * kHostBlock];
+    const int b0 = blockIdx.x * kHostBlock;
+    const int m = min(kHostBlock, a.n - b0);
+    const int t = threadIdx.x;
+    const size_t o3 = 3 * (size_t)b0;
+    const bool read_vel = a.first || a.vel_step;
+    for (int k = t; k < 3 * m; k += kHostBlock) {
+        sx[k] = a.pos[o3 + k];
+        sx0[k] = a.pos0[o3 + k];
+        sf[k] = a.F[o3 + k];
+        sf0[k] = a.F0[o3 + k];
+        sv[k] = read_vel ? a.vel[o3 + k] : 0.0;
+    }
+    if (a.noise)
+        for (int k = t; k < 6 * m; k += kHostBlock) sxi[k] = a.noise[6 * (size_t)b0 + k];
+    __syncthreads();
+    if (t < m) {
+        const int i = b0 + t;
+        uint32_t err = 0;
+        double x[3], x0[3], mx[3], F[3], F0[3], v[3], xi[6], mc[3], xn[3], x0n[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            x[k] = sx[3 * t + k];
+            x0[k] = sx0[3 * t + k];
+            F[k] = sf[3 * t + k];
+            F0[k] = sf0[3 * t + k];
+            v[k] = sv[3 * t + k];
+            mx[k] = a.mem[3 * (size_t)i + k];
+        }
+        if (a.noise) {
+#pragma unroll
+            for (int k = 0; k < 6; ++k) xi[k] = sxi[6 * t + k];
+        } else {
+            philox_gaussians6(a.seed, (uint32_t)i, (uint32_t)a.philox_step, xi);
+        }
+        const double minv = 1.0 / a.mass[i];
+        vgb_particle(p, L, L / 2, a.first != 0, a.vel_step != 0, x, x0, mx, mc, F, F0, v, xi,
+                     minv, xn, x0n, err);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            sx[3 * t + k] = xn[k];
+            sx0[3 * t + k] = x0n[k];
+            sv[3 * t + k] = v[k];
+            a.mem[3 * (size_t)i + k] = mx[k];
+            a.mem_corr[3 * (size_t)i + k] = mc[k];
+        }
+        if (err) atomicOr(a.err, err);
+    }
+    __syncthreads();
+    for (int k = t; k < 3 * m; k += kHostBlock) {
+        a.pos[o3 + k] = sx[k];
+        a.pos0[o3 + k] = sx0[k];
+        if (a.vel_step) a.vel[o3 + k] = sv[k];
+        if (a.frc_out) {
+            a.frc0_out[o3 + k] = sf0[k];
+            a.frc_out[o3 + k] = sf[k];
+        }
+    }
+}
+
 }  // namespace psim

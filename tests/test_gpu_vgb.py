@@ -9,6 +9,14 @@ from oracle import port
 pytestmark = pytest.mark.gpu
 
 
+@pytest.fixture(params=["direct", "copies"])
+def host_access(request, monkeypatch):
+    """Both drop-in paths: the GPU on the caller's arrays in place (a device
+    with pageable host memory access), or copies in and out in chunks."""
+    monkeypatch.setenv("PSIM_DROPIN_COPIES", "1" if request.param == "copies" else "0")
+    return request.param
+
+
 def _setup(n=2000, box=20.0, seed=3):
     pos, rad = rsa_state(n, box, seed)
     rng = np.random.default_rng(seed)
@@ -18,7 +26,7 @@ def _setup(n=2000, box=20.0, seed=3):
 
 
 @pytest.mark.parametrize("gamma,dt", [(1.0, 0.001), (0.01, 0.001), (5.0, 0.002)])
-def test_next_system_matches_oracle(psim, gamma, dt):
+def test_next_system_matches_oracle(psim, gamma, dt, host_access):
     s = _setup()
     n, box = s["n"], s["box"]
     vel_freq = 1
@@ -50,7 +58,7 @@ def test_next_system_matches_oracle(psim, gamma, dt):
             assert np.max(np.abs(gp[k] - op[k])) <= 1e-15 * max(1.0, np.max(np.abs(op[k]))), (k, step)
 
 
-def test_out_of_bounds_is_reported_as_7703(psim):
+def test_out_of_bounds_is_reported_as_7703(psim, host_access):
     n, box = 4, 12.0
     it = psim.Integrator(n, gamma=1.0, dt=0.001, kT=1.0)
     pos = np.array([1.0, 1.0, 1.0, 5.0, 5.0, 5.0, 9.0, 9.0, 9.0, 2.0, 8.0, 3.0])
@@ -71,7 +79,7 @@ def test_gamma_zero_is_refused(psim):
     assert e.value.code == psim.ERR_INPUT
 
 
-def test_philox_noise_is_keyed_by_particle(psim):
+def test_philox_noise_is_keyed_by_particle(psim, host_access):
     # the copies and the update run in chunks: every particle keeps its own
     # Philox stream (no two particles move alike without forces)
     n, box = 4096, 40.0
@@ -86,3 +94,25 @@ def test_philox_noise_is_keyed_by_particle(psim):
     assert np.all(np.isfinite(d)) and np.unique(d, axis=0).shape[0] == n
     assert 0.5 < np.var(d) / np.var(d[: n // 8]) < 2.0   # the same spread in every chunk
     it.close()
+
+
+def test_direct_and_copied_paths_agree(psim, monkeypatch):
+    # the same Philox keys and the same FP64 operations: identical arrays,
+    # through a first step, normal steps and a velocity step, without and
+    # with the force push
+    s = _setup(n=3001, seed=8)
+    n, box = s["n"], s["box"]
+    out = {}
+    for mode in ("0", "1"):
+        monkeypatch.setenv("PSIM_DROPIN_COPIES", mode)
+        it = psim.Integrator(n, gamma=1.0, dt=0.002, kT=1.0, vel_freq=2, seed=11)
+        a = {k: s[k].copy() for k in ("pos", "pos0", "vel", "frc", "frc0")}
+        rng = np.random.default_rng(9)
+        for step in range(5):
+            pf = rng.standard_normal(3 * n) * 20 if step != 2 else None
+            it.next_system(step * 0.002, box, a["pos"], a["pos0"], a["vel"], a["frc"], a["frc0"],
+                           s["mass"], particle_force=pf)
+        it.close()
+        out[mode] = a
+    for k in out["0"]:
+        assert np.array_equal(out["0"][k], out["1"][k]), k
