@@ -436,7 +436,15 @@ struct Workspace {
     // kept across calls while no particle has moved skin/2 since its build:
     // the build's slot of each original index and original index of each
     // slot, the build positions (high parts), the displacement flag
-    DevBuf lpos, lhalo, lhcount, list, lcount, lslot_of, ltag, lbuild, lflag;
+    DevBuf lpos, lhalo, lhcount, list, lcount, lslot_of, lbuild, lflag, inv;
+    // the kept list's records: compact (one radius lradius, low-part unit
+    // lunit) or full
+    bool lcompact = false;
+    float lradius = 0.f, lunit = 0.f;
+    // the device reads and writes the callers' host arrays in place (a device
+    // with access to pageable host memory); PSIM_DROPIN_COPIES=1 copies them
+    bool direct = false;
+    int pageable = 0;
     struct ListKey {
         bool valid = false;
         int n = 0, s = 0, cap = 0, hcap = 0;
@@ -460,7 +468,7 @@ int ws_begin(Workspace& w) {
                          &w.tag_out, &w.radius_out, &w.cellid, &w.count, &w.start, &w.scratch,
                          &w.posd, &w.posh, &w.posl, &w.hash_index, &w.cse, &w.sorted, &w.force,
                          &w.fxyz, &w.err, &w.lpos, &w.lhalo, &w.lhcount, &w.list, &w.lcount,
-                         &w.lslot_of, &w.ltag, &w.lbuild, &w.lflag};
+                         &w.lslot_of, &w.lbuild, &w.lflag, &w.inv};
         for (DevBuf* b : all) { b->p = nullptr; b->bytes = 0; }
         w.lkey.valid = false;
         w.st = nullptr;
@@ -468,7 +476,12 @@ int ws_begin(Workspace& w) {
     if (!w.st) {
         PSIM_CUDA(cudaStreamCreateWithFlags(&w.st, cudaStreamNonBlocking));
         w.device = dev;
+        if (cudaDeviceGetAttribute(&w.pageable, cudaDevAttrPageableMemoryAccess, dev) !=
+            cudaSuccess)
+            w.pageable = 0;
     }
+    const char* copies = std::getenv("PSIM_DROPIN_COPIES");
+    w.direct = w.pageable == 1 && !(copies && copies[0] == '1');
     return PSIM_OK;
 }
 
@@ -651,9 +664,6 @@ int psim_force_evaluate(const psim_force_params* params, const psim_geometry* gm
     std::lock_guard<std::mutex> lk(w.mu);
     if ((rc = ws_begin(w))) return rc;
     const size_t n = (size_t)g.n, nc = (size_t)g.ncell;
-    PSIM_CUDA(w.sorted.ensure(32 * n));
-    PSIM_CUDA(w.hash_index.ensure(8 * n));
-    PSIM_CUDA(w.cse.ensure(8 * nc));
     PSIM_CUDA(w.posd.ensure(32 * n));
     PSIM_CUDA(w.posh.ensure(16 * n));
     PSIM_CUDA(w.posl.ensure(16 * n));
@@ -663,29 +673,45 @@ int psim_force_evaluate(const psim_force_params* params, const psim_geometry* gm
     PSIM_CUDA(w.count.ensure(4 * nc));
     PSIM_CUDA(w.scratch.ensure(4 * scan_scratch_ints(g.ncell)));
     PSIM_CUDA(w.fxyz.ensure(24 * n));
-    PSIM_CUDA(w.force.ensure(24 * n));
+    PSIM_CUDA(w.inv.ensure(4 * n));
     PSIM_CUDA(w.err.ensure(4));
+    PSIM_CUDA(w.lflag.ensure(8));
     cudaStream_t st = w.st;
-    PSIM_CUDA(cudaMemcpyAsync(w.sorted.p, sorted, 32 * n, cudaMemcpyHostToDevice, st));
-    PSIM_CUDA(cudaMemcpyAsync(w.hash_index.p, hash_index, 8 * n, cudaMemcpyHostToDevice, st));
-    PSIM_CUDA(cudaMemcpyAsync(w.cse.p, cse, 8 * nc, cudaMemcpyHostToDevice, st));
+    // the caller's arrays: read in place by the device, or copied in
+    const double* d_sorted = sorted;
+    const int32_t* d_hi = hash_index;
+    const uint32_t* d_cse = cse;
+    if (!w.direct) {
+        PSIM_CUDA(w.sorted.ensure(32 * n));
+        PSIM_CUDA(w.hash_index.ensure(8 * n));
+        PSIM_CUDA(w.cse.ensure(8 * nc));
+        PSIM_CUDA(w.force.ensure(24 * n));
+        PSIM_CUDA(cudaMemcpyAsync(w.sorted.p, sorted, 32 * n, cudaMemcpyHostToDevice, st));
+        PSIM_CUDA(cudaMemcpyAsync(w.hash_index.p, hash_index, 8 * n, cudaMemcpyHostToDevice, st));
+        PSIM_CUDA(cudaMemcpyAsync(w.cse.p, cse, 8 * nc, cudaMemcpyHostToDevice, st));
+        d_sorted = w.sorted.as<double>();
+        d_hi = w.hash_index.as<int32_t>();
+        d_cse = w.cse.as<uint32_t>();
+    }
     PSIM_CUDA(cudaMemsetAsync(w.err.p, 0, 4, st));
-    PSIM_CUDA(launch_import_sorted(g.n, w.sorted.as<double>(), w.hash_index.as<int32_t>(), g,
-                                   w.posd.as<double4_32a>(), w.posh.as<float4>(),
-                                   w.posl.as<float4>(), w.cellid.as<int>(), w.tag_out.as<int>(),
-                                   w.err.as<uint32_t>(), st));
-    PSIM_CUDA(launch_import_cse(g.ncell, g.n, w.cse.as<uint32_t>(), w.start.as<int>(),
-                                w.count.as<int>(), w.scratch.as<int>(), w.err.as<uint32_t>(),
-                                st));
+    // flags: [0] a particle moved too far for the kept list, [1] mixed radii
+    int* flags = w.lflag.as<int>();
+    PSIM_CUDA(cudaMemsetAsync(flags, 0, 8, st));
+    PSIM_CUDA(launch_import_sorted(g.n, d_sorted, d_hi, g, w.posd.as<double4_32a>(),
+                                   w.posh.as<float4>(), w.posl.as<float4>(), w.cellid.as<int>(),
+                                   w.tag_out.as<int>(), w.err.as<uint32_t>(), st, flags + 1));
+    PSIM_CUDA(launch_import_cse(g.ncell, g.n, d_cse, w.start.as<int>(), w.count.as<int>(),
+                                w.scratch.as<int>(), w.err.as<uint32_t>(), st));
     // The mixed form walks a pair list: the pairs within cutOff + skin of a
     // build, kept across calls while no particle has moved skin/2 since (every
     // pair within cutOff is then in it), or, with no skin, a list of this
     // call's pairs only.  Building a list and walking it costs about half the
-    // 27-cell walk; walking a kept one, about a fifth.
+    // 27-cell walk; walking a kept one, about a fifth.  Records are compact
+    // (16 bytes) when every particle has the same radius.
     const double rcm = max_cutoff(params);
     const double skin = precision == PSIM_PRECISION_MIXED ? dropin_skin(w.lskin, g, rcm) : 0.0;
     const ListSizes z = list_sizes(rcm, skin, g);
-    const bool one_list = precision == PSIM_PRECISION_MIXED &&
+    const bool one_list = precision == PSIM_PRECISION_MIXED && g.n > 0 &&
                           (double)(z.cap + kListFold) * (double)g.n < 4294967296.0;
     Workspace::ListKey key;
     key.valid = skin > 0.0;
@@ -698,19 +724,17 @@ int psim_force_evaluate(const psim_force_params* params, const psim_geometry* gm
     key.rc = rcm;
     key.skin = skin;
     const bool kept = one_list && w.lkey == key;
-    int moved = 0;
-    if (kept) {   // this call's positions into the kept records, and the displacement test
-        PSIM_CUDA(cudaMemsetAsync(w.lflag.p, 0, 4, st));
+    if (kept)   // this call's positions into the kept records, and the displacement test
         PSIM_CUDA(launch_list_refresh(g.n, w.posd.as<double4_32a>(), w.tag_out.as<int>(),
                                       w.lslot_of.as<int>(), w.lbuild.as<float4>(),
                                       w.lhalo.as<int>(), w.lpos.as<float4>(), z.disp2, g,
-                                      w.lflag.as<int>(), st));
-        PSIM_CUDA(cudaMemcpyAsync(&moved, w.lflag.p, 4, cudaMemcpyDeviceToHost, st));
-    }
+                                      w.lcompact ? 1.0f / w.lunit : 0.f, w.lradius, flags, st));
     w.lcalls += precision == PSIM_PRECISION_MIXED ? 1 : 0;
     // a position outside the grid has no home cell: stop before the force pass
     uint32_t bits = 0;
+    int hflags[2] = {0, 0};
     PSIM_CUDA(cudaMemcpyAsync(&bits, w.err.p, 4, cudaMemcpyDeviceToHost, st));
+    PSIM_CUDA(cudaMemcpyAsync(hflags, flags, 8, cudaMemcpyDeviceToHost, st));
     PSIM_CUDA(cudaStreamSynchronize(st));
     if (bits) {
         w.lkey.valid = false;
@@ -720,29 +744,34 @@ int psim_force_evaluate(const psim_force_params* params, const psim_geometry* gm
     CellView cv{w.posd.as<double4_32a>(), w.posh.as<float4>(), w.posl.as<float4>(),
                 w.cellid.as<int>(), w.start.as<int>(), w.count.as<int>()};
     ForceOut out{f, f + n, f + 2 * n, w.err.as<uint32_t>()};
-    // forces come out in the list's order (the sorted order of its build)
-    const int* order = w.tag_out.as<int>();
-    if (precision == PSIM_PRECISION_FP64) {
-        PSIM_CUDA(launch_forces_fp64(fs, g, cv, out, st));
-    } else if (one_list) {
-        bool listed = kept && moved == 0;
+    // the forces come out in the list's order (the sorted order of its
+    // build) or this call's sorted order; inv maps original index -> slot
+    const int* inv = nullptr;
+    if (precision == PSIM_PRECISION_MIXED && one_list) {
+        bool listed = kept && hflags[0] == 0;
         if (!listed) {
             w.lkey.valid = false;
-            PSIM_CUDA(w.lpos.ensure(32 * (n + 1 + (size_t)z.hcap)));
+            const bool compact = hflags[1] == 0;
+            const float R = compact ? (float)sorted[3] : 0.f;
+            const double M = g.L + 2.0 * (rcm + skin) + 1.0;   // bounds every record coordinate
+            const float unit = (float)std::ldexp(1.0, std::ilogb(M) - 31);
+            const size_t rec = compact ? 16 : 32;
+            PSIM_CUDA(w.lpos.ensure(rec * (n + 1 + (size_t)z.hcap)));
             PSIM_CUDA(w.lhalo.ensure(4 * n));
             PSIM_CUDA(w.lhcount.ensure(4));
             PSIM_CUDA(w.list.ensure(4 * n * (size_t)(z.cap + kListFold)));
             PSIM_CUDA(w.lcount.ensure(4 * n));
+            PSIM_CUDA(w.lslot_of.ensure(4 * n));
             PSIM_CUDA(cudaMemsetAsync(w.lhcount.p, 0, 4, st));
             // the ghost record that pads the lists, far from every particle
             static const float4 ghost[2] = {make_float4(1e18f, 1e18f, 1e18f, 0.f),
                                             make_float4(0.f, 0.f, 0.f, 0.f)};
-            PSIM_CUDA(cudaMemcpyAsync(w.lpos.as<float4>() + 2 * n, ghost, 32,
+            PSIM_CUDA(cudaMemcpyAsync(w.lpos.as<char>() + rec * n, ghost, rec,
                                       cudaMemcpyHostToDevice, st));
             PSIM_CUDA(launch_list_records(g.n, w.posh.as<float4>(), w.posl.as<float4>(),
                                           w.lpos.as<float4>(), w.lhalo.as<int>(),
                                           w.lhcount.as<int>(), z.hcap, z.hr, g,
-                                          w.err.as<uint32_t>(), st));
+                                          w.err.as<uint32_t>(), st, compact ? 1.0f / unit : 0.f));
             ListBuild lb{w.list.as<uint32_t>(), w.lcount.as<int>(), g.n, z.cap, z.pre, nullptr,
                          w.lhalo.as<int>(), g.n};
             PSIM_CUDA(launch_list_build(g, cv, lb, w.err.as<uint32_t>(), st));
@@ -756,35 +785,39 @@ int psim_force_evaluate(const psim_force_params* params, const psim_geometry* gm
                 PSIM_CUDA(launch_forces_mixed(fs, g, cv, out, st));
             } else if (bits == 0) {
                 listed = true;
-                if (key.valid) {   // kept: the build's order and positions
-                    PSIM_CUDA(w.lslot_of.ensure(4 * n));
-                    PSIM_CUDA(w.ltag.ensure(4 * n));
+                w.lcompact = compact;
+                w.lradius = R;
+                w.lunit = unit;
+                PSIM_CUDA(cudaMemsetAsync(w.lslot_of.p, 0xff, 4 * n, st));
+                PSIM_CUDA(launch_invert_tags(g.n, w.tag_out.as<int>(), w.lslot_of.as<int>(), st));
+                if (key.valid) {   // kept: the build positions
                     PSIM_CUDA(w.lbuild.ensure(16 * n));
-                    PSIM_CUDA(w.lflag.ensure(4));
-                    PSIM_CUDA(cudaMemcpyAsync(w.ltag.p, w.tag_out.p, 4 * n,
-                                              cudaMemcpyDeviceToDevice, st));
-                    PSIM_CUDA(cudaMemsetAsync(w.lslot_of.p, 0xff, 4 * n, st));
-                    PSIM_CUDA(launch_invert_tags(g.n, w.tag_out.as<int>(),
-                                                 w.lslot_of.as<int>(), st));
                     PSIM_CUDA(cudaMemcpyAsync(w.lbuild.p, w.posh.p, 16 * n,
                                               cudaMemcpyDeviceToDevice, st));
                     w.lkey = key;
                 }
             }
-        } else {
-            order = w.ltag.as<int>();
         }
         if (listed) {
             const PairList pl{nullptr, w.lpos.as<float4>(), w.lcount.as<int>(),
-                              w.list.as<uint32_t>(), g.n, 0, 0.f, 0.f};
+                              w.list.as<uint32_t>(), g.n, w.lcompact, w.lradius, w.lunit};
             PSIM_CUDA(launch_forces_list(fs, g, pl, out, st));
+            inv = w.lslot_of.as<int>();
         }
+    } else if (precision == PSIM_PRECISION_FP64) {
+        PSIM_CUDA(launch_forces_fp64(fs, g, cv, out, st));
     } else {
         PSIM_CUDA(launch_forces_mixed(fs, g, cv, out, st));
     }
-    PSIM_CUDA(launch_unsort_force(g.n, order, f, f + n, f + 2 * n, w.force.as<double>(), st));
+    if (!inv) {   // this call's sorted order
+        PSIM_CUDA(launch_invert_tags(g.n, w.tag_out.as<int>(), w.inv.as<int>(), st));
+        inv = w.inv.as<int>();
+    }
+    PSIM_CUDA(launch_export_force(g.n, inv, f, f + n, f + 2 * n,
+                                  w.direct ? force : w.force.as<double>(), st));
     PSIM_CUDA(cudaMemcpyAsync(&bits, w.err.p, 4, cudaMemcpyDeviceToHost, st));
-    PSIM_CUDA(cudaMemcpyAsync(force, w.force.p, 24 * n, cudaMemcpyDeviceToHost, st));
+    if (!w.direct)
+        PSIM_CUDA(cudaMemcpyAsync(force, w.force.p, 24 * n, cudaMemcpyDeviceToHost, st));
     PSIM_CUDA(cudaStreamSynchronize(st));
     if (bits) {
         w.lkey.valid = false;

@@ -264,13 +264,28 @@ cudaError_t launch_unsort_force(int n, const int* tag, const double* fx, const d
     return cudaGetLastError();
 }
 
+// The caller's sorted particles and hash index, which may be host memory
+// read in place: a block stages its spans through shared memory so that each
+// access is a coalesced run.  *mixed_radii (if not null) is set when a radius
+// differs from the first particle's.
 __global__ void __launch_bounds__(256)
 import_sorted_kernel(int n, const double* sorted, const int32_t* hi, DevGeom g, double4_32a* posd,
-                     float4* posh, float4* posl, int* cellid, int* tag, uint32_t* err) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+                     float4* posh, float4* posl, int* cellid, int* tag, uint32_t* err,
+                     int* mixed_radii) {
+    __shared__ double ss[4 * 256];
+    __shared__ int32_t sh[2 * 256];
+    __shared__ double r0;
+    const int b0 = blockIdx.x * blockDim.x;
+    const int m = min((int)blockDim.x, n - b0);
+    if (threadIdx.x == 0 && mixed_radii) r0 = sorted[3];
+    for (int k = threadIdx.x; k < 4 * m; k += blockDim.x) ss[k] = sorted[4 * (size_t)b0 + k];
+    for (int k = threadIdx.x; k < 2 * m; k += blockDim.x) sh[k] = hi[2 * (size_t)b0 + k];
+    __syncthreads();
+    const int i = b0 + threadIdx.x;
     if (i >= n) return;
-    const double x = sorted[4 * (size_t)i], y = sorted[4 * (size_t)i + 1];
-    const double z = sorted[4 * (size_t)i + 2], R = sorted[4 * (size_t)i + 3];
+    const int u = threadIdx.x;
+    const double x = ss[4 * u], y = ss[4 * u + 1], z = ss[4 * u + 2], R = ss[4 * u + 3];
+    if (mixed_radii && R != r0) *mixed_radii = 1;
     posd[i] = make_double4_32a(x, y, z, R);
     float4 h, l;
     split_f64(x, h.x, l.x);
@@ -280,7 +295,7 @@ import_sorted_kernel(int n, const double* sorted, const int32_t* hi, DevGeom g, 
     l.w = __int_as_float(i);
     posh[i] = h;
     if (posl) posl[i] = l;
-    int t = hi[2 * (size_t)i + 1];
+    int t = sh[2 * u + 1];
     if (t < 0 || t >= n) {  // an original index outside [0, n): refuse, stay in bounds
         atomicOr(err, (uint32_t)EBIT_INDEX);
         t = 0;
@@ -303,10 +318,38 @@ import_sorted_kernel(int n, const double* sorted, const int32_t* hi, DevGeom g, 
 
 cudaError_t launch_import_sorted(int n, const double* sorted, const int32_t* hash_index,
                                  const DevGeom& g, double4_32a* posd, float4* posh, float4* posl,
-                                 int* cellid, int* tag, uint32_t* err, cudaStream_t st) {
+                                 int* cellid, int* tag, uint32_t* err, cudaStream_t st,
+                                 int* mixed_radii) {
     if (n == 0) return cudaSuccess;
     import_sorted_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, sorted, hash_index, g, posd, posh,
-                                                          posl, cellid, tag, err);
+                                                          posl, cellid, tag, err, mixed_radii);
+    return cudaGetLastError();
+}
+
+// The force of each original index i, read at its slot inv[i] of the force
+// pass's order, written to `out` (3n, original order; may be host memory
+// written in place) through shared memory in coalesced runs.
+__global__ void __launch_bounds__(256)
+export_force_kernel(int n, const int* inv, const double* fx, const double* fy, const double* fz,
+                    double* out) {
+    __shared__ double so[3 * 256];
+    const int b0 = blockIdx.x * blockDim.x;
+    const int m = min((int)blockDim.x, n - b0);
+    const int i = b0 + threadIdx.x;
+    if (i < n) {
+        const int s = inv[i];
+        so[3 * threadIdx.x] = fx[s];
+        so[3 * threadIdx.x + 1] = fy[s];
+        so[3 * threadIdx.x + 2] = fz[s];
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < 3 * m; k += blockDim.x) out[3 * (size_t)b0 + k] = so[k];
+}
+
+cudaError_t launch_export_force(int n, const int* inv, const double* fx, const double* fy,
+                                const double* fz, double* out, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    export_force_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, inv, fx, fy, fz, out);
     return cudaGetLastError();
 }
 
@@ -493,13 +536,13 @@ cudaError_t launch_pair_count(const DevGeom& g, const CellView& cv, float rc2,
 __global__ void __launch_bounds__(256)
 list_records_kernel(int n, const float4* posh, const float4* posl, float4* lpos, int* lhalo,
                     int* lhcount, int hcap, float hr, float Lf, float Lhi, float Llo,
-                    uint32_t* err) {
+                    float inv_unit, uint32_t* err) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n || *err) return;
     const float4 h = posh[g];
     float4 l = posl[g];
     l.w = 0.f;
-    store_record(lpos, 0.f, (size_t)g, h, l);
+    store_record(lpos, inv_unit, (size_t)g, h, l);
     uint32_t fl = halo_flags(h, hr, Lf);
     const int m = halo_copies(fl);
     int base = 0;
@@ -510,7 +553,8 @@ list_records_kernel(int n, const float4* posh, const float4* posl, float4* lpos,
             fl = 0;
             base = 0;
         } else {
-            halo_write(lpos + 2 * ((size_t)n + 1), 0.f, base, fl, h, l, Lhi, Llo);
+            halo_write(lpos + (inv_unit != 0.f ? 1 : 2) * ((size_t)n + 1), inv_unit, base, fl,
+                       h, l, Lhi, Llo);
         }
     }
     lhalo[g] = (base << 6) | (int)fl;
@@ -518,10 +562,11 @@ list_records_kernel(int n, const float4* posh, const float4* posl, float4* lpos,
 
 cudaError_t launch_list_records(int n, const float4* posh, const float4* posl, float4* lpos,
                                 int* lhalo, int* lhcount, int hcap, float hr, const DevGeom& g,
-                                uint32_t* err, cudaStream_t st) {
+                                uint32_t* err, cudaStream_t st, float inv_unit) {
     if (n == 0) return cudaSuccess;
     list_records_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, posh, posl, lpos, lhalo, lhcount, hcap,
-                                                         hr, (float)g.L, g.Lhi, g.Llo, err);
+                                                         hr, (float)g.L, g.Lhi, g.Llo, inv_unit,
+                                                         err);
     return cudaGetLastError();
 }
 
@@ -535,7 +580,7 @@ cudaError_t launch_list_records(int n, const float4* posh, const float4* posl, f
 __global__ void __launch_bounds__(256)
 list_refresh_kernel(int n, const double4_32a* posd, const int* tag, const int* slot_of,
                     const float4* lbuild, const int* lhalo, float4* lpos, float disp2, float Lhi,
-                    float Llo, double L, int* flag) {
+                    float Llo, double L, float inv_unit, float radius, int* flag) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const int s = slot_of[tag[k]];
@@ -560,21 +605,23 @@ list_refresh_kernel(int n, const double4_32a* posd, const int* tag, const int* s
     }
     const float4 hv = make_float4(h[0], h[1], h[2], (float)p.w);
     const float4 lv = make_float4(l[0], l[1], l[2], 0.f);
-    store_record(lpos, 0.f, (size_t)s, hv, lv);
+    store_record(lpos, inv_unit, (size_t)s, hv, lv);
     const int hal = lhalo[s];
     if (hal & 63)
-        halo_write(lpos + 2 * ((size_t)n + 1), 0.f, hal >> 6, (uint32_t)(hal & 63), hv, lv, Lhi,
-                   Llo);
-    if (d2 > disp2) *flag = 1;
+        halo_write(lpos + (inv_unit != 0.f ? 1 : 2) * ((size_t)n + 1), inv_unit, hal >> 6,
+                   (uint32_t)(hal & 63), hv, lv, Lhi, Llo);
+    // compact records hold no radius: every particle must keep the build's
+    if (d2 > disp2 || (inv_unit != 0.f && (float)p.w != radius)) *flag = 1;
 }
 
 cudaError_t launch_list_refresh(int n, const double4_32a* posd, const int* tag,
                                 const int* slot_of, const float4* lbuild, const int* lhalo,
-                                float4* lpos, float disp2, const DevGeom& g, int* flag,
-                                cudaStream_t st) {
+                                float4* lpos, float disp2, const DevGeom& g, float inv_unit,
+                                float radius, int* flag, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
     list_refresh_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, posd, tag, slot_of, lbuild, lhalo,
-                                                         lpos, disp2, g.Lhi, g.Llo, g.L, flag);
+                                                         lpos, disp2, g.Lhi, g.Llo, g.L, inv_unit,
+                                                         radius, flag);
     return cudaGetLastError();
 }
 

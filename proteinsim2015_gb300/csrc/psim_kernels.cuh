@@ -295,19 +295,22 @@ cudaError_t launch_canonicalize(const CanonArgs& a, cudaStream_t st);
 // Full 32-byte pair-list records of the sorted positions (posh, posl) and
 // the halo images of the particles within hr of a face (lhalo per slot,
 // records n + 1 + [0, hcap) handed out by *lhcount, zeroed by the caller).
+// inv_unit != 0: compact 16-byte records of that low-part unit (every
+// particle has one radius), else full records.
 cudaError_t launch_list_records(int n, const float4* posh, const float4* posl, float4* lpos,
                                 int* lhalo, int* lhcount, int hcap, float hr, const DevGeom& g,
-                                uint32_t* err, cudaStream_t st);
+                                uint32_t* err, cudaStream_t st, float inv_unit = 0.f);
 
 // The force drop-in's kept pair list on a later call: the records at the
 // build's slots (slot_of: original index -> slot) rewritten from this call's
 // sorted positions (tag: slot -> original index), each as the image nearest
 // its build position (lbuild), with its halo images (lhalo); *flag = 1 when
-// a particle has moved more than sqrt(disp2) since the build.
+// a particle has moved more than sqrt(disp2) since the build, or (compact
+// records, inv_unit != 0) when its radius is not the build's `radius`.
 cudaError_t launch_list_refresh(int n, const double4_32a* posd, const int* tag,
                                 const int* slot_of, const float4* lbuild, const int* lhalo,
-                                float4* lpos, float disp2, const DevGeom& g, int* flag,
-                                cudaStream_t st);
+                                float4* lpos, float disp2, const DevGeom& g, float inv_unit,
+                                float radius, int* flag, cudaStream_t st);
 // slot_of[tag[k]] = k (tag: every value in [0, n)).
 cudaError_t launch_invert_tags(int n, const int* tag, int* slot_of, cudaStream_t st);
 
@@ -340,9 +343,16 @@ cudaError_t launch_unsort_force(int n, const int* tag, const double* fx, const d
                                 const double* fz, double* out, cudaStream_t st);
 // Reference layout imports for psim_force_evaluate.
 // Also hashes each position into cellid (EBIT_CELL when outside the grid).
+// sorted/hash_index may be host memory the device can read in place.
+// *mixed_radii (if not null) = 1 when the radii are not all equal.
 cudaError_t launch_import_sorted(int n, const double* sorted, const int32_t* hash_index,
                                  const DevGeom& g, double4_32a* posd, float4* posh, float4* posl,
-                                 int* cellid, int* tag, uint32_t* err, cudaStream_t st);
+                                 int* cellid, int* tag, uint32_t* err, cudaStream_t st,
+                                 int* mixed_radii = nullptr);
+// out[3 i + k] = f_k[inv[i]]: forces from the force pass's order to the
+// original order (out may be host memory written in place).
+cudaError_t launch_export_force(int n, const int* inv, const double* fx, const double* fy,
+                                const double* fz, double* out, cudaStream_t st);
 // Counts from (start, end) pairs, starts re-derived by a scan (so empty
 // cells keep the back-to-back layout the row walk of the force pass needs);
 // a range beyond n, or a start that disagrees with that layout, sets

@@ -103,10 +103,36 @@ def test_radius_change_is_seen(psim, skin_reset):
     g, p, pos, rad, box = liquid(psim, seed=67)
     both(psim, g, p, pos, rad)
     b0 = builds(psim)
-    rad2 = rad * 0.9
-    mixed, fp64 = both(psim, g, p, pos, rad2)
-    assert builds(psim) == b0   # same positions: the list is kept
+    # one radius for all: compact records, which hold no radius -- a new
+    # radius is a new list
+    mixed, fp64 = both(psim, g, p, pos, rad * 0.9)
+    assert builds(psim) == b0 + 1
     assert rel_norm(mixed, fp64) <= FORCE_TOL_MIXED
+    # unequal radii: full records, rebuilt once, then kept as the radii change
+    rad3 = np.random.default_rng(71).uniform(0.42, 0.5, len(rad))
+    mixed, fp64 = both(psim, g, p, pos, rad3)
+    assert builds(psim) == b0 + 2
+    assert rel_norm(mixed, fp64) <= FORCE_TOL_MIXED
+    mixed, fp64 = both(psim, g, p, pos, rad3 * 0.98)
+    assert builds(psim) == b0 + 2
+    assert rel_norm(mixed, fp64) <= FORCE_TOL_MIXED
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("radii", ["one", "unequal"])
+def test_in_place_and_copied_arrays_agree(psim, skin_reset, monkeypatch, precision, radii):
+    # the device reading the caller's arrays in place, or copies of them:
+    # the same forces, bit for bit
+    g, p, pos, rad, box = liquid(psim, seed=72)
+    if radii == "unequal":
+        rad = np.random.default_rng(73).uniform(0.42, 0.5, len(rad))
+    hi, cse, srt = psim.cells_build(g, pos, rad)
+    out = []
+    for mode in ("0", "1"):
+        monkeypatch.setenv("PSIM_DROPIN_COPIES", mode)
+        psim.set_force_list_skin(0.0)   # a fresh list each call: the same summation order
+        out.append(psim.force_evaluate(p, g, srt, hi, cse, precision=precision))
+    assert np.array_equal(out[0], out[1])
 
 
 def test_no_skin_builds_every_call(psim, skin_reset):
