@@ -430,8 +430,8 @@ struct Workspace {
     std::mutex mu;
     int device = -1;
     cudaStream_t st = nullptr;
-    DevBuf pos, radius, xyz, key, rank, tmp, perm, tag_in, tag_out, radius_out, cellid, count,
-        start, scratch, posd, posh, posl, hash_index, cse, sorted, force, fxyz, err;
+    DevBuf pos, radius, radius_in, xyz, key, rank, tmp, perm, tag_in, tag_out, radius_out,
+        cellid, count, start, scratch, posd, posh, posl, hash_index, cse, sorted, force, fxyz, err;
     // the mixed form's pair list (records, halo words and count, entries),
     // kept across calls while no particle has moved skin/2 since its build:
     // the build's slot of each original index and original index of each
@@ -464,7 +464,7 @@ int ws_begin(Workspace& w) {
     PSIM_CUDA(cudaGetDevice(&dev));
     if (w.st && w.device != dev) {
         // the caller switched devices: drop the old device's buffers
-        DevBuf* all[] = {&w.pos, &w.radius, &w.xyz, &w.key, &w.rank, &w.tmp, &w.perm, &w.tag_in,
+        DevBuf* all[] = {&w.pos, &w.radius, &w.radius_in, &w.xyz, &w.key, &w.rank, &w.tmp, &w.perm, &w.tag_in,
                          &w.tag_out, &w.radius_out, &w.cellid, &w.count, &w.start, &w.scratch,
                          &w.posd, &w.posh, &w.posl, &w.hash_index, &w.cse, &w.sorted, &w.force,
                          &w.fxyz, &w.err, &w.lpos, &w.lhalo, &w.lhcount, &w.list, &w.lcount,
@@ -578,7 +578,6 @@ int psim_cells_build(const psim_geometry* gm, const double* pos, const double* r
     std::lock_guard<std::mutex> lk(w.mu);
     if ((rc = ws_begin(w))) return rc;
     const size_t n = (size_t)g.n, nc = (size_t)g.ncell;
-    PSIM_CUDA(w.pos.ensure(24 * n));
     PSIM_CUDA(w.radius.ensure(8 * n));
     PSIM_CUDA(w.xyz.ensure(24 * n));
     PSIM_CUDA(w.key.ensure(4 * n));
@@ -594,17 +593,27 @@ int psim_cells_build(const psim_geometry* gm, const double* pos, const double* r
     PSIM_CUDA(w.scratch.ensure(4 * scan_scratch_ints(g.ncell)));
     PSIM_CUDA(w.posd.ensure(32 * n));
     PSIM_CUDA(w.posh.ensure(16 * n));
-    PSIM_CUDA(w.hash_index.ensure(8 * n));
-    PSIM_CUDA(w.cse.ensure(8 * nc));
-    PSIM_CUDA(w.sorted.ensure(32 * n));
     PSIM_CUDA(w.err.ensure(4));
     cudaStream_t st = w.st;
     double* x = w.xyz.as<double>();
-    PSIM_CUDA(cudaMemcpyAsync(w.pos.p, pos, 24 * n, cudaMemcpyHostToDevice, st));
-    PSIM_CUDA(cudaMemcpyAsync(w.radius.p, radius, 8 * n, cudaMemcpyHostToDevice, st));
+    // the caller's arrays: read and written in place by the device, or copied
+    const double* d_pos = pos;
+    const double* d_radius = radius;
+    if (!w.direct) {
+        PSIM_CUDA(w.pos.ensure(24 * n));
+        PSIM_CUDA(w.radius_in.ensure(8 * n));
+        PSIM_CUDA(w.hash_index.ensure(8 * n));
+        PSIM_CUDA(w.cse.ensure(8 * nc));
+        PSIM_CUDA(w.sorted.ensure(32 * n));
+        PSIM_CUDA(cudaMemcpyAsync(w.pos.p, pos, 24 * n, cudaMemcpyHostToDevice, st));
+        PSIM_CUDA(cudaMemcpyAsync(w.radius_in.p, radius, 8 * n, cudaMemcpyHostToDevice, st));
+        d_pos = w.pos.as<double>();
+        d_radius = w.radius_in.as<double>();
+    }
     PSIM_CUDA(cudaMemsetAsync(w.count.p, 0, 4 * nc, st));
     PSIM_CUDA(cudaMemsetAsync(w.err.p, 0, 4, st));
-    PSIM_CUDA(launch_split_xyz(g.n, w.pos.as<double>(), nullptr, 0, x, x + n, x + 2 * n, st));
+    PSIM_CUDA(launch_import_positions(g.n, d_pos, d_radius, x, x + n, x + 2 * n,
+                                      w.radius.as<double>(), st));
     PSIM_CUDA(launch_hash_count(g.n, x, x + n, x + 2 * n, g, w.key.as<int>(), w.rank.as<int>(),
                                 w.count.as<int>(), w.err.as<uint32_t>(), st));
     PSIM_CUDA(launch_scan(w.count.as<int>(), w.start.as<int>(), g.ncell, w.scratch.as<int>(), st));
@@ -629,16 +638,24 @@ int psim_cells_build(const psim_geometry* gm, const double* pos, const double* r
     ca.posd = w.posd.as<double4_32a>();
     ca.posh = w.posh.as<float4>();
     PSIM_CUDA(launch_canonicalize(ca, st));
-    PSIM_CUDA(launch_export_cells(g.n, g.ncell, w.cellid.as<int>(), w.tag_out.as<int>(),
-                                  w.posd.as<double4_32a>(), w.start.as<int>(), w.count.as<int>(),
-                                  w.hash_index.as<int32_t>(), w.cse.as<uint32_t>(),
-                                  w.sorted.as<double>(), st));
+    if (w.direct) {
+        PSIM_CUDA(launch_export_cells(g.n, g.ncell, w.cellid.as<int>(), w.tag_out.as<int>(),
+                                      w.posd.as<double4_32a>(), w.start.as<int>(),
+                                      w.count.as<int>(), hash_index, cse, sorted, st));
+    } else {
+        PSIM_CUDA(launch_export_cells(g.n, g.ncell, w.cellid.as<int>(), w.tag_out.as<int>(),
+                                      w.posd.as<double4_32a>(), w.start.as<int>(),
+                                      w.count.as<int>(), w.hash_index.as<int32_t>(),
+                                      w.cse.as<uint32_t>(), w.sorted.as<double>(), st));
+        if (hash_index)
+            PSIM_CUDA(cudaMemcpyAsync(hash_index, w.hash_index.p, 8 * n, cudaMemcpyDeviceToHost,
+                                      st));
+        if (cse) PSIM_CUDA(cudaMemcpyAsync(cse, w.cse.p, 8 * nc, cudaMemcpyDeviceToHost, st));
+        if (sorted)
+            PSIM_CUDA(cudaMemcpyAsync(sorted, w.sorted.p, 32 * n, cudaMemcpyDeviceToHost, st));
+    }
     uint32_t bits = 0;
     PSIM_CUDA(cudaMemcpyAsync(&bits, w.err.p, 4, cudaMemcpyDeviceToHost, st));
-    if (hash_index)
-        PSIM_CUDA(cudaMemcpyAsync(hash_index, w.hash_index.p, 8 * n, cudaMemcpyDeviceToHost, st));
-    if (cse) PSIM_CUDA(cudaMemcpyAsync(cse, w.cse.p, 8 * nc, cudaMemcpyDeviceToHost, st));
-    if (sorted) PSIM_CUDA(cudaMemcpyAsync(sorted, w.sorted.p, 32 * n, cudaMemcpyDeviceToHost, st));
     PSIM_CUDA(cudaStreamSynchronize(st));
     if (bits) return fail(code_from_bits(bits), "%s", bits_text(bits));
     return PSIM_OK;

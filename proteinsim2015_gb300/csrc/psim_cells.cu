@@ -206,32 +206,51 @@ cudaError_t launch_canonicalize(const CanonArgs& a, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+// The reference-layout outputs, which may be host memory written in place:
+// each block stages its spans through shared memory and writes them as
+// coalesced runs.
 __global__ void __launch_bounds__(256)
 export_particles_kernel(int n, const int* cellid, const int* tag, const double4_32a* posd,
                         int32_t* hash_index, double* sorted) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    if (hash_index) {
-        hash_index[2 * (size_t)i] = cellid[i];
-        hash_index[2 * (size_t)i + 1] = tag[i];
+    __shared__ double ss[4 * 256];
+    __shared__ int32_t sh[2 * 256];
+    const int b0 = blockIdx.x * blockDim.x;
+    const int m = min((int)blockDim.x, n - b0);
+    const int i = b0 + threadIdx.x, u = threadIdx.x;
+    if (i < n) {
+        if (hash_index) {
+            sh[2 * u] = cellid[i];
+            sh[2 * u + 1] = tag[i];
+        }
+        if (sorted) {
+            const double4_32a p = posd[i];
+            ss[4 * u] = p.x;
+            ss[4 * u + 1] = p.y;
+            ss[4 * u + 2] = p.z;
+            ss[4 * u + 3] = p.w;
+        }
     }
-    if (sorted) {
-        const double4_32a p = posd[i];
-        sorted[4 * (size_t)i] = p.x;
-        sorted[4 * (size_t)i + 1] = p.y;
-        sorted[4 * (size_t)i + 2] = p.z;
-        sorted[4 * (size_t)i + 3] = p.w;
-    }
+    __syncthreads();
+    if (hash_index)
+        for (int k = u; k < 2 * m; k += blockDim.x) hash_index[2 * (size_t)b0 + k] = sh[k];
+    if (sorted)
+        for (int k = u; k < 4 * m; k += blockDim.x) sorted[4 * (size_t)b0 + k] = ss[k];
 }
 
 __global__ void __launch_bounds__(256)
 export_cells_kernel(int ncell, const int* start, const int* count, uint32_t* cse) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= ncell) return;
-    const int k = count[c];
-    // empty cells keep clearCells' sentinel (system.h:166)
-    cse[2 * (size_t)c] = k > 0 ? (uint32_t)start[c] : 0xffffffffu;
-    cse[2 * (size_t)c + 1] = k > 0 ? (uint32_t)(start[c] + k) : 0xffffffffu;
+    __shared__ uint32_t sc[2 * 256];
+    const int b0 = blockIdx.x * blockDim.x;
+    const int m = min((int)blockDim.x, ncell - b0);
+    const int c = b0 + threadIdx.x;
+    if (c < ncell) {
+        const int k = count[c];
+        // empty cells keep clearCells' sentinel (system.h:166)
+        sc[2 * threadIdx.x] = k > 0 ? (uint32_t)start[c] : 0xffffffffu;
+        sc[2 * threadIdx.x + 1] = k > 0 ? (uint32_t)(start[c] + k) : 0xffffffffu;
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < 2 * m; k += blockDim.x) cse[2 * (size_t)b0 + k] = sc[k];
 }
 
 cudaError_t launch_export_cells(int n, int ncell, const int* cellid, const int* tag,
@@ -397,6 +416,32 @@ split_xyz_kernel(int n, const double* aos, const int* tag, int gather, double* x
     x[i] = aos[s];
     y[i] = aos[s + 1];
     z[i] = aos[s + 2];
+}
+
+// Positions (3n AoS) and radii of the caller, which may be host memory read
+// in place, into SoA coordinates and a device copy of the radii, each block
+// reading its spans as coalesced runs through shared memory.
+__global__ void __launch_bounds__(256)
+import_positions_kernel(int n, const double* aos, const double* radius, double* x, double* y,
+                        double* z, double* radius_out) {
+    __shared__ double sp[3 * 256];
+    const int b0 = blockIdx.x * blockDim.x;
+    const int m = min((int)blockDim.x, n - b0);
+    for (int k = threadIdx.x; k < 3 * m; k += blockDim.x) sp[k] = aos[3 * (size_t)b0 + k];
+    __syncthreads();
+    const int i = b0 + threadIdx.x;
+    if (i >= n) return;
+    x[i] = sp[3 * threadIdx.x];
+    y[i] = sp[3 * threadIdx.x + 1];
+    z[i] = sp[3 * threadIdx.x + 2];
+    radius_out[i] = radius[i];
+}
+
+cudaError_t launch_import_positions(int n, const double* aos, const double* radius, double* x,
+                                    double* y, double* z, double* radius_out, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    import_positions_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, aos, radius, x, y, z, radius_out);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_split_xyz(int n, const double* aos, const int* tag, int gather, double* x,

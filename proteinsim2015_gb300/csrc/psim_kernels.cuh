@@ -333,7 +333,7 @@ struct PermuteArgs {
 };
 cudaError_t launch_permute(const PermuteArgs& a, const uint32_t* err, cudaStream_t st);
 
-// Reference layout exports.
+// Reference layout exports (outputs may be host memory written in place).
 cudaError_t launch_export_cells(int n, int ncell, const int* cellid, const int* tag,
                                 const double4_32a* posd, const int* start, const int* count,
                                 int32_t* hash_index, uint32_t* cse, double* sorted,
@@ -359,6 +359,10 @@ cudaError_t launch_export_force(int n, const int* inv, const double* fx, const d
 // EBIT_INDEX.  scratch: scan_scratch_ints(ncell) ints.
 cudaError_t launch_import_cse(int ncell, int n, const uint32_t* cse, int* start, int* count,
                               int* scratch, uint32_t* err, cudaStream_t st);
+// Positions (3n AoS) and radii, possibly host memory read in place, into
+// SoA x, y, z and a device copy of the radii.
+cudaError_t launch_import_positions(int n, const double* aos, const double* radius, double* x,
+                                    double* y, double* z, double* radius_out, cudaStream_t st);
 // AoS xyz -> three arrays, optionally scattered by tag (gather == 0) or
 // gathered (gather == 1: out[i] = in[tag[i]]).
 cudaError_t launch_split_xyz(int n, const double* aos, const int* tag, int gather, double* x,

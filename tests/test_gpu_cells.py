@@ -9,6 +9,14 @@ from oracle import port
 pytestmark = pytest.mark.gpu
 
 
+@pytest.fixture(autouse=True, params=["direct", "copies"])
+def host_access(request, monkeypatch):
+    """Both drop-in paths: the device on the caller's arrays in place (a device
+    with pageable host memory access), or copies in and out."""
+    monkeypatch.setenv("PSIM_DROPIN_COPIES", "1" if request.param == "copies" else "0")
+    return request.param
+
+
 def test_cells_match_reference_golden(psim, golden):
     n, box, cs, scale = (int(v) for v in golden["cellsA_geom"])
     hi, cse, srt = psim.cells_build(psim.geometry(n, box, cs, scale), golden["cellsA_pos"],
