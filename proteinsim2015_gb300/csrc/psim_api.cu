@@ -741,11 +741,27 @@ int psim_force_evaluate(const psim_force_params* params, const psim_geometry* gm
     key.rc = rcm;
     key.skin = skin;
     const bool kept = one_list && w.lkey == key;
-    if (kept)   // this call's positions into the kept records, and the displacement test
+    double* f = w.fxyz.as<double>();
+    CellView cv{w.posd.as<double4_32a>(), w.posh.as<float4>(), w.posl.as<float4>(),
+                w.cellid.as<int>(), w.start.as<int>(), w.count.as<int>()};
+    ForceOut out{f, f + n, f + 2 * n, w.err.as<uint32_t>()};
+    if (kept) {
+        // this call's positions into the kept records with the displacement
+        // test, and the force pass over the kept list in the same stream: the
+        // usual call ends at the one synchronisation below; a call that finds
+        // a particle moved too far discards this force and builds a new list
         PSIM_CUDA(launch_list_refresh(g.n, w.posd.as<double4_32a>(), w.tag_out.as<int>(),
                                       w.lslot_of.as<int>(), w.lbuild.as<float4>(),
                                       w.lhalo.as<int>(), w.lpos.as<float4>(), z.disp2, g,
                                       w.lcompact ? 1.0f / w.lunit : 0.f, w.lradius, flags, st));
+        const PairList pl{nullptr, w.lpos.as<float4>(), w.lcount.as<int>(),
+                          w.list.as<uint32_t>(), g.n, w.lcompact, w.lradius, w.lunit};
+        PSIM_CUDA(launch_forces_list(fs, g, pl, out, st));
+        PSIM_CUDA(launch_export_force(g.n, w.lslot_of.as<int>(), f, f + n, f + 2 * n,
+                                      w.direct ? force : w.force.as<double>(), st));
+        if (!w.direct)
+            PSIM_CUDA(cudaMemcpyAsync(force, w.force.p, 24 * n, cudaMemcpyDeviceToHost, st));
+    }
     w.lcalls += precision == PSIM_PRECISION_MIXED ? 1 : 0;
     // a position outside the grid has no home cell: stop before the force pass
     uint32_t bits = 0;
@@ -757,62 +773,57 @@ int psim_force_evaluate(const psim_force_params* params, const psim_geometry* gm
         w.lkey.valid = false;
         return fail(code_from_bits(bits), "%s", bits_text(bits));
     }
-    double* f = w.fxyz.as<double>();
-    CellView cv{w.posd.as<double4_32a>(), w.posh.as<float4>(), w.posl.as<float4>(),
-                w.cellid.as<int>(), w.start.as<int>(), w.count.as<int>()};
-    ForceOut out{f, f + n, f + 2 * n, w.err.as<uint32_t>()};
+    if (kept && hflags[0] == 0) return PSIM_OK;
     // the forces come out in the list's order (the sorted order of its
     // build) or this call's sorted order; inv maps original index -> slot
     const int* inv = nullptr;
     if (precision == PSIM_PRECISION_MIXED && one_list) {
-        bool listed = kept && hflags[0] == 0;
-        if (!listed) {
-            w.lkey.valid = false;
-            const bool compact = hflags[1] == 0;
-            const float R = compact ? (float)sorted[3] : 0.f;
-            const double M = g.L + 2.0 * (rcm + skin) + 1.0;   // bounds every record coordinate
-            const float unit = (float)std::ldexp(1.0, std::ilogb(M) - 31);
-            const size_t rec = compact ? 16 : 32;
-            PSIM_CUDA(w.lpos.ensure(rec * (n + 1 + (size_t)z.hcap)));
-            PSIM_CUDA(w.lhalo.ensure(4 * n));
-            PSIM_CUDA(w.lhcount.ensure(4));
-            PSIM_CUDA(w.list.ensure(4 * n * (size_t)(z.cap + kListFold)));
-            PSIM_CUDA(w.lcount.ensure(4 * n));
-            PSIM_CUDA(w.lslot_of.ensure(4 * n));
-            PSIM_CUDA(cudaMemsetAsync(w.lhcount.p, 0, 4, st));
-            // the ghost record that pads the lists, far from every particle
-            static const float4 ghost[2] = {make_float4(1e18f, 1e18f, 1e18f, 0.f),
-                                            make_float4(0.f, 0.f, 0.f, 0.f)};
-            PSIM_CUDA(cudaMemcpyAsync(w.lpos.as<char>() + rec * n, ghost, rec,
-                                      cudaMemcpyHostToDevice, st));
-            PSIM_CUDA(launch_list_records(g.n, w.posh.as<float4>(), w.posl.as<float4>(),
-                                          w.lpos.as<float4>(), w.lhalo.as<int>(),
-                                          w.lhcount.as<int>(), z.hcap, z.hr, g,
-                                          w.err.as<uint32_t>(), st, compact ? 1.0f / unit : 0.f));
-            ListBuild lb{w.list.as<uint32_t>(), w.lcount.as<int>(), g.n, z.cap, z.pre, nullptr,
-                         w.lhalo.as<int>(), g.n};
-            PSIM_CUDA(launch_list_build(g, cv, lb, w.err.as<uint32_t>(), st));
-            PSIM_CUDA(cudaMemcpyAsync(&bits, w.err.p, 4, cudaMemcpyDeviceToHost, st));
-            PSIM_CUDA(cudaStreamSynchronize(st));
-            w.lbuilds++;
-            if (bits == EBIT_LIST) {
-                // a denser neighbourhood than the list has room for: the cell walk
-                bits = 0;
-                PSIM_CUDA(cudaMemsetAsync(w.err.p, 0, 4, st));
-                PSIM_CUDA(launch_forces_mixed(fs, g, cv, out, st));
-            } else if (bits == 0) {
-                listed = true;
-                w.lcompact = compact;
-                w.lradius = R;
-                w.lunit = unit;
-                PSIM_CUDA(cudaMemsetAsync(w.lslot_of.p, 0xff, 4 * n, st));
-                PSIM_CUDA(launch_invert_tags(g.n, w.tag_out.as<int>(), w.lslot_of.as<int>(), st));
-                if (key.valid) {   // kept: the build positions
-                    PSIM_CUDA(w.lbuild.ensure(16 * n));
-                    PSIM_CUDA(cudaMemcpyAsync(w.lbuild.p, w.posh.p, 16 * n,
-                                              cudaMemcpyDeviceToDevice, st));
-                    w.lkey = key;
-                }
+        bool listed = false;   // a kept list that is still good has returned above
+        w.lkey.valid = false;
+        const bool compact = hflags[1] == 0;
+        const float R = compact ? (float)sorted[3] : 0.f;
+        const double M = g.L + 2.0 * (rcm + skin) + 1.0;   // bounds every record coordinate
+        const float unit = (float)std::ldexp(1.0, std::ilogb(M) - 31);
+        const size_t rec = compact ? 16 : 32;
+        PSIM_CUDA(w.lpos.ensure(rec * (n + 1 + (size_t)z.hcap)));
+        PSIM_CUDA(w.lhalo.ensure(4 * n));
+        PSIM_CUDA(w.lhcount.ensure(4));
+        PSIM_CUDA(w.list.ensure(4 * n * (size_t)(z.cap + kListFold)));
+        PSIM_CUDA(w.lcount.ensure(4 * n));
+        PSIM_CUDA(w.lslot_of.ensure(4 * n));
+        PSIM_CUDA(cudaMemsetAsync(w.lhcount.p, 0, 4, st));
+        // the ghost record that pads the lists, far from every particle
+        static const float4 ghost[2] = {make_float4(1e18f, 1e18f, 1e18f, 0.f),
+                                        make_float4(0.f, 0.f, 0.f, 0.f)};
+        PSIM_CUDA(cudaMemcpyAsync(w.lpos.as<char>() + rec * n, ghost, rec,
+                                  cudaMemcpyHostToDevice, st));
+        PSIM_CUDA(launch_list_records(g.n, w.posh.as<float4>(), w.posl.as<float4>(),
+                                      w.lpos.as<float4>(), w.lhalo.as<int>(),
+                                      w.lhcount.as<int>(), z.hcap, z.hr, g,
+                                      w.err.as<uint32_t>(), st, compact ? 1.0f / unit : 0.f));
+        ListBuild lb{w.list.as<uint32_t>(), w.lcount.as<int>(), g.n, z.cap, z.pre, nullptr,
+                     w.lhalo.as<int>(), g.n};
+        PSIM_CUDA(launch_list_build(g, cv, lb, w.err.as<uint32_t>(), st));
+        PSIM_CUDA(cudaMemcpyAsync(&bits, w.err.p, 4, cudaMemcpyDeviceToHost, st));
+        PSIM_CUDA(cudaStreamSynchronize(st));
+        w.lbuilds++;
+        if (bits == EBIT_LIST) {
+            // a denser neighbourhood than the list has room for: the cell walk
+            bits = 0;
+            PSIM_CUDA(cudaMemsetAsync(w.err.p, 0, 4, st));
+            PSIM_CUDA(launch_forces_mixed(fs, g, cv, out, st));
+        } else if (bits == 0) {
+            listed = true;
+            w.lcompact = compact;
+            w.lradius = R;
+            w.lunit = unit;
+            PSIM_CUDA(cudaMemsetAsync(w.lslot_of.p, 0xff, 4 * n, st));
+            PSIM_CUDA(launch_invert_tags(g.n, w.tag_out.as<int>(), w.lslot_of.as<int>(), st));
+            if (key.valid) {   // kept: the build positions
+                PSIM_CUDA(w.lbuild.ensure(16 * n));
+                PSIM_CUDA(cudaMemcpyAsync(w.lbuild.p, w.posh.p, 16 * n,
+                                          cudaMemcpyDeviceToDevice, st));
+                w.lkey = key;
             }
         }
         if (listed) {
