@@ -581,7 +581,7 @@ def run_gpu(args):
                       "rebuild_every": (steps_run / builds) if builds else None},
         "e2e": {"value": e2e_v, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "steps": e2e_steps, "force_lists": e2e_lists,
-                "path": "force_evaluate -> next_system -> cells_build on pinned host arrays"},
+                "path": "force_evaluate -> next_system -> cells_build on pinned host arrays, read and written in place by the GPU over NVLink-C2C (copies where the device has no pageable host access)"},
         "gpu_launches": args.steps * s.launches_per_step() + builds_timed * s.launches_per_rebuild(),
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak,
                      "unit": "TFLOP/s", "frac": achieved / fp32_peak,

@@ -144,6 +144,13 @@ int psim_ao_coefficients(double kT, double well_depth, double cutoff, double* co
 
 /* ------------------------------------ drop-ins on the reference layout */
 
+/* Host arrays of the drop-ins.  On a device that can access pageable host
+ * memory (a Grace host's coherent link, cudaDevAttrPageableMemoryAccess) the
+ * GPU reads the caller's input arrays and writes its output arrays in place,
+ * pinned or not; elsewhere, or with PSIM_DROPIN_COPIES=1 in the environment,
+ * the calls copy them in and out.  Either way the arrays must stay valid and
+ * untouched by other threads for the call, and the results are identical. */
+
 /* system::hashParticles + sortParticles + clearCells + reorderParticles
  * (ClusteredCore/src/system/systemHandling.cpp:33-85, system.h:166).
  * pos: 3n original order; radius: n.  Outputs particle_hash_index (2n),
@@ -215,11 +222,8 @@ void psim_integrator_destroy(psim_integrator* integ);
  * firstStep as the reference does.  noise: n*6 Gaussians in the reference
  * draw order (firstStep uses the first 3 per particle) for
  * PSIM_NOISE_INJECTED, ignored for PSIM_NOISE_PHILOX.  pos/pos0/vel/frc/frc0
- * are updated in place.  box_size: the box edge L.  On a device that can
- * access pageable host memory (a Grace host's coherent link) the GPU reads
- * and writes these arrays in place, so they must stay valid and untouched by
- * other threads for the call; elsewhere (or with PSIM_DROPIN_COPIES=1 in the
- * environment when the integrator is created) they are copied in and out. */
+ * are updated in place.  box_size: the box edge L.  Host arrays as for the
+ * other drop-ins (PSIM_DROPIN_COPIES is read when the integrator is created). */
 int psim_integrator_next_system(psim_integrator* integ, double current_time, double box_size,
                                 int32_t noise_mode, const double* noise,
                                 const double* particle_force, double* pos, double* pos0,
