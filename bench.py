@@ -545,6 +545,10 @@ def run_gpu(args):
     # ---- end to end through the reference-layout drop-ins on pinned host buffers
     e2e_steps = max(3, min(args.steps // 50, 30))
     e2e_v, h2d, d2h, e2e_lists = e2e_dropin(psim, w, state, e2e_steps)
+    # the host link the drop-ins' traffic crosses: its measured rates
+    link = psim.measure_host_link(dev)
+    e2e_ms = n / e2e_v * 1e3
+    link_gbs = (h2d + d2h) / (e2e_ms * 1e-3) / 1e9
     # ---- roofline of the dominant kernel (the force pass)
     fp32_peak = psim.measure_fp32_peak(dev)
     f_ms = prof["force_ms"]
@@ -581,6 +585,13 @@ def run_gpu(args):
                       "rebuild_every": (steps_run / builds) if builds else None},
         "e2e": {"value": e2e_v, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "steps": e2e_steps, "force_lists": e2e_lists,
+                "ms_per_step": e2e_ms,
+                "link_roofline": {"bound": "host link", "achieved": link_gbs,
+                                  "peak": link["both"], "unit": "GB/s",
+                                  "frac": link_gbs / link["both"],
+                                  "read_gbs": link["read"], "write_gbs": link["write"],
+                                  "peak_source": "measured: SM loads and stores on pinned "
+                                                 "host memory, both directions at once"},
                 "path": "force_evaluate -> next_system -> cells_build on pinned host arrays, read and written in place by the GPU over NVLink-C2C (copies where the device has no pageable host access)"},
         "gpu_launches": args.steps * s.launches_per_step() + builds_timed * s.launches_per_rebuild(),
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak,

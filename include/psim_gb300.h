@@ -474,6 +474,13 @@ int psim_system_pair_count(psim_system* sys, double cutoff, double* mean_pairs);
  * denominator of the force pass's FP32 roofline. */
 int psim_measure_fp32_peak(int32_t device, double* tflops);
 
+/* Host-link bandwidth of `device` in GB/s, measured with SM loads and stores
+ * on pinned host memory (128 MiB): reading host memory, writing it, and both
+ * at once (host to host through the SMs, each byte counted once per
+ * crossing); the denominators of the drop-ins' end-to-end roofline. */
+int psim_measure_host_link(int32_t device, double* read_gbs, double* write_gbs,
+                           double* both_gbs);
+
 #ifdef __cplusplus
 }
 #endif

@@ -160,6 +160,7 @@ def lib():
             "psim_system_time_steps": ([P, C.c_int32, C.POINTER(C.c_double)], C.c_int),
             "psim_system_pair_count": ([P, C.c_double, C.POINTER(C.c_double)], C.c_int),
             "psim_measure_fp32_peak": ([C.c_int32, C.POINTER(C.c_double)], C.c_int),
+            "psim_measure_host_link": ([C.c_int32] + [C.POINTER(C.c_double)] * 3, C.c_int),
         }
         for name, (args, res) in sigs.items():
             fn = getattr(L, name)
@@ -194,6 +195,14 @@ def _f64(a, n=None):
 
 def device_count():
     return lib().psim_device_count()
+
+
+def measure_host_link(device=0):
+    """Measured host-link bandwidth (GB/s) of the device with SM loads and
+    stores on pinned host memory: {"read", "write", "both"}."""
+    r, w, b = C.c_double(), C.c_double(), C.c_double()
+    _check(lib().psim_measure_host_link(device, C.byref(r), C.byref(w), C.byref(b)))
+    return {"read": r.value, "write": w.value, "both": b.value}
 
 
 def measure_fp32_peak(device=0):
@@ -289,12 +298,14 @@ def ao_coefficients(kT, well_depth, cutoff):
 # ---------------------------------------------------------------- drop-ins
 
 def _out(arr, dtype, size):
-    """A caller's output array (e.g. in pinned memory, which the copies read at
-    full speed), checked, or a new one."""
+    """A caller's output array (which the device may write in place), checked,
+    or a new one."""
     if arr is None:
         return np.empty(size, dtype)
-    if arr.dtype != dtype or not arr.flags.c_contiguous or arr.size != size:
-        raise PsimError(ERR_INPUT, "output array must be contiguous %s[%d]" % (np.dtype(dtype), size))
+    if (arr.dtype != dtype or not arr.flags.c_contiguous or not arr.flags.writeable
+            or arr.size != size):
+        raise PsimError(ERR_INPUT, "output array must be writeable contiguous %s[%d]"
+                        % (np.dtype(dtype), size))
     return arr.reshape(-1)
 
 
@@ -363,8 +374,11 @@ class Integrator:
                     particle_force=None):
         """pushParticleForce (if particle_force is given) + nextSystem; the
         float64 arrays are updated in place."""
-        for a in (pos, pos0, vel, frc, frc0):
-            assert a.dtype == np.float64 and a.flags.c_contiguous and a.size == 3 * self.n
+        for a in (pos, pos0, vel, frc, frc0):   # updated in place, possibly by the device
+            if (a.dtype != np.float64 or not a.flags.c_contiguous or not a.flags.writeable
+                    or a.size != 3 * self.n):
+                raise PsimError(ERR_INPUT, "state arrays must be writeable contiguous "
+                                "float64[%d]" % (3 * self.n))
         mode = NOISE_INJECTED if noise is not None else NOISE_PHILOX
         nz = _f64(noise, 6 * self.n) if noise is not None else None
         pf = _f64(particle_force, 3 * self.n) if particle_force is not None else None

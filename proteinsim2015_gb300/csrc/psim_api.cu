@@ -2654,4 +2654,60 @@ int psim_measure_fp32_peak(int32_t device, double* tflops) {
     return PSIM_OK;
 }
 
+int psim_measure_host_link(int32_t device, double* read_gbs, double* write_gbs,
+                           double* both_gbs) {
+    if (!read_gbs || !write_gbs || !both_gbs) return fail(PSIM_ERR_INPUT, "NULL argument");
+    int rc = ensure_device();
+    if (rc) return rc;
+    DeviceGuard dg(device);
+    int sms = 0;
+    PSIM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    const size_t bytes = 128ull << 20;
+    ScopedBuf d;
+    PSIM_CUDA(d.ensure(bytes));
+    PSIM_CUDA(cudaMemset(d.p, 0, bytes));
+    void* h[2] = {nullptr, nullptr};
+    for (void*& p : h) {
+        if (cudaHostAlloc(&p, bytes, cudaHostAllocDefault) != cudaSuccess) {
+            for (void* q : h)
+                if (q) cudaFreeHost(q);
+            return fail(PSIM_ERR_CUDA, "pinned host allocation failed");
+        }
+        std::memset(p, 1, bytes);
+    }
+    void* hd[2] = {nullptr, nullptr};   // the device's addresses of the host buffers
+    rc = PSIM_OK;
+    for (int k = 0; k < 2 && rc == PSIM_OK; ++k)
+        if (cudaHostGetDevicePointer(&hd[k], h[k], 0) != cudaSuccess)
+            rc = fail(PSIM_ERR_CUDA, "host buffer not mapped");
+    cudaEvent_t a = nullptr, b = nullptr;
+    if (rc == PSIM_OK && (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess))
+        rc = fail(PSIM_ERR_CUDA, "event creation failed");
+    // read: host -> device; write: device -> host; both: host -> host through
+    // the SMs (each byte crosses the link twice, as in the in-place drop-ins)
+    const void* src[3] = {hd[0], d.p, hd[0]};
+    void* dst[3] = {d.p, hd[1], hd[1]};
+    double* out[3] = {read_gbs, write_gbs, both_gbs};
+    for (int k = 0; k < 3 && rc == PSIM_OK; ++k) {
+        float best = 1e30f;
+        for (int r = 0; r < 4 && rc == PSIM_OK; ++r) {
+            if (cudaEventRecord(a, 0) != cudaSuccess ||
+                launch_link_copy(sms * 4, src[k], dst[k], bytes, 0) != cudaSuccess ||
+                cudaEventRecord(b, 0) != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess) {
+                rc = fail(PSIM_ERR_CUDA, "link probe failed: %s",
+                          cudaGetErrorString(cudaGetLastError()));
+                break;
+            }
+            float t = 0.f;
+            cudaEventElapsedTime(&t, a, b);
+            if (r > 0 && t < best) best = t;   // the first run warms the mappings
+        }
+        *out[k] = (k == 2 ? 2.0 : 1.0) * (double)bytes / (best * 1e-3) / 1e9;
+    }
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+    for (void* q : h) cudaFreeHost(q);
+    return rc;
+}
+
 }  // extern "C"

@@ -741,4 +741,28 @@ cudaError_t launch_fma_probe(int blocks, int threads, int iters, float* sink, cu
     return cudaGetLastError();
 }
 
+// Host-link probe: dst[i] = src[i] over n 16-byte words, four in flight per
+// thread; either side may be host memory the device reads or writes in place.
+__global__ void __launch_bounds__(256) link_copy_kernel(const uint4* __restrict__ src,
+                                                        uint4* __restrict__ dst, size_t n) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    for (; i + 3 * stride < n; i += 4 * stride) {
+        const uint4 a = src[i], b = src[i + stride], c = src[i + 2 * stride],
+                    d = src[i + 3 * stride];
+        dst[i] = a;
+        dst[i + stride] = b;
+        dst[i + 2 * stride] = c;
+        dst[i + 3 * stride] = d;
+    }
+    for (; i < n; i += stride) dst[i] = src[i];
+}
+
+cudaError_t launch_link_copy(int blocks, const void* src, void* dst, size_t bytes,
+                             cudaStream_t st) {
+    link_copy_kernel<<<blocks, 256, 0, st>>>(static_cast<const uint4*>(src),
+                                             static_cast<uint4*>(dst), bytes / 16);
+    return cudaGetLastError();
+}
+
 }  // namespace psim

@@ -386,6 +386,10 @@ cudaError_t launch_pair_count(const DevGeom& g, const CellView& cv, float rc2,
                               unsigned long long* total, cudaStream_t st);
 // FMA-chain throughput probe: `iters` rounds of 8 independent FMA chains per thread.
 cudaError_t launch_fma_probe(int blocks, int threads, int iters, float* sink, cudaStream_t st);
+// Host-link probe: copies `bytes` (a multiple of 16) from src to dst with
+// SM loads and stores; either may be host memory.
+cudaError_t launch_link_copy(int blocks, const void* src, void* dst, size_t bytes,
+                             cudaStream_t st);
 
 // Observables of the device-resident state (psim_observe.cu).
 enum ObserveWhat { OBS_MEAN_DISP = 0, OBS_TRACKED = 1, OBS_POTENTIAL = 2 };

@@ -120,3 +120,15 @@ def test_geometry_validation_needs_no_gpu(psim):
     with pytest.raises(psim.PsimError) as e:  # cellSize below the cutoff
         psim.force_evaluate(f, g, np.zeros(16), np.zeros(8, np.int32), np.zeros(128, np.uint32))
     assert e.value.code == psim.ERR_INPUT
+
+
+def test_output_arrays_must_be_writeable(psim):
+    # the device may write a caller's output array in place: a read-only one
+    # is refused on the host, before any call
+    ro = np.zeros(12)
+    ro.flags.writeable = False
+    with pytest.raises(psim.PsimError) as e:
+        psim._out(ro, np.float64, 12)
+    assert e.value.code == psim.ERR_INPUT
+    ok = np.zeros(12)
+    assert psim._out(ok, np.float64, 12) is not None

@@ -154,3 +154,11 @@ def test_skin_is_clamped_to_the_cells_room(psim, skin_reset):
         mixed, fp64 = both(psim, g, p, pos, rad)
         assert rel_norm(mixed, fp64) <= FORCE_TOL_MIXED
         pos = np.mod(pos + rng.uniform(-0.02, 0.02, pos.shape), box)
+
+
+def test_host_link_probe(psim):
+    # the denominators of the drop-ins' end-to-end roofline: finite, positive,
+    # and both directions at once no slower than either alone
+    link = psim.measure_host_link(0)
+    assert all(v > 1.0 for v in link.values())
+    assert link["both"] >= 0.9 * min(link["read"], link["write"])
