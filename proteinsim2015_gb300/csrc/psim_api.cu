@@ -1160,6 +1160,7 @@ double* d3(DevBuf& b, int n, int k) { return b.as<double>() + (size_t)k * n; }
 // The list-order records the canonicalisation writes when the list is
 // rebuilt: positions, build positions and halo images.
 void set_halo_args(psim_system* s, CanonArgs& ca) {
+    ca.xorder = 1;   // each row of cells sorted by x: the list build trims its runs
     ca.lbuild = s->lbuild.as<float4>();
     ca.lpos = s->lpos.as<float4>();
     ca.linv_unit = s->lcompact ? 1.0f / s->lunit : 0.f;
@@ -1184,6 +1185,7 @@ cudaError_t enqueue_list_build(psim_system* s, int cb, const int* gate) {
                 s->start.as<int>(), s->count[cb].as<int>()};
     ListBuild lb{s->list.as<uint32_t>(), s->lcount.as<int>(), s->n, s->lcap, s->lpre, gate,
                  s->lhalo.as<int>(), s->n};
+    lb.xsorted = 1;   // the order set_halo_args asks the canonicalisation for
     if (s->n_reps) {   // each replica's own grid and list radius
         lb.rep = s->b_rep.as<int>();
         lb.geoms = s->b_geoms.as<DevGeom>();

@@ -135,7 +135,18 @@ __global__ void __launch_bounds__(256) canonicalize_kernel(CanonArgs a, int vel_
         const int cnt = a.count[c];
         const int mine = a.tag_in[f];
         int r = 0;
-        for (int q = st; q < st + cnt; ++q) r += (a.tag_in[a.tmp[q]] < mine) ? 1 : 0;
+        if (a.xorder) {
+            // by x, then tag: the bit patterns of the (non-negative) positions
+            // order like their values, and every pattern is comparable
+            const long long mx = __double_as_longlong(a.x[f]);
+            for (int q = st; q < st + cnt; ++q) {
+                const int fq = a.tmp[q];
+                const long long xq = __double_as_longlong(a.x[fq]);
+                r += (xq < mx || (xq == mx && a.tag_in[fq] < mine)) ? 1 : 0;
+            }
+        } else {
+            for (int q = st; q < st + cnt; ++q) r += (a.tag_in[a.tmp[q]] < mine) ? 1 : 0;
+        }
         const int g = st + r;
         a.perm[g] = f;
         a.tag_out[g] = mine;

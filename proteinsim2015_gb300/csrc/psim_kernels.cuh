@@ -104,6 +104,9 @@ struct ListBuild {
     const int* rep;
     const DevGeom* geoms;
     const float* pre;
+    // 1: each cell's particles are sorted by x (CanonArgs::xorder), so a row
+    // of cells is an x-sorted run that the build trims to the home's reach
+    int xsorted;
 };
 cudaError_t launch_list_build(const DevGeom& g, const CellView& cv, const ListBuild& lb,
                               uint32_t* err, cudaStream_t st);
@@ -289,6 +292,10 @@ struct CanonArgs {
     const int* rep;
     const DevGeom* geoms;
     const float* hr_rep;
+    // order within a cell: 0 by tag (the reference layout), 1 by x then tag
+    // (a pair-list order: each row of cells is sorted by x, which the list
+    // build uses to trim its runs)
+    int xorder;
 };
 cudaError_t launch_canonicalize(const CanonArgs& a, cudaStream_t st);
 
