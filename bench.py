@@ -43,6 +43,9 @@ UNIT = "particle-steps/s"
 KT, WD, RC, LJN, DT, GAMMA = 1.5, 1.0 / 1.5, 2.5, 6, 0.002, 1.0
 FLOPS_PER_PAIR_LJ = 30   # algorithmic FLOPs per in-range ordered pair (FMA = 2)
 FLOPS_VGB = 60           # algorithmic FP64 FLOPs per particle of the vGB update
+# algorithmic HBM bytes per particle-step of the whole mixed step, each unique state
+# array read and written once: rebuild 84, force 28, vGB 180
+BYTES_PER_PARTICLE_STEP = 292
 # Verlet pair-list skin of the mixed form; the cell grid is the finest with
 # cellSize >= rc + skin, so the list can be built from the 27-cell walk
 SKIN = 0.4
@@ -602,6 +605,16 @@ def run_gpu(args):
                          FLOPS_PER_PAIR_LJ, pairs),
                      "peak_source": "measured FP32 FMA probe (MEASURED_PEAKS.json has no FP32 figure)",
                      "hbm_peak_gbs": peaks.get("hbm_gbs")},
+        "step_roofline": {
+            "flops_per_particle_step": pairs * FLOPS_PER_PAIR_LJ + FLOPS_VGB,
+            "bytes_per_particle_step": BYTES_PER_PARTICLE_STEP,
+            "achieved_tflops": value * (pairs * FLOPS_PER_PAIR_LJ + FLOPS_VGB) / 1e12,
+            "achieved_gbs": value * BYTES_PER_PARTICLE_STEP / 1e9,
+            "frac": max(value * (pairs * FLOPS_PER_PAIR_LJ + FLOPS_VGB) / 1e12 / fp32_peak,
+                        value * BYTES_PER_PARTICLE_STEP / 1e9 / peaks["hbm_gbs"])
+            if peaks.get("hbm_gbs") else None,
+            "note": "whole step: max(FLOP/s over the FP32 peak, algorithmic bytes/s over "
+                    "the measured HBM copy rate)"},
         "cpu_baseline": cpu,
         "batched": batched,
         "differentiable": differentiable,
