@@ -1100,7 +1100,10 @@ struct psim_system {
     long long total = 0;      // steps since upload, as the host has enqueued them
     bool uploaded = false;
     bool snap_pending = false;
+    // one graph per buffer phase (one step), and one of kGraphSteps steps
+    // starting at phase 0 (fewer graph launches for small systems)
     cudaGraphExec_t graph[6] = {};
+    cudaGraphExec_t graph_multi = nullptr;
     uint32_t latched = 0;
     // Verlet pair list of the mixed form (list_on): list slot of each storage
     // slot (ping-pong with the order), positions at the build, entries,
@@ -1140,6 +1143,9 @@ namespace {
 struct Phase {
     int sb, ob, cb, pb, fprev, fcur;
 };
+
+// steps in one multi-step graph: a whole number of buffer periods (6)
+constexpr int kGraphSteps = 12;
 
 // Buffer roles after `t` steps (t = 0: just uploaded).  Period 6: the
 // ping-pong pairs flip every step, the three force buffers rotate.
@@ -1462,28 +1468,40 @@ int enqueue_step(psim_system* s, long long t, cudaEvent_t* evs) {
 
 // The step graph with a pair list: the step, then a conditional node (set by
 // the step end) whose body is the rebuild.
-int graph_for_lazy(psim_system* s, int phase, cudaGraphExec_t* out) {
+// Steps phase .. phase + steps - 1 with a pair list, captured into one graph:
+// each step's kernels followed by a conditional node whose body is that
+// step's rebuild (the step end sets the node's condition).
+int graph_lazy_steps(psim_system* s, int phase, int steps, cudaGraphExec_t* out) {
     cudaGraph_t g = nullptr;
     PSIM_CUDA(cudaGraphCreate(&g, 0));
     auto done = [&](int rc) {
         if (g) cudaGraphDestroy(g);
         return rc;
     };
-    cudaError_t e = cudaGraphConditionalHandleCreate(&s->cond, g, 0, cudaGraphCondAssignDefault);
+    // a condition handle per conditional node: the step end that sets it is
+    // captured with s->cond holding that step's handle
+    std::vector<cudaGraphConditionalHandle> conds(steps);
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < steps && e == cudaSuccess; ++k)
+        e = cudaGraphConditionalHandleCreate(&conds[k], g, 0, cudaGraphCondAssignDefault);
     if (e != cudaSuccess)
         return done(fail(PSIM_ERR_CUDA, "conditional handle: %s", cudaGetErrorString(e)));
+    std::vector<cudaGraph_t> bodies;
     e = cudaStreamBeginCaptureToGraph(s->st, g, nullptr, nullptr, 0,
                                       cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return done(fail(PSIM_ERR_CUDA, "capture: %s", cudaGetErrorString(e)));
-    int rc = enqueue_step_lazy(s, phase, nullptr);
-    cudaGraphNodeParams cp{};
-    if (!rc) {
+    int rc = PSIM_OK;
+    for (int k = 0; k < steps && !rc; ++k) {
+        s->cond = conds[k];
+        rc = enqueue_step_lazy(s, phase + k, nullptr);
+        if (rc) break;
         cudaStreamCaptureStatus cs;
         const cudaGraphNode_t* deps = nullptr;
         size_t nd = 0;
         cudaGraph_t cg = nullptr;
         e = cudaStreamGetCaptureInfo(s->st, &cs, nullptr, &cg, &deps, nullptr, &nd);
         cudaGraphNode_t cn = nullptr;
+        cudaGraphNodeParams cp{};
         if (e == cudaSuccess) {
             cp.type = cudaGraphNodeTypeConditional;
             cp.conditional.handle = s->cond;
@@ -1495,41 +1513,55 @@ int graph_for_lazy(psim_system* s, int phase, cudaGraphExec_t* out) {
         if (e == cudaSuccess)
             e = cudaStreamUpdateCaptureDependencies(s->st, &cn, nullptr, 1,
                                                     cudaStreamSetCaptureDependencies);
-        if (e != cudaSuccess) rc = fail(PSIM_ERR_CUDA, "conditional node: %s", cudaGetErrorString(e));
+        if (e != cudaSuccess)
+            rc = fail(PSIM_ERR_CUDA, "conditional node: %s", cudaGetErrorString(e));
+        else
+            bodies.push_back(cp.conditional.phGraph_out[0]);
     }
     cudaGraph_t captured = g;
     e = cudaStreamEndCapture(s->st, &captured);
     if (rc) return done(rc);
     if (e != cudaSuccess) return done(fail(PSIM_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e)));
-    // the body: the rebuild, captured into the node's own graph
-    cudaGraph_t body = cp.conditional.phGraph_out[0];
-    e = cudaStreamBeginCaptureToGraph(s->st, body, nullptr, nullptr, 0,
-                                      cudaStreamCaptureModeThreadLocal);
-    if (e != cudaSuccess) return done(fail(PSIM_ERR_CUDA, "capture: %s", cudaGetErrorString(e)));
-    rc = enqueue_rebuild_lazy(s, phase);
-    cudaGraph_t bcap = body;
-    e = cudaStreamEndCapture(s->st, &bcap);
-    if (rc) return done(rc);
-    if (e != cudaSuccess) return done(fail(PSIM_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e)));
-    e = cudaGraphInstantiate(&s->graph[phase], g, 0);
+    // the bodies: each step's rebuild, captured into its node's own graph
+    for (int k = 0; k < steps; ++k) {
+        cudaGraph_t body = bodies[k];
+        e = cudaStreamBeginCaptureToGraph(s->st, body, nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return done(fail(PSIM_ERR_CUDA, "capture: %s", cudaGetErrorString(e)));
+        rc = enqueue_rebuild_lazy(s, phase + k);
+        cudaGraph_t bcap = body;
+        e = cudaStreamEndCapture(s->st, &bcap);
+        if (rc) return done(rc);
+        if (e != cudaSuccess)
+            return done(fail(PSIM_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e)));
+    }
+    e = cudaGraphInstantiate(out, g, 0);
     if (e != cudaSuccess)
         return done(fail(PSIM_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e)));
-    *out = s->graph[phase];
     return done(PSIM_OK);
 }
 
-int graph_for(psim_system* s, int phase, cudaGraphExec_t* out) {
-    if (s->graph[phase]) { *out = s->graph[phase]; return PSIM_OK; }
-    if (s->list_on) return graph_for_lazy(s, phase, out);
+// Steps phase .. phase + steps - 1, captured into one graph.
+int graph_steps(psim_system* s, int phase, int steps, cudaGraphExec_t* out) {
+    if (s->list_on) return graph_lazy_steps(s, phase, steps, out);
     cudaGraph_t g = nullptr;
     PSIM_CUDA(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal));
-    int rc = enqueue_step(s, phase, nullptr);
+    int rc = PSIM_OK;
+    for (int k = 0; k < steps && !rc; ++k) rc = enqueue_step(s, phase + k, nullptr);
     cudaError_t e = cudaStreamEndCapture(s->st, &g);
     if (rc) { if (g) cudaGraphDestroy(g); return rc; }
     if (e != cudaSuccess) return fail(PSIM_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
-    e = cudaGraphInstantiate(&s->graph[phase], g, 0);
+    e = cudaGraphInstantiate(out, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(PSIM_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+    return PSIM_OK;
+}
+
+int graph_for(psim_system* s, int phase, cudaGraphExec_t* out) {
+    if (!s->graph[phase]) {
+        int rc = graph_steps(s, phase, 1, &s->graph[phase]);
+        if (rc) return rc;
+    }
     *out = s->graph[phase];
     return PSIM_OK;
 }
@@ -1537,6 +1569,7 @@ int graph_for(psim_system* s, int phase, cudaGraphExec_t* out) {
 void drop_graphs(psim_system* s) {
     for (auto& g : s->graph)
         if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+    if (s->graph_multi) { cudaGraphExecDestroy(s->graph_multi); s->graph_multi = nullptr; }
 }
 
 struct DeviceGuard {
@@ -2110,12 +2143,25 @@ int psim_system_step_async(psim_system* s, int32_t n_steps) {
             if (rc) return rc;
         }
     }
-    for (int k = 0; k < n_steps; ++k) {
+    if (n_steps >= kGraphSteps + 5 && !s->graph_multi) {
+        PSIM_CUDA(cudaStreamSynchronize(s->st));
+        int rc = graph_steps(s, 0, kGraphSteps, &s->graph_multi);
+        if (rc) return rc;
+    }
+    // single steps up to a multiple of 6, then kGraphSteps steps per launch
+    while (n_steps > 0) {
+        if (s->graph_multi && s->total % 6 == 0 && n_steps >= kGraphSteps) {
+            PSIM_CUDA(cudaGraphLaunch(s->graph_multi, s->st));
+            s->total += kGraphSteps;
+            n_steps -= kGraphSteps;
+            continue;
+        }
         cudaGraphExec_t ge;
         int rc = graph_for(s, (int)(s->total % 6), &ge);
         if (rc) return rc;
         PSIM_CUDA(cudaGraphLaunch(ge, s->st));
         s->total++;
+        --n_steps;
     }
     return PSIM_OK;
 }
@@ -2583,6 +2629,10 @@ int psim_system_time_steps(psim_system* s, int32_t n_steps, double* ms) {
             PSIM_CUDA(cudaStreamSynchronize(s->st));
             if ((rc = graph_for(s, ph, &ge))) return rc;
         }
+    }
+    if (n_steps >= kGraphSteps + 5 && !s->graph_multi) {
+        PSIM_CUDA(cudaStreamSynchronize(s->st));
+        if ((rc = graph_steps(s, 0, kGraphSteps, &s->graph_multi))) return rc;
     }
     PSIM_CUDA(cudaStreamSynchronize(s->st));
     PSIM_CUDA(cudaEventRecord(s->ev[0], s->st));
