@@ -119,6 +119,31 @@ def test_deterministic_and_graph_phases(psim):
         assert np.array_equal(res[0][k], res[1][k])
 
 
+@pytest.mark.parametrize("skin", [0.0, 0.1])
+def test_multi_step_graphs_match_single_steps(psim, skin):
+    # a long call runs graphs of 12 steps (after single steps up to a multiple
+    # of 6): the same state as one step per call, through list rebuilds too
+    n, box, scale = 3000, 20.0, 6
+    pos, rad = rsa_state(n, box, seed=24)
+    p = psim.make_force("AO", 1.1, kT=1.0, well_depth=0.25)
+    g = psim.geometry(n, box, box / scale, scale)
+    res = []
+    for calls in ((3, 60), (1,) * 63):
+        s = psim.System(g, p, gamma=1.0, dt=0.002, kT=1.0, vel_freq=5, seed=9,
+                        precision=psim.PRECISION_MIXED, skin=skin)
+        s.upload(pos, rad)
+        for k in calls:
+            s.step(k)
+        out = s.download()
+        out["builds"] = np.array([s.list_builds()])
+        res.append(out)
+        s.close()
+    for k in res[0]:
+        assert np.array_equal(res[0][k], res[1][k]), k
+    if skin > 0:
+        assert res[0]["builds"][0] > 1
+
+
 def test_snapshot_async_equals_download(psim):
     n, box, scale = 2000, 16.0, 5
     pos, rad = rsa_state(n, box, seed=24)
