@@ -277,7 +277,7 @@ __device__ __forceinline__ ListRec<false> load_rec(const float4* pos, uint32_t j
 // for nearby values and the second comes out of the record's decode
 // (compact) or one subtraction (full), so d carries one FP32 rounding.
 template <class Body, bool kCompact, bool kReplicas>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(256)
 force_list_kernel(Body body0, DevGeom g, PairList pl, ForceOut out) {
     constexpr int kBatch = 4;
     static_assert(kListFold == 2 * kBatch, "a fold is two batches");
@@ -372,21 +372,21 @@ template <class Body>
 cudaError_t launch_force_list(const Body& body, const DevGeom& g, const PairList& pl,
                               const ForceOut& out, cudaStream_t st) {
     if (g.n == 0) return cudaSuccess;
-    const int blocks = (g.n + 127) / 128;
+    const int blocks = (g.n + 255) / 256;
     if (pl.rep) {
         if constexpr (Body::kBatchable) {
             if (pl.compact)
-                force_list_kernel<Body, true, true><<<blocks, 128, 0, st>>>(body, g, pl, out);
+                force_list_kernel<Body, true, true><<<blocks, 256, 0, st>>>(body, g, pl, out);
             else
-                force_list_kernel<Body, false, true><<<blocks, 128, 0, st>>>(body, g, pl, out);
+                force_list_kernel<Body, false, true><<<blocks, 256, 0, st>>>(body, g, pl, out);
             return cudaGetLastError();
         }
         return cudaErrorInvalidValue;
     }
     if (pl.compact)
-        force_list_kernel<Body, true, false><<<blocks, 128, 0, st>>>(body, g, pl, out);
+        force_list_kernel<Body, true, false><<<blocks, 256, 0, st>>>(body, g, pl, out);
     else
-        force_list_kernel<Body, false, false><<<blocks, 128, 0, st>>>(body, g, pl, out);
+        force_list_kernel<Body, false, false><<<blocks, 256, 0, st>>>(body, g, pl, out);
     return cudaGetLastError();
 }
 
