@@ -132,3 +132,15 @@ def test_output_arrays_must_be_writeable(psim):
     assert e.value.code == psim.ERR_INPUT
     ok = np.zeros(12)
     assert psim._out(ok, np.float64, 12) is not None
+
+
+def test_force_list_settings_need_no_gpu(psim):
+    # the drop-in pair list's skin and counters are host state: settable and
+    # readable without a device; a NaN skin is refused
+    psim.set_force_list_skin(0.25)
+    psim.set_force_list_skin(-1.0)
+    with pytest.raises(psim.PsimError) as e:
+        psim.set_force_list_skin(float("nan"))
+    assert e.value.code == psim.ERR_INPUT
+    calls, builds = psim.force_list_stats()
+    assert calls >= 0 and 0 <= builds <= max(calls, 0)
