@@ -169,12 +169,13 @@ int psim_cells_build(const psim_geometry* geom, const double* pos, const double*
  * layouts as psim_cells_build: d_pos (3n), d_radius (n) in; d_hash_index
  * (2n), d_cell_start_end (2*s^3), d_sorted (4n, 32-byte aligned) out.  Work
  * is queued on `stream` (a cudaStream_t; NULL = default stream) and the call
- * waits for it.  The scratch is one static 32 MiB device array held by every
- * GPU that loads the library until exit; the first call on a device looks it
- * up (make that call before any stream capture); calls that overlap on the
- * GPU share and race on it.  Problems needing more scratch than the array
- * (about 76 bytes per particle plus 8 per cell) return PSIM_ERR_INPUT.
- * Allocates no device memory. */
+ * blocks until it is done, so it cannot be called while a stream is being
+ * captured.  The scratch is one static 32 MiB device array held by every GPU
+ * that loads the library until exit; each call looks its address up with the
+ * caller's device current (so calls after a device reset are fine); calls
+ * that overlap on the GPU share and race on it.  Problems needing more
+ * scratch than the array (about 76 bytes per particle plus 8 per cell) return
+ * PSIM_ERR_INPUT.  Allocates no device memory. */
 int psim_cells_build_noalloc(const psim_geometry* geom, const double* d_pos,
                              const double* d_radius, int32_t* d_hash_index,
                              uint32_t* d_cell_start_end, double* d_sorted, void* stream);

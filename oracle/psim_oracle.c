@@ -8,7 +8,8 @@
  * relative to the reference project).  Floating-point expressions keep the
  * reference's operand order so that, built with -ffp-contract=off, results
  * are bit-identical to the reference's own x86-64 build (checked by
- * tests/test_oracle_ref.py against oracle/_ref).  The one deliberate change:
+ * tests/test_oracle_golden.py against the fixtures tests/golden/make_golden.py
+ * wrote from the reference rebuilt in oracle/_ref).  The one deliberate change:
  * the reference's unstable __gnu_parallel::sort is replaced by a stable
  * counting sort, i.e. the order inside a cell is by original index.  The
  * reference leaves that order unspecified; cell membership is unchanged.

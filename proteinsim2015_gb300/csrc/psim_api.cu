@@ -463,13 +463,23 @@ int ws_begin(Workspace& w) {
     int dev = 0;
     PSIM_CUDA(cudaGetDevice(&dev));
     if (w.st && w.device != dev) {
-        // the caller switched devices: drop the old device's buffers
+        // the caller switched devices: free the old device's buffers and
+        // stream on that device, then make the caller's device current again
         DevBuf* all[] = {&w.pos, &w.radius, &w.radius_in, &w.xyz, &w.key, &w.rank, &w.tmp, &w.perm, &w.tag_in,
                          &w.tag_out, &w.radius_out, &w.cellid, &w.count, &w.start, &w.scratch,
                          &w.posd, &w.posh, &w.posl, &w.hash_index, &w.cse, &w.sorted, &w.force,
                          &w.fxyz, &w.err, &w.lpos, &w.lhalo, &w.lhcount, &w.list, &w.lcount,
                          &w.lslot_of, &w.lbuild, &w.lflag, &w.inv};
-        for (DevBuf* b : all) { b->p = nullptr; b->bytes = 0; }
+        if (cudaSetDevice(w.device) == cudaSuccess) {
+            cudaStreamSynchronize(w.st);
+            for (DevBuf* b : all) b->release();
+            cudaStreamDestroy(w.st);
+        } else {
+            // the old device is gone (reset or lost): its memory went with it
+            cudaGetLastError();
+            for (DevBuf* b : all) { b->p = nullptr; b->bytes = 0; }
+        }
+        PSIM_CUDA(cudaSetDevice(dev));
         w.lkey.valid = false;
         w.st = nullptr;
     }

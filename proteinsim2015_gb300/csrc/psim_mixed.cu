@@ -229,14 +229,15 @@ cudaError_t launch_forces_list(const ForceSetup& fs, const DevGeom& g, const Pai
 cudaError_t launch_list_build(const DevGeom& g, const CellView& cv, const ListBuild& lb,
                               uint32_t* err, cudaStream_t st) {
     if (g.n == 0) return cudaSuccess;
-    static int blocks = 0;   // 32 blocks per SM of the current device
-    if (blocks == 0) {
-        int dev = 0, sms = 0;
-        if (cudaGetDevice(&dev) != cudaSuccess ||
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-            sms = 152;
-        blocks = 32 * sms;
+    // 32 blocks per SM of the current device (looked up per call: the
+    // attribute query is a cached read in the runtime)
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+        cudaGetLastError();
+        sms = 152;
     }
+    const int blocks = 32 * sms;
     list_build_kernel<<<std::min(blocks, (g.n + 127) / 128), 128, 0, st>>>(g, cv, lb, err);
     return cudaGetLastError();
 }

@@ -14,9 +14,13 @@
 // Costs and rules, stated for the caller:
 //   * every GPU that loads this library holds the 32 MiB array until the
 //     process exits;
-//   * the first call on a device looks the array up (cudaGetSymbolAddress)
-//     with that device current; make that first call before any stream
-//     capture;
+//   * every call looks the array's device address up (cudaGetSymbolAddress)
+//     with the caller's device current, so a device reset, after which the
+//     library's module is loaded again and the array may sit elsewhere, needs
+//     nothing from the caller;
+//   * the call waits for its own work (it reads the error word back), so it
+//     blocks until the build is done and cannot be called while a stream is
+//     being captured;
 //   * all calls share the one array and it keeps the last call's contents:
 //     calls whose work overlaps on the GPU (other streams, other host
 //     threads) race on it -- serialise them;
@@ -26,7 +30,6 @@
 #include <cstdint>
 #include <cstdio>
 #include <cmath>
-#include <mutex>
 
 #include "../../include/psim_gb300.h"
 #include "psim_kernels.cuh"
@@ -37,10 +40,6 @@ namespace {
 
 constexpr size_t kNoAllocBytes = size_t(32) << 20;
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
-
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-void* g_base[kMaxDevices] = {};  // device address of the array, per device
 
 // bump allocator over the static array (256-byte aligned pieces)
 struct Carve {
@@ -101,22 +100,15 @@ extern "C" int psim_cells_build_noalloc(const psim_geometry* gm, const double* d
 
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+    if (e != cudaSuccess)
         return refuse(PSIM_ERR_NO_DEVICE, "no usable CUDA device (%s)", cudaGetErrorString(e));
+    // The host-side name g_noalloc_scratch is not a device address.  Look the
+    // address up on every call, with the caller's device current: it is cheap
+    // once the module is loaded, and it stays right after a device reset.
     void* base = nullptr;
-    {
-        std::lock_guard<std::mutex> lk(g_mu);
-        if (!g_base[dev]) {
-            // once per device, with that device current
-            e = cudaGetSymbolAddress(&g_base[dev], g_noalloc_scratch);
-            if (e != cudaSuccess) {
-                g_base[dev] = nullptr;
-                return refuse(PSIM_ERR_CUDA, "cudaGetSymbolAddress failed: %s",
-                              cudaGetErrorString(e));
-            }
-        }
-        base = g_base[dev];
-    }
+    e = cudaGetSymbolAddress(&base, g_noalloc_scratch);
+    if (e != cudaSuccess || !base)
+        return refuse(PSIM_ERR_CUDA, "cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
 
     DevGeom g{};
     g.n = (int)n;

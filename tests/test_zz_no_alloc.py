@@ -24,7 +24,9 @@ def _case(n, box, scale, seed):
     return pos, rad
 
 
-def _noalloc(psim, torch, geom, pos, rad):
+def _noalloc_rc(psim, torch, geom, pos, rad, stream=None):
+    """Call the entry point on device buffers PyTorch owns; returns the status
+    and the three outputs as host arrays."""
     n, ncell = geom.n_particles, geom.cell_scale ** 3
     dev = torch.device("cuda:0")
     d_pos = torch.from_numpy(pos).to(dev)
@@ -34,12 +36,19 @@ def _noalloc(psim, torch, geom, pos, rad):
     d_srt = torch.empty(4 * n, dtype=torch.float64, device=dev)
     assert d_srt.data_ptr() % 32 == 0
     torch.cuda.synchronize()
+    st = None if stream is None else C.c_void_p(stream.cuda_stream)
     rc = psim.lib().psim_cells_build_noalloc(
         C.byref(geom), C.c_void_p(d_pos.data_ptr()), C.c_void_p(d_rad.data_ptr()),
         C.c_void_p(d_hi.data_ptr()), C.c_void_p(d_cse.data_ptr()),
-        C.c_void_p(d_srt.data_ptr()), None)
+        C.c_void_p(d_srt.data_ptr()), st)
+    torch.cuda.synchronize()
+    return rc, (d_hi.cpu().numpy(), d_cse.cpu().numpy().view(np.uint32), d_srt.cpu().numpy())
+
+
+def _noalloc(psim, torch, geom, pos, rad, stream=None):
+    rc, out = _noalloc_rc(psim, torch, geom, pos, rad, stream)
     assert rc == 0, psim.lib().psim_last_error_string()
-    return (d_hi.cpu().numpy(), d_cse.cpu().numpy().view(np.uint32), d_srt.cpu().numpy())
+    return out
 
 
 @pytest.mark.parametrize("n,box,scale", [(4000, 21.0, 7), (20000, 41.53, 13)])
@@ -54,13 +63,43 @@ def test_noalloc_matches_cells_build_twice(psim, n, box, scale):
             assert np.array_equal(a, b)
 
 
+def test_noalloc_on_a_side_stream(psim):
+    # the work is queued on the caller's stream, not the default one
+    torch = pytest.importorskip("torch")
+    n, box, scale = 4000, 21.0, 7
+    g = psim.geometry(n, box, box / scale, scale)
+    side = torch.cuda.Stream()
+    for seed in (3, 4):
+        pos, rad = _case(n, box, scale, seed)
+        ref = psim.cells_build(g, pos, rad)
+        got = _noalloc(psim, torch, g, pos, rad, stream=side)
+        for a, b in zip(got, ref):
+            assert np.array_equal(a, b)
+
+
+def test_noalloc_reports_a_particle_outside_the_grid(psim):
+    # a position beyond the box hashes outside the grid: the kernel clamps the
+    # cell it writes and raises the 7702 bit, as psim_cells_build does; a
+    # clean call afterwards is unaffected by the flagged one
+    torch = pytest.importorskip("torch")
+    g = psim.geometry(2, 12.0, 3.0, 4)
+    pos = np.array([1.0, 1.0, 1.0, 12.5, 1.0, 1.0])
+    rc, _ = _noalloc_rc(psim, torch, g, pos, np.full(2, 0.5))
+    assert rc == psim.ERR_CELL_BOUNDS
+    pos[3] = 11.5
+    got = _noalloc(psim, torch, g, pos, np.full(2, 0.5))
+    ref = psim.cells_build(g, pos, np.full(2, 0.5))
+    for a, b in zip(got, ref):
+        assert np.array_equal(a, b)
+
+
 def test_noalloc_refuses_oversized_problem(psim):
-    # 2^20 particles need ~80 MB of scratch, beyond the 32 MiB array; the
-    # size check comes before any device work
+    # 2^20 particles need ~80 MB of scratch, beyond the 32 MiB array.  Every
+    # buffer is NULL: the size check refuses first, and were the checks ever
+    # reordered the NULL-buffer check would refuse on the host, so no kernel
+    # can be handed an address it does not own.
     n = 1 << 20
     g = psim.geometry(n, 100.0, 100.0 / 40, 40)
-    rc = psim.lib().psim_cells_build_noalloc(C.byref(g), C.c_void_p(16), C.c_void_p(16),
-                                             C.c_void_p(16), C.c_void_p(16), C.c_void_p(32),
-                                             None)
+    rc = psim.lib().psim_cells_build_noalloc(C.byref(g), None, None, None, None, None, None)
     assert rc == psim.ERR_INPUT
     assert b"static scratch" in psim.lib().psim_last_error_string()
