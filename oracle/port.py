@@ -87,6 +87,8 @@ def lib():
         _lib.oracle_fastrandom_init.argtypes = [C.POINTER(FastRandom)]
         _lib.oracle_fastrandom_g250.argtypes = [C.POINTER(FastRandom), C.c_int]
         _lib.oracle_fastrandom_g250.restype = C.c_double
+        _lib.oracle_fastrandom_fill.argtypes = [C.POINTER(FastRandom), C.c_int, C.c_int, C.c_int,
+                                                C.c_int, P]
     return _lib
 
 
@@ -225,3 +227,25 @@ def fastrandom_draws(seed, count):
     r = FastRandom()
     lib().oracle_fastrandom_init(C.byref(r))
     return np.array([lib().oracle_fastrandom_g250(C.byref(r), seed) for _ in range(count)])
+
+
+class ReferenceNoise:
+    """The reference's own noise stream: one fastRandom generator per particle,
+    seeded seed*(i+1) as brownianIntegrator does (valid while that product
+    fits an int, e.g. N = 4000 at seed 90210).  ``take(k)`` returns the next k
+    steps in the injected-noise layout (k*n*6 doubles); the first call's first
+    step is firstStep's three draws."""
+
+    def __init__(self, n, seed=90210):
+        assert seed * n < 2 ** 31, "seed*(i+1) overflows an int: the reference stream breaks"
+        self.n, self.seed, self.first = int(n), int(seed), 1
+        self.gens = (FastRandom * self.n)()
+        for g in self.gens:
+            lib().oracle_fastrandom_init(C.byref(g))
+
+    def take(self, n_steps):
+        out = np.empty(int(n_steps) * self.n * 6)
+        lib().oracle_fastrandom_fill(self.gens, self.n, self.seed, self.first, int(n_steps),
+                                     _p(out))
+        self.first = 0
+        return out

@@ -595,3 +595,24 @@ double oracle_fastrandom_g250(oracle_fastrandom* r, int seed) {
     r->deviate_available = 0;
     return r->stored_deviate * 1.0 + 0.0;
 }
+
+/* The reference's own noise stream in the injected-noise layout
+ * out[(t*n + i)*6 + k].  Particle i draws from its own generator gens[i]
+ * with threadSeed = seed*(i+1) (brownianIntegrator.cpp:204, :236; int
+ * arithmetic, so valid only while that product fits an int).  The first
+ * step draws memX, memY, memZ (:206-208) into k = 0..2; a normal step draws
+ * the three memCorr deviates then memX, memY, memZ (:238-249) into
+ * k = 0..5.  first != 0: local step 0 is the first step. */
+void oracle_fastrandom_fill(oracle_fastrandom* gens, int n, int seed, int first,
+                            int n_steps, double* out) {
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; i++) {
+        const int ts = (int)(int32_t)((uint32_t)seed * (uint32_t)(i + 1));
+        for (int t = 0; t < n_steps; t++) {
+            double* o = out + ((size_t)t * (size_t)n + (size_t)i) * 6;
+            const int draws = (first && t == 0) ? 3 : 6;
+            for (int k = 0; k < draws; k++) o[k] = oracle_fastrandom_g250(&gens[i], ts);
+            for (int k = draws; k < 6; k++) o[k] = 0.0;
+        }
+    }
+}

@@ -145,6 +145,12 @@ typedef struct {
 } oracle_fastrandom;
 void   oracle_fastrandom_init(oracle_fastrandom* r);
 double oracle_fastrandom_g250(oracle_fastrandom* r, int seed);
+/* n_steps of the reference's own per-particle noise (generators gens[0..n),
+ * threadSeed = seed*(i+1)), in the layout oracle_run takes as injected noise:
+ * out[(t*n + i)*6 + k]; with first != 0 local step 0 is firstStep's three
+ * draws (k = 3..5 zero). */
+void   oracle_fastrandom_fill(oracle_fastrandom* gens, int n, int seed, int first,
+                              int n_steps, double* out);
 
 #ifdef __cplusplus
 }
