@@ -55,7 +55,9 @@ typedef enum {
     PSIM_FORCE_AO = 1,          /* AOPotential/src/AOPotential.cpp */
     PSIM_FORCE_LJ = 2,          /* LennardJones/src/LJPotential.cpp */
     PSIM_FORCE_CALIBRATION = 3, /* Calibration/src/Calibration.cpp */
-    PSIM_FORCE_AO_YUKAWA = 4    /* AO + LJ(n) summed (the reference evaluates one plugin only) */
+    PSIM_FORCE_AO_YUKAWA = 4,   /* AO + LJ(n) summed (the reference evaluates one plugin only) */
+    PSIM_FORCE_PLUGIN = 5       /* a plugin's own device functor, run through its
+                                   psim_force_launch entry (see psim_force_args) */
 } psim_force_kind;
 
 typedef enum {
@@ -74,7 +76,10 @@ typedef enum {
  *                        cutOff (2.5), debyeLength (0.5).
  * Calibration.cpp:30-39: cutOff (1.1).
  * PSIM_FORCE_AO_YUKAWA: the AO part uses kT/well_depth/cutoff, the LJ(n)
- * part kT/well_depth2/yukawa_strength/debye_length/lj_num/cutoff2. */
+ * part kT/well_depth2/yukawa_strength/debye_length/lj_num/cutoff2.
+ * PSIM_FORCE_PLUGIN: the library reads only `cutoff` (the cell-size check,
+ * the candidate test and the pair list's radius); `user` carries whatever
+ * the plugin's functor needs, filled by the plugin itself. */
 typedef struct {
     int32_t kind;
     int32_t lj_num;
@@ -85,6 +90,7 @@ typedef struct {
     double debye_length;
     double cutoff2;
     double well_depth2;
+    double user[8];
 } psim_force_params;
 
 /* Cell-grid geometry: mirrors systemState's boxSize/cellSize/cellScale
@@ -115,6 +121,61 @@ typedef struct {
     int32_t vel_freq;
     int32_t seed;
 } psim_integrator_config;
+
+/* ------------------------------------------------ plugin device entry */
+
+/* What a force plugin's device entry receives: one force pass over the
+ * system's current cell list or pair list, queued on the caller's stream.
+ * The pointers are device memory owned by the library; the plugin owns only
+ * its parameters.  Each force plugin (a shared object that exports the
+ * reference factory getForce(config*), e.g. AOPotential.h:77-80) also
+ * exports
+ *     int psim_force_launch(const psim_force_args* args, void* stream);
+ * built from the library's header-only force templates instantiated with the
+ * plugin's own __device__ pair functor (csrc/psim_plugin.cuh), so a new
+ * potential needs no rebuild of the library.  It returns 0 or a PSIM_ERR_*
+ * code (PSIM_ERR_CUDA for a failed launch); physical errors (overlap,
+ * non-finite force) are latched in *err as the library's own passes do. */
+#define PSIM_FORCE_ABI 1
+typedef enum {
+    PSIM_PASS_FP64 = 0,   /* plain FP64 form, 27-cell walk over pos_fp64 */
+    PSIM_PASS_MIXED = 1,  /* FP32 pairs + Kahan sums, 27-cell walk over pos_hi/pos_lo */
+    PSIM_PASS_LIST = 2    /* FP32 pairs + Kahan sums over the Verlet pair list */
+} psim_force_pass;
+typedef struct {
+    int32_t abi;                      /* PSIM_FORCE_ABI */
+    int32_t pass;                     /* psim_force_pass */
+    const psim_force_params* params;  /* the plugin's parameters */
+    /* the cell grid (systemState's nParticles, cellScale, boxSize, cellSize) */
+    int32_t n_particles;
+    int32_t cell_scale;
+    double box_size;
+    double cell_size;
+    /* the cell list in sorted order (PSIM_PASS_FP64 / PSIM_PASS_MIXED) */
+    const void* pos_fp64;             /* n x {x, y, z, R} doubles, 32-byte aligned */
+    const void* pos_hi;               /* n x {x, y, z, R} floats (rounded) */
+    const void* pos_lo;               /* n x float4 low parts (x - x_hi, ...) */
+    const int32_t* cell_id;           /* cell of each sorted slot */
+    const int32_t* cell_start;        /* first sorted slot of each cell */
+    const int32_t* cell_count;        /* particles of each cell */
+    float prefilter_r2;               /* FP32 candidate bound on r^2 (>= cutoff^2) */
+    int32_t tile;                     /* 0: a warp per 32 sorted particles; 1: a block per cell */
+    /* the Verlet pair list (PSIM_PASS_LIST) */
+    const void* list_pos;             /* records, list order (compact: 16 B; full: 32 B) */
+    const int32_t* list_count;        /* entries of each list slot */
+    const uint32_t* list;             /* entries, groups of 8 per slot */
+    int32_t list_stride;
+    int32_t list_compact;
+    float list_radius;                /* the one radius of compact records */
+    float list_lo_unit;               /* unit of compact records' low parts */
+    /* output, in the pass's order (sorted or list order) */
+    double* fx;
+    double* fy;
+    double* fz;
+    uint32_t* err;                    /* error bits, OR-ed */
+    const int32_t* gate;              /* NULL, or: the pass runs only when *gate != 0 */
+} psim_force_args;
+typedef int (*psim_force_launch_fn)(const psim_force_args* args, void* stream);
 
 /* ------------------------------------------------------------ general */
 
@@ -190,6 +251,16 @@ int psim_force_evaluate(const psim_force_params* params, const psim_geometry* ge
                         const int32_t* particle_hash_index, const uint32_t* cell_start_end,
                         double* particle_force);
 
+/* psim_force_evaluate through a force plugin's device entry (its
+ * psim_force_launch, with its parameters): defaultForceManager::
+ * getAcceleration for a plugin whose pair functor is not built into this
+ * library.  Same arrays, precisions and errors as psim_force_evaluate. */
+int psim_force_evaluate_plugin(psim_force_launch_fn launch, const psim_force_params* params,
+                               const psim_geometry* geom, int32_t precision,
+                               const double* sorted_particles,
+                               const int32_t* particle_hash_index,
+                               const uint32_t* cell_start_end, double* particle_force);
+
 /* The pair list of psim_force_evaluate's mixed precision.  The call walks the
  * pairs within cutOff + skin of a list it built on an earlier call, found
  * from that call's cell list, and keeps doing so while no particle (by its
@@ -247,6 +318,10 @@ typedef struct {
      * each step's force is the same set of pair terms.  Needs
      * cellSize >= cutOff + skin. */
     double skin;
+    /* NULL: the library's own functor for force.kind.  Otherwise a force
+     * plugin's psim_force_launch entry: every force pass of the system runs
+     * through it (force.kind may then be PSIM_FORCE_PLUGIN). */
+    psim_force_launch_fn force_launch;
 } psim_system_config;
 
 /* ---------------------------------------------- initial states (host) */

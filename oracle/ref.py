@@ -46,6 +46,10 @@ def lib():
         _lib.psimref_vgb_coeffs.argtypes = [C.c_char_p, P]
         _lib.psimref_run.argtypes = ([C.c_char_p, C.c_char_p] + [C.c_int] * 5 + [P] * 12
                                      + [C.c_int])
+        _lib.psimref_foreign_forces.argtypes = ([C.c_char_p, C.c_char_p] + [C.c_int] * 4 +
+                                                [P] * 4 + [C.c_int])
+        _lib.psimref_system_constants.argtypes = [C.c_char_p] + [C.POINTER(C.c_int)] * 4 + [
+            C.POINTER(C.c_double)]
     return _lib
 
 
@@ -60,6 +64,30 @@ def write_settings(settings):
         for k, v in settings.items():
             fh.write("%s = %s\n" % (k, v))
     return path
+
+
+def foreign_forces(plugin_path, settings, n, box, cell_size, scale, sorted_, hi, cse,
+                   threads=1):
+    """The reference's defaultForceManager::getAcceleration on a plugin it
+    dlopens by path (runSim.cpp:35-61), e.g. a GB300 plugin; (force, status)."""
+    path = write_settings(settings)
+    try:
+        out = np.zeros(3 * n)
+        rc = lib().psimref_foreign_forces(plugin_path.encode(), path.encode(), n, int(box),
+                                          int(cell_size), scale, _p(sorted_), _p(hi), _p(cse),
+                                          _p(out), threads)
+        return out, rc
+    finally:
+        os.unlink(path)
+
+
+def system_constants(settings_path):
+    """The reference's setSystemConstants on a settings.cfg file: (nParticles,
+    boxSize, cellSize, cellScale, concentration)."""
+    v = [C.c_int() for _ in range(4)]
+    c = C.c_double()
+    lib().psimref_system_constants(settings_path.encode(), *[C.byref(x) for x in v], C.byref(c))
+    return tuple(x.value for x in v) + (c.value,)
 
 
 def build_cells(n, box, cell_size, scale, pos, radius, threads=1):

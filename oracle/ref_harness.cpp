@@ -15,6 +15,7 @@
 // in raw storage and only the members its hot-path methods touch are
 // constructed, which skips the reference's O(N^2) random initialisation.
 #include <bits/stdc++.h>
+#include <dlfcn.h>
 #include <parallel/algorithm>
 #include <omp.h>
 #include <sys/sendfile.h>
@@ -133,6 +134,25 @@ void set_threads(int nthreads) {
 
 extern "C" {
 
+// system::setSystemConstants (system.cpp:28-65) on a settings.cfg file: the
+// integer box and cell edge the reference derives from nParticles, conc,
+// radius and scale, and the concentration it reports.
+int psimref_system_constants(const char* settings_path, int* n, int* box, int* cell_size,
+                             int* scale, double* concentration) {
+    PSim::config cfg{std::string(settings_path)};
+    void* mem = ::operator new(sizeof(PSim::system));
+    std::memset(mem, 0, sizeof(PSim::system));
+    PSim::system* s = static_cast<PSim::system*>(mem);
+    new (&s->trialName) std::string("/tmp/psimref_trial");
+    s->setSystemConstants(&cfg, nullptr, nullptr);
+    *n = s->state.nParticles;
+    *box = s->state.boxSize;
+    *cell_size = s->state.cellSize;
+    *scale = s->state.cellScale;
+    *concentration = s->state.concentration;
+    return 0;
+}
+
 // Reference cell-list build on the given positions (original order).
 int psimref_build_cells(int n, int box, int cell_size, int scale, const double* pos,
                         const double* radius, int* hash_index, uint32_t* cse, double* sorted,
@@ -155,6 +175,39 @@ int psimref_forces(const char* plugin, const char* settings_path, int n, int box
     PSim::config cfg{std::string(settings_path)};
     PSim::IForce* f = make_force(plugin, &cfg);
     if (!f) return 100;
+    PSim::defaultForceManager* mgr = new PSim::defaultForceManager();
+    mgr->addForce(f);
+    set_threads(nthreads);
+    PSim::systemState st = PSim::systemState();
+    st.nParticles = n;
+    st.boxSize = box;
+    st.cellSize = cell_size;
+    st.cellScale = scale;
+    std::vector<std::tuple<int, int>> phi(n), cells((size_t)scale * scale * scale);
+    for (int i = 0; i < n; i++) phi[i] = std::make_tuple(hash_index[2 * i], hash_index[2 * i + 1]);
+    for (size_t c = 0; c < cells.size(); c++)
+        cells[c] = std::make_tuple((int)cse[2 * c], (int)cse[2 * c + 1]);
+    std::vector<double> sp(sorted, sorted + 4 * (size_t)n);
+    mgr->getAcceleration(sp.data(), force, &phi, &cells, &st);
+    return 0;
+}
+
+// The reference's own force call on a plugin it loads the way runSim.cpp:
+// 35-61 does (dlopen + dlsym "getForce"), given by path: a plugin built
+// outside the reference (a GB300 plugin) driven through the reference's
+// config, IForce vtable and defaultForceManager::getAcceleration.  Returns
+// 100 when the plugin does not load.
+int psimref_foreign_forces(const char* plugin_path, const char* settings_path, int n, int box,
+                           int cell_size, int scale, const double* sorted,
+                           const int* hash_index, const uint32_t* cse, double* force,
+                           int nthreads) {
+    void* lib = dlopen(plugin_path, RTLD_NOW | RTLD_LOCAL);
+    if (!lib) return 100;
+    typedef PSim::IForce* factory_t(PSim::config*);
+    factory_t* factory = (factory_t*)dlsym(lib, "getForce");
+    if (!factory) return 100;
+    PSim::config cfg{std::string(settings_path)};
+    PSim::IForce* f = factory(&cfg);
     PSim::defaultForceManager* mgr = new PSim::defaultForceManager();
     mgr->addForce(f);
     set_threads(nthreads);

@@ -7,7 +7,7 @@ Berendsen integrator -- runs as hand-written sm_103a CUDA kernels in
 (``include/psim_gb300.h``) with the reference's names:
 
     Config                  settings.cfg reader          (config.h)
-    load_force              "./<force>.so" + getForce    (runSim.cpp:29-79)
+    load_force / load_plugin "./<force>.so" + getForce   (runSim.cpp:29-79)
     cells_build             hash/sort/clear/reorder      (systemHandling.cpp:33-85)
     force_evaluate          defaultForceManager::getAcceleration
     vgb_coefficients        brownianIntegrator set-up
@@ -38,11 +38,12 @@ ERR_INPUT = 7706
 ERR_CUDA = 7790
 ERR_NO_DEVICE = 7791
 
-FORCE_AO, FORCE_LJ, FORCE_CALIBRATION, FORCE_AO_YUKAWA = 1, 2, 3, 4
+FORCE_AO, FORCE_LJ, FORCE_CALIBRATION, FORCE_AO_YUKAWA, FORCE_PLUGIN = 1, 2, 3, 4, 5
 PRECISION_FP64, PRECISION_MIXED = 0, 1
 NOISE_PHILOX, NOISE_INJECTED = 0, 1
 
-KIND_NAMES = {FORCE_AO: "AO", FORCE_LJ: "LJ", FORCE_CALIBRATION: "CAL", FORCE_AO_YUKAWA: "AO_YUK"}
+KIND_NAMES = {FORCE_AO: "AO", FORCE_LJ: "LJ", FORCE_CALIBRATION: "CAL", FORCE_AO_YUKAWA: "AO_YUK",
+              FORCE_PLUGIN: "PLUGIN"}
 
 
 class PsimError(RuntimeError):
@@ -55,11 +56,13 @@ class ForceParams(C.Structure):
     _fields_ = [("kind", C.c_int32), ("lj_num", C.c_int32), ("kT", C.c_double),
                 ("cutoff", C.c_double), ("well_depth", C.c_double),
                 ("yukawa_strength", C.c_double), ("debye_length", C.c_double),
-                ("cutoff2", C.c_double), ("well_depth2", C.c_double)]
+                ("cutoff2", C.c_double), ("well_depth2", C.c_double),
+                ("user", C.c_double * 8)]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_}
         d["kind"] = KIND_NAMES[self.kind]
+        d["user"] = list(self.user)
         return d
 
     def max_cutoff(self):
@@ -88,7 +91,7 @@ class IntegratorConfig(C.Structure):
 class SystemConfig(C.Structure):
     _fields_ = [("geom", Geometry), ("integ", IntegratorConfig), ("force", ForceParams),
                 ("precision", C.c_int32), ("noise_mode", C.c_int32), ("device", C.c_int32),
-                ("skin", C.c_double)]
+                ("skin", C.c_double), ("force_launch", C.c_void_p)]
 
 
 class Replica(C.Structure):
@@ -115,6 +118,7 @@ def lib():
             "psim_cells_build": ([C.POINTER(Geometry), P, P, P, P, P], C.c_int),
             "psim_cells_build_noalloc": ([C.POINTER(Geometry), P, P, P, P, P, P], C.c_int),
             "psim_force_evaluate": ([C.POINTER(ForceParams), C.POINTER(Geometry), C.c_int32, P, P, P, P], C.c_int),
+            "psim_force_evaluate_plugin": ([P, C.POINTER(ForceParams), C.POINTER(Geometry), C.c_int32, P, P, P, P], C.c_int),
             "psim_force_set_list_skin": ([C.c_double], C.c_int),
             "psim_force_list_stats": ([C.POINTER(C.c_int64), C.POINTER(C.c_int64)], C.c_int),
             "psim_vgb_coefficients": ([C.c_double] * 3 + [C.POINTER(VgbCoeffs)], C.c_int),
@@ -251,6 +255,38 @@ class Config:
         return v
 
 
+def system_constants(cfg):
+    """system::setSystemConstants (system.cpp:28-65): the run constants of a
+    settings.cfg (a Config).  The box holds nParticles spheres of ``radius``
+    at volume fraction ``conc``, cut to a whole number of integer cells:
+    L = int(cbrt(vP / conc)), cellSize = L // scale, L = cellSize * scale; the
+    concentration is that of the quantised box.  A ``boxSize`` key (never read
+    by the reference) gives a real-valued box cut into ``scale`` cells.
+    Returns (state dict, Geometry)."""
+    import math
+    n = cfg.get("nParticles", 1000)
+    conc = cfg.get("conc", 0.01)
+    scale = cfg.get("scale", 4)
+    r = cfg.get("radius", 0.5)
+    vp = n * (4.0 / 3.0) * math.atan(1.0) * 4.0 * r * r * r
+    if "boxSize" in cfg.options:
+        box = cfg.get("boxSize", 0.0)
+        cell = box / scale
+        st = {"boxSize": int(box), "cellSize": int(cell), "concentration": vp / box ** 3}
+    else:
+        ibox = int(np.cbrt(vp / conc))      # libm cbrt, truncated as the (int) cast
+        cell_i = ibox // scale if scale else 0
+        box = float(cell_i * scale)
+        cell = float(cell_i)
+        st = {"boxSize": cell_i * scale, "cellSize": cell_i,
+              "concentration": vp / math.pow(box, 3.0)}
+    dt = cfg.get("timeStep", 0.001)
+    st.update(nParticles=n, cellScale=scale, dTime=dt, seed=cfg.get("seed", 90210),
+              temp=cfg.get("kT", 1.0), outputFreq=cfg.get("outputFreq", int(1.0 / dt)),
+              radius=r, mass=cfg.get("mass", 1.0))
+    return st, geometry(n, box, cell, scale)
+
+
 def force_params_from_settings(plugin, text):
     p = ForceParams()
     _check(lib().psim_force_params_from_settings(plugin.encode(), text.encode(), C.byref(p)))
@@ -259,21 +295,53 @@ def force_params_from_settings(plugin, text):
 
 def load_force(cfg, plugin_dir=PLUGIN_DIR):
     """runSim.cpp:29-79: open ``<plugin_dir>/<force>.so`` named by the
-    ``force`` key and take the device functor parameters its factory builds
-    from the same settings."""
-    name = cfg.get("force", "")
-    path = os.path.join(plugin_dir, name + ".so")
-    if not os.path.exists(path):
-        raise PsimError(ERR_LOAD, "cannot load force library %s" % path)
-    plug = C.CDLL(path)
-    if not hasattr(plug, "getForce"):
-        raise PsimError(ERR_LOAD, "could not find symbol getForce in %s" % path)
-    fn = plug.psim_plugin_params
-    fn.argtypes = [C.c_char_p, C.POINTER(ForceParams)]
-    fn.restype = C.c_int
-    p = ForceParams()
-    fn(cfg.text.encode(), C.byref(p))
-    return p
+    ``force`` key and take the parameters its factory builds from the same
+    settings (the plugin itself: load_plugin)."""
+    return load_plugin(cfg, plugin_dir).params
+
+
+class ForcePlugin:
+    """A force plugin shared object: the reference factory getForce(config*)
+    plus the GB300 device entry psim_force_launch, whose force passes run the
+    plugin's own __device__ pair functor.  ``params`` are the parameters its
+    factory builds from the settings text; System and force_evaluate take
+    the plugin in place of a ForceParams and run it through its entry."""
+
+    def __init__(self, path, settings_text=""):
+        if not os.path.exists(path):
+            raise PsimError(ERR_LOAD, "cannot load force library %s" % path)
+        self.path = path
+        self.lib = C.CDLL(path)
+        for sym in ("getForce", "psim_plugin_abi", "psim_plugin_params", "psim_force_launch"):
+            if not hasattr(self.lib, sym):
+                raise PsimError(ERR_LOAD, "could not find symbol %s in %s" % (sym, path))
+        if self.lib.psim_plugin_abi() != 1:
+            raise PsimError(ERR_LOAD, "%s was built for another device-entry ABI" % path)
+        fn = self.lib.psim_plugin_params
+        fn.argtypes = [C.c_char_p, C.POINTER(ForceParams)]
+        fn.restype = C.c_int
+        self.params = ForceParams()
+        _check(fn(settings_text.encode(), C.byref(self.params)))
+        self.launch = C.cast(self.lib.psim_force_launch, C.c_void_p).value
+
+    def as_dict(self):
+        return self.params.as_dict()
+
+    def max_cutoff(self):
+        return self.params.max_cutoff()
+
+
+def load_plugin(cfg, plugin_dir=PLUGIN_DIR):
+    """runSim.cpp:29-79: the plugin ``<plugin_dir>/<force>.so`` named by the
+    ``force`` key, with the parameters its factory builds from cfg."""
+    return ForcePlugin(os.path.join(plugin_dir, cfg.get("force", "") + ".so"), cfg.text)
+
+
+def _force_of(force):
+    """(parameters, device entry or None) of a ForceParams or ForcePlugin."""
+    if isinstance(force, ForcePlugin):
+        return force.params, force.launch
+    return force, None
 
 
 def make_force(kind, cutoff, kT=1.0, well_depth=0.0, yukawa_strength=0.0, debye_length=0.5,
@@ -328,14 +396,20 @@ def cells_build(geom, pos, radius, out=None):
 def force_evaluate(params, geom, sorted_particles, hash_index, cell_start_end,
                    precision=PRECISION_FP64, out=None):
     """defaultForceManager::getAcceleration on the reference's arrays; returns
-    particle_force[3n] in original order (written into `out` when given)."""
+    particle_force[3n] in original order (written into `out` when given).
+    params: a ForceParams, or a ForcePlugin (run through its device entry)."""
     n = geom.n_particles
     srt = _f64(sorted_particles, 4 * n)
     hi = np.ascontiguousarray(hash_index, np.int32).reshape(-1)
     cse = np.ascontiguousarray(cell_start_end, np.uint32).reshape(-1)
     out = _out(out, np.float64, 3 * n)
-    _check(lib().psim_force_evaluate(C.byref(params), C.byref(geom), precision, _p(srt), _p(hi),
-                                     _p(cse), _p(out)))
+    fp, launch = _force_of(params)
+    if launch:
+        _check(lib().psim_force_evaluate_plugin(launch, C.byref(fp), C.byref(geom), precision,
+                                                _p(srt), _p(hi), _p(cse), _p(out)))
+    else:
+        _check(lib().psim_force_evaluate(C.byref(fp), C.byref(geom), precision, _p(srt),
+                                         _p(hi), _p(cse), _p(out)))
     return out
 
 
@@ -412,16 +486,19 @@ class System:
 
     def __init__(self, geom, force, gamma=1.0, dt=0.001, kT=1.0, vel_freq=1000, seed=90210,
                  precision=PRECISION_MIXED, noise_mode=NOISE_PHILOX, device=0, skin=0.0):
-        """skin: Verlet pair-list skin of the mixed form (0: walk the 27 cells
-        every step; "auto": the largest of 0.4 and cellSize - cutOff that the
-        cell size allows, if at least 0.1)."""
+        """force: a ForceParams, or a ForcePlugin whose device entry runs every
+        force pass.  skin: Verlet pair-list skin of the mixed form (0: walk the
+        27 cells every step; "auto": the largest of 0.4 and cellSize - cutOff
+        that the cell size allows, if at least 0.1)."""
         if skin == "auto":
             skin = auto_skin(geom, force) if precision == PRECISION_MIXED else 0.0
+        fp, launch = _force_of(force)
+        self._plugin = force if launch else None   # keeps the plugin library loaded
         self.cfg = SystemConfig(geom=geom,
                                 integ=IntegratorConfig(gamma=gamma, dt=dt, kT=kT,
                                                        vel_freq=vel_freq, seed=seed),
-                                force=force, precision=precision, noise_mode=noise_mode,
-                                device=device, skin=float(skin))
+                                force=fp, precision=precision, noise_mode=noise_mode,
+                                device=device, skin=float(skin), force_launch=launch)
         self.skin = float(skin)
         self.n = geom.n_particles
         self.ncell = geom.cell_scale ** 3

@@ -7,7 +7,9 @@ Translation units are compiled in parallel with one -gencode each:
   psim_cells.cu  integer counting sort and layout conversions
   psim_api.cu    host side of the C ABI
   psim_noalloc.cu  the cell-list build on a static device scratch array
-The CUDA runtime is linked statically, so the library needs only the driver.
+and the three force plugins (csrc/plugins/*.cu, each compiled twice, see
+build_force_plugin).  The CUDA runtime is linked statically, so the library
+and the plugins need only the driver.
 Output goes next to this file (git-ignored) and is what the package loads.
 """
 import os
@@ -48,11 +50,12 @@ def _stale(target, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def _compile(src, extra, verbose):
-    obj = os.path.join(OUT_DIR, src.replace(".cu", ".o"))
+def _compile_any(src, extra, obj, verbose):
+    """nvcc -c src -> obj (skipped when obj is newer than src, the library's
+    headers and this recipe)."""
     headers = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith(".cuh")]
-    deps = [os.path.join(CSRC, src)] + headers + [
-        os.path.join(ROOT, "include", "psim_gb300.h"), __file__]
+    deps = [src] + headers + [os.path.join(ROOT, "include", h)
+                              for h in ("psim_gb300.h", "psim_gb300.hpp")] + [__file__]
     if not _stale(obj, deps):
         return obj
     # -ffp-contract=off: the host compiler on Arm contracts a*b+c into FMA by
@@ -60,7 +63,7 @@ def _compile(src, extra, verbose):
     cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
            "-Xcompiler", "-fno-fast-math", "-Xcompiler", "-ffp-contract=off",
            "--expt-relaxed-constexpr", *extra,
-           "-c", os.path.join(CSRC, src), "-o", obj + ".tmp"]
+           "-c", src, "-o", obj + ".tmp"]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -72,52 +75,75 @@ def _compile(src, extra, verbose):
     return obj
 
 
-def build(verbose=False, force=False):
-    """Compile every translation unit and link libpsim_gb300.so; returns its path."""
-    os.makedirs(OUT_DIR, exist_ok=True)
-    if force:
-        for f in os.listdir(OUT_DIR):
-            os.unlink(os.path.join(OUT_DIR, f))
-    with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        objs = list(ex.map(lambda kv: _compile(kv[0], kv[1], verbose), SOURCES.items()))
-    if _stale(LIB, objs):
-        tmp = LIB + ".tmp%d" % os.getpid()
-        cmd = [nvcc(), *ARCH, "-shared", "-cudart", "static", "-o", tmp, *objs]
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
-        os.replace(tmp, LIB)
-    build_plugins()
-    return LIB
+def _link(objs, out):
+    if not _stale(out, objs):
+        return out
+    os.makedirs(os.path.dirname(out), exist_ok=True)
+    tmp = out + ".tmp%d" % os.getpid()
+    cmd = [nvcc(), *ARCH, "-shared", "-cudart", "static", "-o", tmp, *objs]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("link of %s failed:\n%s\n%s" % (out, r.stdout, r.stderr))
+    os.replace(tmp, out)
+    return out
 
 
+# The force plugins built with the library: the reference's three plugins,
+# each exporting getForce(config*) and the device entry psim_force_launch.
 PLUGINS = ["AOPotential", "LennardJones", "Calibration"]
+PLUGIN_DIR = os.path.join(HERE, "plugins")
 # the names the reference's own settings.cfg files use for the same plugins
 ALIASES = {"AO": "AOPotential", "LJ": "LennardJones", "Cal": "Calibration"}
 
 
-def build_plugins():
-    """The drop-in force plugins: AOPotential.so, LennardJones.so and
-    Calibration.so, each exporting the reference's getForce(config*) factory
-    (host C++ only; the device functors live in libpsim_gb300.so)."""
-    src = os.path.join(CSRC, "plugins", "psim_plugin.cpp")
-    hdr = os.path.join(ROOT, "include", "psim_gb300.hpp")
+def _plugin_jobs(src, obj_dir, verbose=False, include_dirs=()):
+    """The two compiles of a plugin source (psim_plugin.cuh): part 1, the
+    plain FP64 pass, without FMA contraction; part 2, the mixed passes and
+    the host entries."""
+    base = os.path.splitext(os.path.basename(src))[0]
+    inc = [x for d in include_dirs for x in ("-I", d)]
+    return [
+        (src, ["-DPSIM_PLUGIN_PART=1", "--fmad=false", *inc],
+         os.path.join(obj_dir, base + ".part1.o"), verbose),
+        (src, ["-DPSIM_PLUGIN_PART=2", *inc], os.path.join(obj_dir, base + ".part2.o"), verbose),
+    ]
+
+
+def build_force_plugin(src, out=None, include_dirs=(), verbose=False):
+    """Compile a force plugin source into a shared object (default: the
+    source's name + .so beside it) and return its path.  The source includes
+    proteinsim2015_gb300/csrc/psim_plugin.cuh and ends with
+    PSIM_FORCE_PLUGIN(Class); it needs nothing else of the library."""
+    src = os.path.abspath(src)
+    out = out or os.path.splitext(src)[0] + ".so"
+    obj_dir = os.path.join(os.path.dirname(os.path.abspath(out)), "_build")
+    os.makedirs(obj_dir, exist_ok=True)
+    objs = [_compile_any(*j) for j in _plugin_jobs(src, obj_dir, verbose, include_dirs)]
+    return _link(objs, out)
+
+
+def build(verbose=False, force=False):
+    """Compile every translation unit, link libpsim_gb300.so and the force
+    plugins; returns the library's path."""
+    os.makedirs(OUT_DIR, exist_ok=True)
+    if force:
+        for f in os.listdir(OUT_DIR):
+            os.unlink(os.path.join(OUT_DIR, f))
+    jobs = [(os.path.join(CSRC, src), extra, os.path.join(OUT_DIR, src.replace(".cu", ".o")),
+             verbose) for src, extra in SOURCES.items()]
     for name in PLUGINS:
-        out = os.path.join(HERE, "plugins", name + ".so")
-        if not _stale(out, [src, hdr, os.path.join(ROOT, "include", "psim_gb300.h")]):
-            continue
-        os.makedirs(os.path.dirname(out), exist_ok=True)
-        cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off",
-               "-I", os.path.join(ROOT, "include"),
-               "-DPSIM_PLUGIN_NAME=\"%s\"" % name, src, "-o", out + ".tmp"]
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError("plugin build failed for %s:\n%s" % (name, r.stderr))
-        os.replace(out + ".tmp", out)
+        jobs += _plugin_jobs(os.path.join(CSRC, "plugins", name + ".cu"), OUT_DIR, verbose)
+    with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
+        objs = list(ex.map(lambda j: _compile_any(*j), jobs))
+    _link(objs[:len(SOURCES)], LIB)
+    for k, name in enumerate(PLUGINS):
+        i = len(SOURCES) + 2 * k
+        _link(objs[i:i + 2], os.path.join(PLUGIN_DIR, name + ".so"))
     for alias, name in ALIASES.items():
-        link = os.path.join(HERE, "plugins", alias + ".so")
+        link = os.path.join(PLUGIN_DIR, alias + ".so")
         if not os.path.lexists(link):
             os.symlink(name + ".so", link)
+    return LIB
 
 
 if __name__ == "__main__":

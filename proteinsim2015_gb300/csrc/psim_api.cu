@@ -126,8 +126,19 @@ struct Settings {
 
 // ------------------------------------------------------------- validation
 
-int check_params(const psim_force_params* p) {
+// plugin: the force runs through a plugin's device entry, which owns the
+// meaning of every parameter but the cutoff.
+int check_params(const psim_force_params* p, bool plugin = false) {
     if (!p) return fail(PSIM_ERR_INPUT, "force params are NULL");
+    if (plugin) {
+        if (!(p->cutoff > 0.0) || !std::isfinite(p->cutoff))
+            return fail(PSIM_ERR_INPUT, "cutOff must be positive and finite");
+        if (p->kind == 4 && !(p->cutoff2 > 0.0))
+            return fail(PSIM_ERR_INPUT, "the composite needs the LJ part's cutOff");
+        return PSIM_OK;
+    }
+    if (p->kind == PSIM_FORCE_PLUGIN)
+        return fail(PSIM_ERR_INPUT, "force kind PSIM_FORCE_PLUGIN needs the plugin's psim_force_launch");
     if (p->kind < 1 || p->kind > 4) return fail(PSIM_ERR_INPUT, "unknown force kind %d", p->kind);
     if (!(p->cutoff > 0.0) || !std::isfinite(p->cutoff))
         return fail(PSIM_ERR_INPUT, "cutOff must be positive and finite");
@@ -161,40 +172,10 @@ int make_geom(const psim_geometry* gm, double rc_max, DevGeom* g) {
                     gm->box_size);
     if (rc_max > 0.0 && gm->cell_size < rc_max)
         return fail(PSIM_ERR_INPUT, "cellSize %.9g is below the cutoff %.9g", gm->cell_size, rc_max);
-    g->n = gm->n_particles;
-    g->s = gm->cell_scale;
-    g->s2 = g->s * g->s;
-    g->ncell = g->s2 * g->s;
-    g->L = gm->box_size;
-    g->half = g->L / 2.0;
-    double fl = std::floor(g->L);
-    g->half_uv = (fl == g->L && g->L < 2147483647.0) ? (double)(((int)g->L) / 2) : g->L / 2.0;
-    g->cs = gm->cell_size;
-    g->inv_cs = 1.0 / gm->cell_size;
-    g->Lhi = (float)g->L;
-    g->Llo = (float)(g->L - (double)g->Lhi);
-    g->inv_csf = (float)g->inv_cs;
-    // FP32 hash error: x cut or rounded to FP32 (< ulp(L)) scaled by 1/cs, plus
-    // the roundings of 1/cs and of the product (each ~s 2^-24 cells); 4x that
-    // is the guard
-    const double ex = std::ldexp(1.0, std::ilogb(std::max(g->L, 1.0)) - 23) * g->inv_cs +
-                      2.0 * g->s * std::ldexp(1.0, -24);
-    const double guard = 4.0 * ex + 1e-6;
-    g->hash_guard = guard < 0.25 ? (float)guard : 0.5f;  // 0.5: always the FP64 path
-    g->c0 = 0;
-    g->p0 = 0;
-    g->p1 = g->n;
+    fill_geom(gm->n_particles, gm->cell_scale, gm->box_size, gm->cell_size, g);
     return PSIM_OK;
 }
 
-void ao_coeffs(double kT, double wd, double rc, double* c1, double* c2) {  // AOPotential.cpp:50-55
-    double q = rc / (rc - 1.0);
-    double a1 = -kT * wd * q * q * q;
-    double a2 = -3.0 / (2.0 * rc);
-    double a3 = 1.0 / (2.0 * rc * rc * rc);
-    *c1 = -a1 * a2;
-    *c2 = -3.0 * a1 * a3;
-}
 
 // The FP32 candidate test sees positions rounded to FP32 (ulp(L)/2 each),
 // L rounded (ulp(L)/2), the imaged home position rounded (ulp(L)) and the
@@ -248,32 +229,11 @@ double dropin_skin(double want, const DevGeom& g, double rc) {
 ForceSetup make_setup(const psim_force_params* p, double L) {
     ForceSetup fs{};
     fs.kind = p->kind;
-    double rc_ao = p->cutoff;
-    double rc_lj = p->kind == 4 ? p->cutoff2 : p->cutoff;
-    double c1, c2;
-    ao_coeffs(p->kT, p->well_depth, rc_ao, &c1, &c2);
-    fs.ao.rc2 = rc_ao * rc_ao;
-    fs.ao.c1 = c1;
-    fs.ao.c2 = c2;
-    fs.ao.rc2f = (float)fs.ao.rc2;
-    fs.ao.c1f = (float)c1;
-    fs.ao.c2f = (float)c2;
-    double wd_lj = p->kind == 4 ? p->well_depth2 : p->well_depth;
-    fs.lj.rc2 = rc_lj * rc_lj;
-    fs.lj.kTwd = p->kT * wd_lj;
-    fs.lj.n = p->lj_num;
-    fs.lj.four_n = 4.0 * p->lj_num;
-    fs.lj.yuk = p->yukawa_strength;
-    fs.lj.lambda = p->debye_length;
-    fs.lj.inv_lambda = 1.0 / p->debye_length;
-    fs.lj.rc2f = (float)fs.lj.rc2;
-    fs.lj.kTwdf = (float)fs.lj.kTwd;
-    fs.lj.four_nf = (float)fs.lj.four_n;
-    fs.lj.yukf = (float)fs.lj.yuk;
-    fs.lj.lambdaf = (float)fs.lj.lambda;
-    fs.lj.inv_lambdaf = (float)fs.lj.inv_lambda;
-    fs.cal.rc2 = p->cutoff * p->cutoff;
-    fs.cal.rc2f = (float)fs.cal.rc2;
+    const double rc_lj = p->kind == 4 ? p->cutoff2 : p->cutoff;
+    const double wd_lj = p->kind == 4 ? p->well_depth2 : p->well_depth;
+    fs.ao = make_ao_pair(p->kT, p->well_depth, p->cutoff);
+    fs.lj = make_lj_pair(p->kT, wd_lj, p->lj_num, p->yukawa_strength, p->debye_length, rc_lj);
+    fs.cal = make_cal_pair(p->cutoff);
     fs.rc_max = max_cutoff(p);
     fs.pre_rc2f = prefilter_r2(fs.rc_max, L);
     fs.lj_pure = p->kind == PSIM_FORCE_LJ && p->yukawa_strength == 0.0;
@@ -293,6 +253,57 @@ int choose_tile(const DevGeom&) {
     }
     return 0;
 }
+
+// One force pass: the library's own functor for the parameters' kind, or a
+// plugin's device entry (psim_force_launch) with the same arrays.  pass:
+// psim_force_pass; cv for the cell walks, pl for the pair list.
+struct ForceRunner {
+    const ForceSetup* fs;
+    psim_force_launch_fn plugin;
+    const psim_force_params* params;
+    cudaError_t run(int pass, const DevGeom& g, const CellView* cv, const PairList* pl,
+                    const ForceOut& out, cudaStream_t st) const {
+        if (!plugin) {
+            if (pass == PSIM_PASS_LIST) return launch_forces_list(*fs, g, *pl, out, st);
+            if (pass == PSIM_PASS_FP64) return launch_forces_fp64(*fs, g, *cv, out, st);
+            return launch_forces_mixed(*fs, g, *cv, out, st);
+        }
+        psim_force_args a{};
+        a.abi = PSIM_FORCE_ABI;
+        a.pass = pass;
+        a.params = params;
+        a.n_particles = g.n;
+        a.cell_scale = g.s;
+        a.box_size = g.L;
+        a.cell_size = g.cs;
+        if (cv) {
+            a.pos_fp64 = cv->posd;
+            a.pos_hi = cv->posh;
+            a.pos_lo = cv->posl;
+            a.cell_id = cv->cellid;
+            a.cell_start = cv->cstart;
+            a.cell_count = cv->ccount;
+        }
+        a.prefilter_r2 = fs->pre_rc2f;
+        a.tile = fs->tile;
+        if (pl) {
+            a.list_pos = pl->pos;
+            a.list_count = pl->count;
+            a.list = pl->list;
+            a.list_stride = pl->stride;
+            a.list_compact = pl->compact;
+            a.list_radius = pl->radius;
+            a.list_lo_unit = pl->lo_unit;
+        }
+        a.fx = out.fx;
+        a.fy = out.fy;
+        a.fz = out.fz;
+        a.err = out.err;
+        a.gate = out.gate;
+        // the plugin's own CUDA runtime reports its launch errors as a status
+        return plugin(&a, st) == PSIM_OK ? cudaSuccess : cudaErrorLaunchFailure;
+    }
+};
 
 // brownianIntegrator.cpp:27-99 with setupHigh/setupLow/setupZero (:111-175)
 void vgb_coeffs(double gamma, double dt, double kT, psim_vgb_coeffs* c) {
@@ -501,7 +512,7 @@ int ws_begin(Workspace& w) {
 
 extern "C" {
 
-int psim_abi_version(void) { return 2; }
+int psim_abi_version(void) { return 3; }
 
 // Lets other translation units of this library report through
 // psim_last_error_string (not part of the public header).
@@ -673,10 +684,11 @@ int psim_cells_build(const psim_geometry* gm, const double* pos, const double* r
 
 // ----------------------------------------------------------- force drop-in
 
-int psim_force_evaluate(const psim_force_params* params, const psim_geometry* gm,
-                        int32_t precision, const double* sorted, const int32_t* hash_index,
-                        const uint32_t* cse, double* force) {
-    int rc = check_params(params);
+namespace {
+int force_evaluate(psim_force_launch_fn plugin, const psim_force_params* params,
+                   const psim_geometry* gm, int32_t precision, const double* sorted,
+                   const int32_t* hash_index, const uint32_t* cse, double* force) {
+    int rc = check_params(params, plugin != nullptr);
     if (rc) return rc;
     DevGeom g;
     if ((rc = make_geom(gm, max_cutoff(params), &g))) return rc;
@@ -687,6 +699,7 @@ int psim_force_evaluate(const psim_force_params* params, const psim_geometry* gm
     if ((rc = ensure_device())) return rc;
     ForceSetup fs = make_setup(params, g.L);
     fs.tile = choose_tile(g);
+    const ForceRunner fr{&fs, plugin, params};
     Workspace& w = g_ws;
     std::lock_guard<std::mutex> lk(w.mu);
     if ((rc = ws_begin(w))) return rc;
@@ -766,7 +779,7 @@ int psim_force_evaluate(const psim_force_params* params, const psim_geometry* gm
                                       w.lcompact ? 1.0f / w.lunit : 0.f, w.lradius, flags, st));
         const PairList pl{nullptr, w.lpos.as<float4>(), w.lcount.as<int>(),
                           w.list.as<uint32_t>(), g.n, w.lcompact, w.lradius, w.lunit};
-        PSIM_CUDA(launch_forces_list(fs, g, pl, out, st));
+        PSIM_CUDA(fr.run(PSIM_PASS_LIST, g, nullptr, &pl, out, st));
         PSIM_CUDA(launch_export_force(g.n, w.lslot_of.as<int>(), f, f + n, f + 2 * n,
                                       w.direct ? force : w.force.as<double>(), st));
         if (!w.direct)
@@ -821,7 +834,7 @@ int psim_force_evaluate(const psim_force_params* params, const psim_geometry* gm
             // a denser neighbourhood than the list has room for: the cell walk
             bits = 0;
             PSIM_CUDA(cudaMemsetAsync(w.err.p, 0, 4, st));
-            PSIM_CUDA(launch_forces_mixed(fs, g, cv, out, st));
+            PSIM_CUDA(fr.run(PSIM_PASS_MIXED, g, &cv, nullptr, out, st));
         } else if (bits == 0) {
             listed = true;
             w.lcompact = compact;
@@ -839,13 +852,13 @@ int psim_force_evaluate(const psim_force_params* params, const psim_geometry* gm
         if (listed) {
             const PairList pl{nullptr, w.lpos.as<float4>(), w.lcount.as<int>(),
                               w.list.as<uint32_t>(), g.n, w.lcompact, w.lradius, w.lunit};
-            PSIM_CUDA(launch_forces_list(fs, g, pl, out, st));
+            PSIM_CUDA(fr.run(PSIM_PASS_LIST, g, nullptr, &pl, out, st));
             inv = w.lslot_of.as<int>();
         }
     } else if (precision == PSIM_PRECISION_FP64) {
-        PSIM_CUDA(launch_forces_fp64(fs, g, cv, out, st));
+        PSIM_CUDA(fr.run(PSIM_PASS_FP64, g, &cv, nullptr, out, st));
     } else {
-        PSIM_CUDA(launch_forces_mixed(fs, g, cv, out, st));
+        PSIM_CUDA(fr.run(PSIM_PASS_MIXED, g, &cv, nullptr, out, st));
     }
     if (!inv) {   // this call's sorted order
         PSIM_CUDA(launch_invert_tags(g.n, w.tag_out.as<int>(), w.inv.as<int>(), st));
@@ -862,6 +875,21 @@ int psim_force_evaluate(const psim_force_params* params, const psim_geometry* gm
         return fail(code_from_bits(bits), "%s", bits_text(bits));
     }
     return PSIM_OK;
+}
+}  // namespace
+
+int psim_force_evaluate(const psim_force_params* params, const psim_geometry* gm,
+                        int32_t precision, const double* sorted, const int32_t* hash_index,
+                        const uint32_t* cse, double* force) {
+    return force_evaluate(nullptr, params, gm, precision, sorted, hash_index, cse, force);
+}
+
+int psim_force_evaluate_plugin(psim_force_launch_fn launch, const psim_force_params* params,
+                               const psim_geometry* gm, int32_t precision,
+                               const double* sorted, const int32_t* hash_index,
+                               const uint32_t* cse, double* force) {
+    if (!launch) return fail(PSIM_ERR_INPUT, "the plugin's psim_force_launch is NULL");
+    return force_evaluate(launch, params, gm, precision, sorted, hash_index, cse, force);
 }
 
 int psim_force_set_list_skin(double skin) {
@@ -1215,6 +1243,17 @@ cudaError_t enqueue_list_build(psim_system* s, int cb, const int* gate) {
 cudaError_t enqueue_force(psim_system* s, const Phase& ph, const ForceOut& fo) {
     CellView cv{s->posd.as<double4_32a>(), s->posh.as<float4>(), s->posl.as<float4>(),
                 s->cellid.as<int>(), s->start.as<int>(), s->count[ph.cb].as<int>()};
+    if (s->cfg.force_launch) {   // a plugin's device entry (single systems only)
+        const ForceRunner fr{&s->fs, s->cfg.force_launch, &s->cfg.force};
+        if (s->cfg.precision == PSIM_PRECISION_FP64)
+            return fr.run(PSIM_PASS_FP64, s->g, &cv, nullptr, fo, s->st);
+        if (s->list_on) {
+            PairList pl{nullptr, s->lpos.as<float4>(), s->lcount.as<int>(),
+                        s->list.as<uint32_t>(), s->n, s->lcompact, s->lradius, s->lunit};
+            return fr.run(PSIM_PASS_LIST, s->g, nullptr, &pl, fo, s->st);
+        }
+        return fr.run(PSIM_PASS_MIXED, s->g, &cv, nullptr, fo, s->st);
+    }
     if (s->n_reps && s->list_on) {   // each particle with its replica's pair functor
         PairList pl{nullptr, s->lpos.as<float4>(), s->lcount.as<int>(), s->list.as<uint32_t>(),
                     s->n, s->lcompact, s->lradius, s->lunit, s->b_rep.as<int>(), s->b_pairs.p};
@@ -1683,7 +1722,7 @@ extern "C" {
 
 psim_system* psim_system_create(const psim_system_config* cfg) {
     if (!cfg) { fail(PSIM_ERR_INPUT, "NULL config"); return nullptr; }
-    if (check_params(&cfg->force)) return nullptr;
+    if (check_params(&cfg->force, cfg->force_launch != nullptr)) return nullptr;
     if (cfg->precision != PSIM_PRECISION_FP64 && cfg->precision != PSIM_PRECISION_MIXED) {
         fail(PSIM_ERR_INPUT, "unknown precision %d", cfg->precision);
         return nullptr;
@@ -1953,6 +1992,37 @@ psim_system* system_new(const psim_system_config* cfg, const DevGeom& g, bool ba
         fail(PSIM_ERR_CUDA, "system allocation failed: %s", cudaGetErrorString(cudaGetLastError()));
         psim_system_destroy(s);
         return nullptr;
+    }
+    if (cfg->force_launch) {
+        // One call of the plugin's pass with its error word already set (and
+        // every cell empty): each kernel of the pass launches and returns at
+        // once.  It brings the plugin's own CUDA runtime up and loads its
+        // kernels here, outside the stream capture of the step graphs.
+        DevBuf word;
+        double* f = s->frc[0].as<double>();
+        ForceOut fo{f, f + n, f + 2 * n, nullptr, nullptr};
+        ok = !word.ensure(4) && cudaMemset(word.p, 0xff, 4) == cudaSuccess &&
+             cudaMemset(s->count[0].p, 0, 4 * nc) == cudaSuccess &&
+             cudaMemset(s->start.p, 0, 4 * nc) == cudaSuccess;
+        if (ok) {
+            fo.err = word.as<uint32_t>();
+            const ForceRunner fr{&s->fs, cfg->force_launch, &s->cfg.force};
+            CellView cv{s->posd.as<double4_32a>(), s->posh.as<float4>(), s->posl.as<float4>(),
+                        s->cellid.as<int>(), s->start.as<int>(), s->count[0].as<int>()};
+            PairList pl{nullptr, s->lpos.as<float4>(), s->lcount.as<int>(),
+                        s->list.as<uint32_t>(), s->n, 0, 0.f, 0.f};
+            const int pass = cfg->precision == PSIM_PRECISION_FP64
+                                 ? PSIM_PASS_FP64
+                                 : (list_on ? PSIM_PASS_LIST : PSIM_PASS_MIXED);
+            ok = fr.run(pass, g, &cv, &pl, fo, s->st) == cudaSuccess &&
+                 cudaStreamSynchronize(s->st) == cudaSuccess;
+        }
+        word.release();
+        if (!ok) {
+            fail(PSIM_ERR_CUDA, "the plugin's psim_force_launch failed on a first, empty pass");
+            psim_system_destroy(s);
+            return nullptr;
+        }
     }
     return s;
 }

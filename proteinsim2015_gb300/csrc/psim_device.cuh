@@ -8,6 +8,8 @@
 //   Philox4x32-10 counter-based Gaussians (Salmon et al., SC'11)
 #pragma once
 
+#include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -42,6 +44,35 @@ struct DevGeom {
     // its first global cell and its particle range in every storage order
     int c0, p0, p1;
 };
+
+// The grid of n particles in a box of edge L cut into s cells of edge cs
+// (checked by the caller: s >= 3, s * cs == L).  One system: its cells and
+// particles start at 0.
+inline void fill_geom(int n, int s, double L, double cs, DevGeom* g) {
+    g->n = n;
+    g->s = s;
+    g->s2 = s * s;
+    g->ncell = g->s2 * s;
+    g->L = L;
+    g->half = L / 2.0;
+    const double fl = std::floor(L);
+    g->half_uv = (fl == L && L < 2147483647.0) ? (double)(((int)L) / 2) : L / 2.0;
+    g->cs = cs;
+    g->inv_cs = 1.0 / cs;
+    g->Lhi = (float)L;
+    g->Llo = (float)(L - (double)g->Lhi);
+    g->inv_csf = (float)g->inv_cs;
+    // FP32 hash error: x cut or rounded to FP32 (< ulp(L)) scaled by 1/cs, plus
+    // the roundings of 1/cs and of the product (each ~s 2^-24 cells); 4x that
+    // is the guard
+    const double ex = std::ldexp(1.0, std::ilogb(std::max(L, 1.0)) - 23) * g->inv_cs +
+                      2.0 * s * std::ldexp(1.0, -24);
+    const double guard = 4.0 * ex + 1e-6;
+    g->hash_guard = guard < 0.25 ? (float)guard : 0.5f;  // 0.5: always the FP64 path
+    g->c0 = 0;
+    g->p0 = 0;
+    g->p1 = n;
+}
 
 // floor(x / cs) exactly as the reference computes it (systemHandling.cpp:39-41):
 // a multiply by 1/cs decides unless x/cs lies within 1e-9 of an integer, in
@@ -234,10 +265,12 @@ __device__ __forceinline__ int wrap_cell(int c, int s, int& shift) {
 // fnet64: the plugin's FP64 per-pair magnitude in the reference's operation
 // order, except that integer powers use binary powering and divisions by r2
 // or r multiply by 1/r (a few ulp, far inside the 1e-12 parity tolerance).
+// It is host-callable too: a plugin's CPU getAcceleration (the reference's
+// per-particle entry) evaluates the same functor.
 // fnet32: the same formula in FP32 for the mixed form.
 
 template <typename T>
-__device__ __forceinline__ T powi_binary(T base, int e) {  // utilities.cpp:144-154
+__host__ __device__ __forceinline__ T powi_binary(T base, int e) {  // utilities.cpp:144-154
     T ans = T(1);
     while (e) {
         if (e & 1) ans *= base;
@@ -250,7 +283,7 @@ __device__ __forceinline__ T powi_binary(T base, int e) {  // utilities.cpp:144-
 // powi_binary with the exponent known at compile time: the same products in
 // the same order (multiplying by the initial 1 is exact), fully unrolled.
 template <int N, typename T>
-__device__ __forceinline__ T powi_fixed(T base) {
+__host__ __device__ __forceinline__ T powi_fixed(T base) {
     T ans = T(1);
 #pragma unroll
     for (int e = N; e; e >>= 1) {
@@ -261,7 +294,7 @@ __device__ __forceinline__ T powi_fixed(T base) {
 }
 
 template <typename T>
-__device__ __forceinline__ T pow36(T rinv) {
+__host__ __device__ __forceinline__ T pow36(T rinv) {
     T r2 = rinv * rinv, r4 = r2 * r2, r8 = r4 * r4, r16 = r8 * r8, r32 = r16 * r16;
     return r32 * r4;
 }
@@ -271,7 +304,7 @@ struct AOPair {
     double rc2, c1, c2;
     float rc2f, c1f, c2f;
     static constexpr bool kCheckNan = true;
-    __device__ __forceinline__ double fnet64(double r2, double r, double rinv, double) const {
+    __host__ __device__ __forceinline__ double fnet64(double r2, double r, double rinv, double) const {
         double r36 = pow36(rinv);
         double r38 = r36 * (rinv * rinv);
         double f = 36.0 * r38 + c1 * rinv + c2 * r;
@@ -291,7 +324,7 @@ struct LJPair {
     float rc2f, kTwdf, four_nf, yukf, lambdaf, inv_lambdaf;
     int n;
     static constexpr bool kCheckNan = false;
-    __device__ __forceinline__ double fnet64(double r2, double r, double rinv, double size) const {
+    __host__ __device__ __forceinline__ double fnet64(double r2, double r, double rinv, double size) const {
         double lj = powi_binary(size * rinv, n);
         double attract = (2.0 * lj) - 1.0;
         attract *= (four_n * rinv * lj);
@@ -316,13 +349,56 @@ struct CalPair {
     double rc2;
     float rc2f;
     static constexpr bool kCheckNan = false;
-    __device__ __forceinline__ double fnet64(double, double, double rinv, double) const {
+    __host__ __device__ __forceinline__ double fnet64(double, double, double rinv, double) const {
         return -(36.0 * (pow36(rinv) * rinv));
     }
     __device__ __forceinline__ float fnet32(float, float, float rinv, float) const {
         return -(36.0f * (pow36(rinv) * rinv));
     }
 };
+
+// The functors of the three reference plugins from their settings values,
+// with the FP32 copies the mixed form reads.
+inline void ao_coeffs(double kT, double wd, double rc, double* c1, double* c2) {  // AOPotential.cpp:50-55
+    double q = rc / (rc - 1.0);
+    double a1 = -kT * wd * q * q * q;
+    double a2 = -3.0 / (2.0 * rc);
+    double a3 = 1.0 / (2.0 * rc * rc * rc);
+    *c1 = -a1 * a2;
+    *c2 = -3.0 * a1 * a3;
+}
+inline AOPair make_ao_pair(double kT, double wd, double rc) {
+    AOPair p{};
+    ao_coeffs(kT, wd, rc, &p.c1, &p.c2);
+    p.rc2 = rc * rc;
+    p.rc2f = (float)p.rc2;
+    p.c1f = (float)p.c1;
+    p.c2f = (float)p.c2;
+    return p;
+}
+inline LJPair make_lj_pair(double kT, double wd, int n, double yuk, double lambda, double rc) {
+    LJPair p{};
+    p.rc2 = rc * rc;
+    p.kTwd = kT * wd;
+    p.n = n;
+    p.four_n = 4.0 * n;
+    p.yuk = yuk;
+    p.lambda = lambda;
+    p.inv_lambda = 1.0 / lambda;
+    p.rc2f = (float)p.rc2;
+    p.kTwdf = (float)p.kTwd;
+    p.four_nf = (float)p.four_n;
+    p.yukf = (float)p.yuk;
+    p.lambdaf = (float)p.lambda;
+    p.inv_lambdaf = (float)p.inv_lambda;
+    return p;
+}
+inline CalPair make_cal_pair(double rc) {
+    CalPair p{};
+    p.rc2 = rc * rc;
+    p.rc2f = (float)p.rc2;
+    return p;
+}
 
 // ---------------------------------------------------------------- Philox
 // Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as

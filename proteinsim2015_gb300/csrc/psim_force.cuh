@@ -243,7 +243,7 @@ cudaError_t launch_force_pass(const Body& body, const DevGeom& g, const CellView
 // values 0, 6, 12, 18); LJPair's runtime loop covers the rest.
 template <int N>
 struct LJFixed : LJPair {
-    __device__ __forceinline__ double fnet64(double r2, double r, double rinv, double size) const {
+    __host__ __device__ __forceinline__ double fnet64(double r2, double r, double rinv, double size) const {
         double lj = powi_fixed<N>(size * rinv);
         double attract = (2.0 * lj) - 1.0;
         attract *= (four_n * rinv * lj);

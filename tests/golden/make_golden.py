@@ -6,7 +6,7 @@ rebuilt from its sources by oracle/build_ref.sh (oracle/_ref), on seeded
 inputs.  Inputs are stored next to the outputs so the fixtures stand alone
 (the GPU machine has no reference tree).
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [--settings-only]
 """
 import os
 import sys
@@ -26,10 +26,48 @@ def state_small(n, box, seed):
     return pos.reshape(-1), np.full(n, 0.5)
 
 
+# settings.cfg texts whose run constants the reference derives
+# (system::setSystemConstants): its own ClusteredUI/settings.cfg, read from the
+# reference tree, and synthetic ones around the integer-box quantisation
+SETTINGS_CASES = {
+    "c0_scale7": "nParticles = 4000\nconc = 0.2\nscale = 7\nradius = 0.5\n",
+    "c0_scale4": "nParticles = 4000\nconc = 0.2\nscale = 4\n",
+    "c0_scale3": "nParticles = 4000\nconc = 0.2\nscale = 3\nradius = 0.5\nmass = 2\n",
+    "big_radius": "nParticles = 1000\nconc = 0.1\nscale = 5\nradius = 0.75\n",
+    "defaults": "force = AOPotential\n",
+}
+
+
+def settings_fixtures():
+    """reference_settings.npz: settings texts and the (nParticles, boxSize,
+    cellSize, cellScale) and concentration the reference derives from each."""
+    out = {}
+    cases = dict(SETTINGS_CASES)
+    with open(os.path.join(ref.REFERENCE, "ClusteredUI", "settings.cfg")) as fh:
+        cases["reference_settings_cfg"] = fh.read()
+    for key, text in cases.items():
+        path = ref.write_settings({})
+        with open(path, "w") as fh:
+            fh.write(text)
+        try:
+            n, box, cell, scale, conc = ref.system_constants(path)
+        finally:
+            os.unlink(path)
+        out["text_" + key] = np.array(text)
+        out["ints_" + key] = np.array([n, box, cell, scale], np.int64)
+        out["conc_" + key] = np.array(conc)
+    path = os.path.join(HERE, "reference_settings.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path, os.path.getsize(path), "bytes")
+
+
 def main():
     if not ref.available():
         if not ref.build():
             sys.exit("reference sources not found; cannot generate golden fixtures")
+    settings_fixtures()
+    if "--settings-only" in sys.argv:
+        return
     out = {}
     # ---- case A: AO-type state, L=12, cellSize 3, scale 4 (N=300)
     n, box, cs, scale = 300, 12, 3, 4

@@ -31,7 +31,7 @@ def test_library_exports_every_declared_symbol(psim):
 
 
 def test_abi_version_and_no_device_is_reported(psim):
-    assert psim.lib().psim_abi_version() == 2
+    assert psim.lib().psim_abi_version() == 3
     if psim.device_count() == 0:
         g = psim.geometry(4, 12, 3, 4)
         with pytest.raises(psim.PsimError) as e:
@@ -85,7 +85,8 @@ def test_ao_coefficients_match_oracle(psim, oracle_port):
 
 def test_cpp_header_and_plugin_loader(tmp_path, psim):
     # A C++ host program that loads a plugin the reference's way
-    # (dlopen "./<force>.so", dlsym getForce) and reads its device parameters.
+    # (dlopen "./<force>.so", dlsym getForce) and reads the parameters of its
+    # device entry.
     src = tmp_path / "host.cpp"
     src.write_text(r'''
 #include "psim_gb300.hpp"
@@ -93,7 +94,7 @@ def test_cpp_header_and_plugin_loader(tmp_path, psim):
 int main(int argc, char** argv) {
     PSim::config cfg = PSim::config::fromText("force = LennardJones\nljNum = 6\nwellDepth = 2\n");
     PSim::IForce* f = PSim::loadForces(&cfg, argv[1]);
-    psim_force_params p = f->deviceParams();
+    psim_force_params p = PSim::requireDevice(f).params;
     std::printf("%s %d %d %.3f\n", f->getName().c_str(), p.kind, p.lj_num, p.well_depth);
     try { PSim::config bad = PSim::config::fromText("force = Nope\n"); PSim::loadForces(&bad, argv[1]); }
     catch (const std::exception& e) { std::printf("caught\n"); }
