@@ -49,6 +49,8 @@ BYTES_PER_PARTICLE_STEP = 292
 # Verlet pair-list skin of the mixed form; the cell grid is the finest with
 # cellSize >= rc + skin, so the list can be built from the 27-cell walk
 SKIN = 0.4
+# untimed steps run under the clock sampler before the timed ones (~1.5 s)
+CLOCK_WINDOW_STEPS = 6000
 
 
 def workload(cells=64):
@@ -71,7 +73,7 @@ def dist_env():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons sampled every 100 ms."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -85,7 +87,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -270,10 +272,11 @@ def pinned(n, dtype=None):
     return torch.empty(n, dtype=dtype or torch.float64, pin_memory=True).numpy()
 
 
-def e2e_dropin(psim, w, state, n_steps):
+def e2e_dropin(psim, w, state, min_steps=30, min_seconds=1.0):
     """The reference's step loop on host arrays with the GPU drop-ins:
-    force_evaluate -> nextSystem (with push) -> cells_build.  Returns
-    (particle-steps/s, h2d bytes/step, d2h bytes/step)."""
+    force_evaluate -> nextSystem (with push) -> cells_build, for at least
+    min_steps steps and min_seconds.  Returns (particle-steps/s, h2d
+    bytes/step, d2h bytes/step, pair-list calls and builds, steps)."""
     n, box, scale = w["n"], w["box"], w["scale"]
     g = psim.geometry(n, box, box / scale, scale)
     p = psim.make_force("LJ", RC, kT=KT, well_depth=WD, lj_num=LJN, yukawa_strength=0.0)
@@ -294,13 +297,15 @@ def e2e_dropin(psim, w, state, n_steps):
     hi, cse, srt = psim.cells_build(g, buf["pos"], rad, out=cells)
     t_cur = DT  # continue as a normal step
     calls0, builds0 = psim.force_list_stats()
+    n_steps = 0
     t0 = time.perf_counter()
-    for _ in range(n_steps):
+    while n_steps < min_steps or time.perf_counter() - t0 < min_seconds:
         psim.force_evaluate(p, g, srt, hi, cse, precision=psim.PRECISION_MIXED, out=f)
         it.next_system(t_cur, box, buf["pos"], buf["pos0"], buf["vel"], buf["frc"], buf["frc0"],
                        mass, particle_force=f)
         psim.cells_build(g, buf["pos"], rad, out=cells)
         t_cur += DT
+        n_steps += 1
     el = time.perf_counter() - t0
     calls1, builds1 = psim.force_list_stats()
     # per step: force_evaluate (sorted, hash index, cell ranges in; force out),
@@ -312,7 +317,52 @@ def e2e_dropin(psim, w, state, n_steps):
     d2h = 24 * n + 4 * 24 * n + (8 * n + 8 * ncell + 32 * n)
     it.close()
     lists = {"calls": calls1 - calls0, "builds": builds1 - builds0}
-    return n * n_steps / el, h2d, d2h, lists
+    return n * n_steps / el, h2d, d2h, lists, n_steps
+
+
+def mixed_vs_fp64(psim, g, p, w, state, seed, dev, steps=200, every=20):
+    """The mixed form's error against the plain FP64 form in the quantities a
+    run reports: from the same melted state and the same Philox noise, both
+    forms step `steps` steps (velocities every step); every `every` steps the
+    FP64 potential energy and virial per particle (psim_system_energy), the
+    kinetic temperature (getTemperature) and g(r) (100 bins on [0.8, 2.9))
+    are taken.  Reported: the relative differences of the run means and of
+    the final values, and the largest relative g(r) bin difference."""
+    runs = []
+    for prec, skin in ((psim.PRECISION_MIXED, SKIN), (psim.PRECISION_FP64, 0.0)):
+        s = psim.System(g, p, gamma=GAMMA, dt=DT, kT=KT, vel_freq=0, seed=seed + 1,
+                        precision=prec, device=dev, skin=skin)
+        s.upload(state["pos"], w["radius"], vel=state["vel"], pos0=state["pos0"],
+                 frc=state["frc"], frc0=state["frc0"])
+        u, vir, T, gr = [], [], [], []
+        for _ in range(steps // every):
+            s.step(every)
+            e = s.energy()
+            u.append(e[0])
+            vir.append(e[1])
+            T.append(s.temperature())
+            gr.append(s.rdf(0.8, 2.9, 100))
+        s.close()
+        runs.append((np.array(u), np.array(vir), np.array(T), np.array(gr)))
+    (um, wm, tm, gm), (u6, w6, t6, g6) = runs
+    rel = lambda a, b: float(abs(a - b) / abs(b))
+    gmean_m, gmean_6 = gm.mean(0), g6.mean(0)
+    return {"steps": steps, "samples": steps // every, "n_particles": g.n_particles,
+            "energy_per_particle": {"mixed": float(um.mean()), "fp64": float(u6.mean()),
+                                    "rel_diff_mean": rel(um.mean(), u6.mean()),
+                                    "rel_diff_final": rel(um[-1], u6[-1])},
+            "virial_per_particle": {"mixed": float(wm.mean()), "fp64": float(w6.mean()),
+                                    "rel_diff_mean": rel(wm.mean(), w6.mean()),
+                                    "rel_diff_final": rel(wm[-1], w6[-1])},
+            "temperature": {"mixed": float(tm.mean()), "fp64": float(t6.mean()),
+                            "rel_diff_mean": rel(tm.mean(), t6.mean()),
+                            "rel_diff_final": rel(tm[-1], t6[-1])},
+            "gr": {"rel_l2_mean": float(np.linalg.norm(gmean_m - gmean_6) / np.linalg.norm(gmean_6)),
+                   "max_bin_rel_diff_mean": float(np.max(np.abs(gmean_m - gmean_6) /
+                                                         np.maximum(gmean_6, 1e-3))),
+                   "bins": 100, "range": [0.8, 2.9]},
+            "note": "same start and Philox noise; energy and virial are FP64 reductions "
+                    "(pair energy u(r) integrated from the plugin's force law)"}
 
 
 def run_batched(psim, dev, steps=2000, n_reps=512, tune=True, skin=0.3):
@@ -393,17 +443,21 @@ def run_differentiable(psim, dev, steps=2000):
             "note": "q through the AO coefficients; the cutoff 1 + q is held fixed"}
 
 
-def run_gel(psim, dev, steps=1000, skin=0.3, chunk=100):
+def run_gel(psim, dev, steps=1000, skin=0.0, chunk=100):
     """The gel stress workload: N = 2^23 AO colloids at phi = 0.30 (q = 0.08,
     6 kT contact attraction, cutoff 1.08), seeded RSA start, gamma = 1,
-    dt = 1e-3, mixed form with a pair list; the cell list is rebuilt every
-    step.  Reports the maximum and mean particles per cell every `chunk`
-    steps while the colloids aggregate, and the clusters at the end."""
+    dt = 1e-3, mixed form.  skin 0: the cell list is rebuilt every step and
+    the force pass walks the 27 cells (the workload as stated); skin > 0: a
+    pair list rebuilt when a particle has moved skin/2.  Reports the maximum
+    and mean particles per cell every `chunk` steps while the colloids
+    aggregate, the clusters and the kinetic temperature at the end."""
     from proteinsim2015_gb300 import init, batch
     n, phi = 1 << 23, 0.30
     box = (n * math.pi / 6.0 / phi) ** (1.0 / 3.0)
     f = batch.ao_params(psim, 6.0, 0.08)
-    scale = int(math.floor(box / (f.cutoff + skin)))
+    # cells of at least cutOff + skin and of the 1.2 contact distance the
+    # cluster analysis walks (updateInteractions' radius)
+    scale = int(math.floor(box / max(f.cutoff + skin, 1.2)))
     g = psim.geometry(n, box, box / scale, scale)
     t0 = time.time()
     pos = init.rsa_native(n, box, 1.0, seed=2023).reshape(-1)
@@ -428,7 +482,11 @@ def run_gel(psim, dev, steps=1000, skin=0.3, chunk=100):
            "occupancy_max": [m for m, _ in occ], "occupancy_mean": occ[0][1],
            "occupancy_every_steps": chunk, "rsa_seconds": round(t_init, 2),
            "clusters_gt4": len(groups), "mean_cluster_size": avg,
-           "temperature": s.temperature()}
+           "temperature": s.temperature(),
+           "temperature_note": "above kT while the colloids aggregate: the energy released "
+                               "into the 6 kT wells outpaces the gamma = 1 friction; the "
+                               "oracle reads the same at every dt tried, and a repulsive "
+                               "control stays at kT"}
     s.close()
     return out
 
@@ -501,10 +559,14 @@ def run_gpu(args):
     s.step(max(args.warmup, 3))          # W >= 3 untimed warm-up steps (melting the lattice)
     if dist:
         dist.barrier()
-    builds0 = s.list_builds()
+    # clocks are sampled every 100 ms over ~1.5 s of untimed steps of the same
+    # workload and then over the timed steps, so the record covers the load
+    # the timed steps run under
     with ClockSampler(dev) as clk:
+        s.time_steps(CLOCK_WINDOW_STEPS)
+        builds0 = s.list_builds()
         ms = s.time_steps(args.steps)
-    builds_timed = s.list_builds() - builds0
+        builds_timed = s.list_builds() - builds0
     if dist:
         import torch
         t = torch.tensor([ms], dtype=torch.float64)
@@ -536,6 +598,22 @@ def run_gpu(args):
     ms64 = s64.time_steps(k64)
     prof64 = s64.profile(3)
     plain = n * k64 / (ms64 * 1e-3)
+    # ---- the mixed form without a pair list (the 27-cell walk, the cell
+    # list rebuilt every step) on the same state and grid: the precision gain
+    # apart from the Verlet-list gain
+    s0 = psim.System(g, p, gamma=GAMMA, dt=DT, kT=KT, vel_freq=1000, seed=seed,
+                     precision=psim.PRECISION_MIXED, device=dev, skin=0.0)
+    s0.upload(state["pos"], w["radius"], vel=state["vel"], pos0=state["pos0"],
+              frc=state["frc"], frc0=state["frc0"])
+    s0.step(3)
+    k0 = max(10, min(args.steps, 200))
+    ms0 = s0.time_steps(k0)
+    prof0 = s0.profile(3)
+    s0.close()
+    mixed_skin0 = {"value": n * k0 / (ms0 * 1e-3), "unit": UNIT, "steps": k0,
+                   "ms_per_step": ms0 / k0, "force_ms": prof0["force_ms"], "skin": 0.0,
+                   "speedup_vs_fp64": (n * k0 / (ms0 * 1e-3)) / plain}
+    precision_errors = mixed_vs_fp64(psim, g, p, w, state, seed, dev)
     # ---- force error of the mixed form (the pair-list pass the timed steps
     # ran) against the plain FP64 pass, on the melted state
     hi, cse, srt = s.download_cells()
@@ -546,8 +624,7 @@ def run_gpu(args):
     fmax = float(np.max(np.abs(f32 - f64).reshape(-1, 3).max(1)) / rms)
     s64.close()
     # ---- end to end through the reference-layout drop-ins on pinned host buffers
-    e2e_steps = max(3, min(args.steps // 50, 30))
-    e2e_v, h2d, d2h, e2e_lists = e2e_dropin(psim, w, state, e2e_steps)
+    e2e_v, h2d, d2h, e2e_lists, e2e_steps = e2e_dropin(psim, w, state)
     # the host link the drop-ins' traffic crosses: its measured rates
     link = psim.measure_host_link(dev)
     e2e_ms = n / e2e_v * 1e3
@@ -566,7 +643,13 @@ def run_gpu(args):
         batched = run_batched(psim, dev, args.batched_steps)
         batched["vs_single_system"] = batched["value"] / value
     differentiable = run_differentiable(psim, dev) if args.batched_steps > 0 and ws == 1 else None
-    gel = run_gel(psim, dev, args.gel_steps) if args.gel_steps > 0 and ws == 1 else None
+    gel = None
+    if args.gel_steps > 0 and ws == 1:
+        gel = run_gel(psim, dev, args.gel_steps, skin=0.0)
+        gl = run_gel(psim, dev, args.gel_steps, skin=0.3)
+        gel["pair_list"] = {k: gl[k] for k in ("skin", "value", "ms_per_step", "phases_ms",
+                                               "list_builds", "cell_scale", "temperature",
+                                               "clusters_gt4")}
     c0 = run_c0(psim, dev) if args.gel_steps > 0 and ws == 1 else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -577,10 +660,13 @@ def run_gpu(args):
                    "cell_scale": scale, "cell_size": box / scale, "potential": "LJ 12-6 rc=2.5",
                    "kT": KT, "gamma": GAMMA, "dt": DT, "precision": "mixed",
                    "noise": "philox", "parallelism": "replicas" if ws > 1 else "single",
+                   "skin": args.skin, "pair_list": args.skin > 0,
                    "l2": "inputs larger than L2 (FP64 SoA state ~300 MB, sorted copies 32 MB)"},
         "plain_fp64": {"value": plain, "unit": UNIT, "steps": k64, "ms_per_step": ms64 / k64,
                        "force_ms": prof64["force_ms"]},
         "speedup_vs_fp64": value / plain,
+        "mixed_skin0": mixed_skin0,
+        "precision_errors": precision_errors,
         "force_rel_err": ferr, "force_abs_err_max_over_rms_force": fmax,
         "phases_ms": {k: round(v, 5) for k, v in prof.items()},
         "pairs_per_particle": pairs,

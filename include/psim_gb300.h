@@ -513,6 +513,16 @@ int psim_system_clusters(psim_system* sys, double r_contact, int32_t min_size, i
  * N rho 4/3 pi (r1^3 - r0^3).  r_max <= cellSize.  Single systems only. */
 int psim_system_rdf(psim_system* sys, double r_min, double r_max, int32_t n_bins, double* g);
 
+/* Potential energy and virial of the current state, in FP64 whatever the
+ * system's precision (no reference counterpart: the reference reports only
+ * its work estimate <EAP>).  The pair energy u(r) is the integral of the
+ * plugin's force law fNet (AOPotential.cpp:90-99, LJPotential.cpp:96-109,
+ * Calibration.cpp:75-81: u' = fNet) shifted to zero at the cutoff;
+ * potential = sum over pairs of u(r_ij) / N, virial = sum over pairs of
+ * r_ij . f_ij / N (pressure = rho (kT + virial / 3)).  Single systems with a
+ * library functor only (a plugin's energy is not known here). */
+int psim_system_energy(psim_system* sys, double* potential, double* virial);
+
 /* Pair-list rebuilds since the upload (0 without a skin; the list the upload
  * builds is not counted). */
 int psim_system_list_builds(psim_system* sys, int32_t* builds);

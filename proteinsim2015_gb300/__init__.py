@@ -153,6 +153,7 @@ def lib():
             "psim_system_track_start": ([P], C.c_int),
             "psim_system_tracked_displacement": ([P, C.POINTER(C.c_double)], C.c_int),
             "psim_system_interactions": ([P, C.c_double, P, C.POINTER(C.c_int64)], C.c_int),
+            "psim_system_energy": ([P, C.POINTER(C.c_double), C.POINTER(C.c_double)], C.c_int),
             "psim_system_rdf": ([P, C.c_double, C.c_double, C.c_int32, P], C.c_int),
             "psim_system_clusters": ([P, C.c_double, C.c_int32, P, C.POINTER(C.c_int32),
                                       C.POINTER(C.c_int32)], C.c_int),
@@ -611,6 +612,14 @@ class System:
         g = np.empty(int(n_bins))
         _check(lib().psim_system_rdf(self._h, r_min, r_max, int(n_bins), _p(g)))
         return g
+
+    def energy(self):
+        """(potential energy per particle, virial per particle) of the current
+        state in FP64: u(r) is the integral of the plugin's force law, zero at
+        the cutoff; the virial is sum r_ij . f_ij / N."""
+        u, w = C.c_double(), C.c_double()
+        _check(lib().psim_system_energy(self._h, C.byref(u), C.byref(w)))
+        return u.value, w.value
 
     def list_builds(self):
         b = C.c_int32()

@@ -2634,6 +2634,28 @@ int psim_system_rdf(psim_system* s, double r_min, double r_max, int32_t n_bins, 
     return PSIM_OK;
 }
 
+int psim_system_energy(psim_system* s, double* potential, double* virial) {
+    if (!s || !s->uploaded) return fail(PSIM_ERR_INPUT, "NULL system or no state");
+    if (s->n_reps) return fail(PSIM_ERR_INPUT, "energy: single systems only");
+    if (s->cfg.force_launch || s->cfg.force.kind == PSIM_FORCE_PLUGIN)
+        return fail(PSIM_ERR_INPUT, "energy: the plugin's pair energy is not known to the library");
+    DeviceGuard dg(s->device);
+    int rc = settle(s);
+    if (rc) return rc;
+    PairScanArgs a{};
+    ScopedBuf pd, scratch, res;
+    if ((rc = sorted_view(s, pd, a))) return rc;
+    PSIM_CUDA(scratch.ensure(16 * (size_t)((s->n + 127) / 128 + 1)));
+    PSIM_CUDA(res.ensure(16));
+    PSIM_CUDA(launch_energy(s->fs, a, scratch.as<double>(), res.as<double>(), s->st));
+    double out[2] = {0.0, 0.0};
+    PSIM_CUDA(cudaMemcpyAsync(out, res.p, 16, cudaMemcpyDeviceToHost, s->st));
+    PSIM_CUDA(cudaStreamSynchronize(s->st));
+    if (potential) *potential = s->n ? out[0] / s->n : 0.0;
+    if (virial) *virial = s->n ? out[1] / s->n : 0.0;
+    return PSIM_OK;
+}
+
 int psim_system_list_builds(psim_system* s, int32_t* builds) {
     if (!s || !builds) return fail(PSIM_ERR_INPUT, "NULL argument");
     DeviceGuard dg(s->device);

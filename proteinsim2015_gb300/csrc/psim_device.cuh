@@ -315,6 +315,13 @@ struct AOPair {
         float r38 = r36 * (rinv * rinv);
         return -(36.0f * r38 + c1f * rinv + c2f * r);
     }
+    // the pair energy whose derivative is fnet64 (u' = fNet), zero at the
+    // cutoff: 36/37 (r^-37 - rc^-37) + coEff1 ln(rc/r) + coEff2 (rc^2 - r^2)/2
+    __host__ __device__ __forceinline__ double u64(double r2, double, double rinv, double) const {
+        const double rc = sqrt(rc2), rcinv = 1.0 / rc;
+        return (36.0 / 37.0) * (pow36(rinv) * rinv - pow36(rcinv) * rcinv) + c1 * log(rc * rinv) +
+               0.5 * c2 * (rc2 - r2);
+    }
 };
 
 // LennardJones: fNet = -kT wd [(2L-1) 4n L / r + yukStr e^{-r/lambda} (lambda + r)/r^2],
@@ -342,6 +349,16 @@ struct LJPair {
         if (yukf != 0.0f) repel = __expf(-r * inv_lambdaf) * (rinv * rinv * (lambdaf + r) * yukf);
         return -kTwdf * (attract + repel);
     }
+    // the pair energy whose derivative is fnet64, zero at the cutoff:
+    // kT wd [4 (L^2 - L) + yukStr lambda e^{-r/lambda} / r] - (the same at rc)
+    __host__ __device__ __forceinline__ double u64(double, double r, double rinv, double size) const {
+        const double rc = sqrt(rc2);
+        const double L = powi_binary(size * rinv, n), Lc = powi_binary(size / rc, n);
+        double u = 4.0 * ((L * L - L) - (Lc * Lc - Lc));
+        if (yuk != 0.0)
+            u += yuk * lambda * (exp(-r * inv_lambda) * rinv - exp(-rc * inv_lambda) / rc);
+        return kTwd * u;
+    }
 };
 
 // Calibration: fNet = -36 r^-37                           (Calibration.cpp:75-81)
@@ -354,6 +371,10 @@ struct CalPair {
     }
     __device__ __forceinline__ float fnet32(float, float, float rinv, float) const {
         return -(36.0f * (pow36(rinv) * rinv));
+    }
+    // the pair energy whose derivative is fnet64, zero at the cutoff: r^-36 - rc^-36
+    __host__ __device__ __forceinline__ double u64(double, double, double rinv, double) const {
+        return pow36(rinv) - pow36(1.0 / sqrt(rc2));
     }
 };
 

@@ -435,6 +435,12 @@ struct PairScanArgs {
     unsigned long long* hist;
 };
 cudaError_t launch_pair_scan(const PairScanArgs& a, cudaStream_t st);
+// FP64 potential energy and virial of the plugin's pair force over the 27-cell
+// walk of a: out[0] = sum over pairs of u(r), out[1] = sum over pairs of
+// r_ij . f_ij (f_ij the force on i from j).  scratch: 2 * ceil(n / 128) doubles.
+// cudaErrorInvalidValue for a force kind without an energy.
+cudaError_t launch_energy(const ForceSetup& fs, const PairScanArgs& a, double* scratch,
+                          double* out, cudaStream_t st);
 // Clusters of the contact graph (r < a.r_contact): root[original index] = the
 // smallest original index of its cluster, size[root] = cluster size (zeroed
 // by the caller); label: union-find scratch (n ints).

@@ -7,6 +7,7 @@
 //   potential ("EAP")    particle::calculatePotential (particle.cpp:133-149), summed
 //   coordination         system::updateInteractions (systemHandling.cpp:94-161)
 //   g(r)                 a pair-distance histogram over the same 27-cell walk
+//   energy and virial    FP64 sums over pairs of the plugin's u(r) and r.f
 //
 // Sums are deterministic: each block writes its partial, one block adds the
 // partials in block order.
@@ -223,7 +224,109 @@ __global__ void __launch_bounds__(256) uf_final_kernel(int n, const int* label, 
     if (err) atomicOr(err_out, err);
 }
 
+// ------------------------------------------------------ energy and virial
+// One pair term of the energy walk: u(r) and fNet(r) inside the cutoff.
+template <class Pair>
+struct OneTerm {
+    Pair p;
+    __device__ double rc2() const { return p.rc2; }
+    __device__ void eval(double r2, double r, double rinv, double size, double& u,
+                         double& f) const {
+        if (r2 < p.rc2) {
+            u += p.u64(r2, r, rinv, size);
+            f += p.fnet64(r2, r, rinv, size);
+        }
+    }
+};
+struct ComboTerms {  // the AO + LJ(n) composite: each part inside its own cutoff
+    AOPair ao;
+    LJPair lj;
+    __device__ double rc2() const { return ao.rc2 > lj.rc2 ? ao.rc2 : lj.rc2; }
+    __device__ void eval(double r2, double r, double rinv, double size, double& u,
+                         double& f) const {
+        if (r2 < ao.rc2) {
+            u += ao.u64(r2, r, rinv, size);
+            f += ao.fnet64(r2, r, rinv, size);
+        }
+        if (r2 < lj.rc2) {
+            u += lj.u64(r2, r, rinv, size);
+            f += lj.fnet64(r2, r, rinv, size);
+        }
+    }
+};
+
+// Per particle i: half the sum over its neighbours j of u(r_ij) and of
+// r_ij . f_ij = -fNet(r_ij) r_ij (pbcDist's minimum image), in FP64; block
+// partials of both, added in block order by finish_kernel.
+template <class Terms>
+__global__ void __launch_bounds__(128) energy_kernel(PairScanArgs a, Terms t, double* part,
+                                                     int stride) {
+    __shared__ double sh[4];
+    double eu = 0.0, ew = 0.0;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < a.g.n) {
+        const double4_32a pi = a.posd[i];
+        const int c = a.cellid[i];
+        const int cx = c % a.g.s, cy = (c / a.g.s) % a.g.s, cz = c / a.g.s2;
+        const double rc2 = t.rc2();
+        for (int dx = -1; dx <= 1; ++dx)
+            for (int dy = -1; dy <= 1; ++dy)
+                for (int dz = -1; dz <= 1; ++dz) {
+                    int sh_;
+                    const int x = wrap_cell(cx + dx, a.g.s, sh_);
+                    const int y = wrap_cell(cy + dy, a.g.s, sh_);
+                    const int z = wrap_cell(cz + dz, a.g.s, sh_);
+                    const int cell = x + a.g.s * y + a.g.s2 * z;
+                    const int st = a.cstart[cell], en = st + a.ccount[cell];
+                    for (int j = st; j < en; ++j) {
+                        if (j == i) continue;
+                        const double4_32a pj = a.posd[j];
+                        double d0 = fabs(pj.x - pi.x), d1 = fabs(pj.y - pi.y),
+                               d2 = fabs(pj.z - pi.z);
+                        if (d0 > a.g.half) d0 -= a.g.L;
+                        if (d1 > a.g.half) d1 -= a.g.L;
+                        if (d2 > a.g.half) d2 -= a.g.L;
+                        const double r2 = d0 * d0 + d1 * d1 + d2 * d2;
+                        if (!(r2 < rc2)) continue;
+                        const double r = sqrt(r2), rinv = 1.0 / r;
+                        double u = 0.0, f = 0.0;
+                        t.eval(r2, r, rinv, pi.w + pj.w, u, f);
+                        eu += u;
+                        ew -= f * r;
+                    }
+                }
+    }
+    const double su = block_sum(0.5 * eu, sh);
+    const double sw = block_sum(0.5 * ew, sh);
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = su;
+        part[stride + blockIdx.x] = sw;
+    }
+}
+
+template <class Terms>
+cudaError_t run_energy(const Terms& t, const PairScanArgs& a, double* scratch, double* out,
+                       cudaStream_t st) {
+    const int blocks = (a.g.n + 127) / 128;
+    energy_kernel<Terms><<<blocks, 128, 0, st>>>(a, t, scratch, blocks);
+    finish_kernel<<<1, kRedThreads, 0, st>>>(scratch, blocks, out);
+    finish_kernel<<<1, kRedThreads, 0, st>>>(scratch + blocks, blocks, out + 1);
+    return cudaGetLastError();
+}
+
 }  // namespace
+
+cudaError_t launch_energy(const ForceSetup& fs, const PairScanArgs& a, double* scratch,
+                          double* out, cudaStream_t st) {
+    if (a.g.n == 0) return cudaMemsetAsync(out, 0, 2 * sizeof(double), st);
+    switch (fs.kind) {
+    case 1: return run_energy(OneTerm<AOPair>{fs.ao}, a, scratch, out, st);
+    case 2: return run_energy(OneTerm<LJPair>{fs.lj}, a, scratch, out, st);
+    case 3: return run_energy(OneTerm<CalPair>{fs.cal}, a, scratch, out, st);
+    case 4: return run_energy(ComboTerms{fs.ao, fs.lj}, a, scratch, out, st);
+    }
+    return cudaErrorInvalidValue;
+}
 
 cudaError_t launch_clusters(const PairScanArgs& a, int* label, int* root, int* size,
                             uint32_t* err, cudaStream_t st) {

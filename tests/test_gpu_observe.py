@@ -111,3 +111,92 @@ def test_clusters_match_connected_components(psim):
     assert len(groups) == len(big) and all(np.array_equal(a, b) for a, b in zip(groups, big))
     assert avg == (sum(len(m) for m in big) // len(big) if big else 0)
     s.close()
+
+
+# ------------------------------------------------------------ energy, virial
+
+def _pair_u_f(kind, p, r, size):
+    """u(r) (zero at the cutoff) and fNet(r) of the plugin force laws
+    (AOPotential.cpp:90-99, LJPotential.cpp:96-109, Calibration.cpp:75-81)."""
+    rc = p["cutoff"]
+    if kind == "AO":
+        from oracle import port
+        c1, c2 = port.ao_coeffs(p["kT"], p["well_depth"], rc)
+        u = 36 / 37 * (r ** -37 - rc ** -37) + c1 * np.log(rc / r) + 0.5 * c2 * (rc * rc - r * r)
+        f = -(36 * r ** -38 + c1 / r + c2 * r)
+    elif kind == "LJ":
+        n, e, lam, y = p["lj_num"], p["kT"] * p["well_depth"], p["debye_length"], p["yukawa_strength"]
+        L, Lc = (size / r) ** n, (size / rc) ** n
+        u = e * (4 * (L * L - L) - 4 * (Lc * Lc - Lc)
+                 + y * lam * (np.exp(-r / lam) / r - np.exp(-rc / lam) / rc))
+        f = -e * ((2 * L - 1) * 4 * n * L / r + y * np.exp(-r / lam) * (lam + r) / r ** 2)
+    else:
+        u = r ** -36 - rc ** -36
+        f = -36 * r ** -37
+    return u, f
+
+
+ENERGY_CASES = {
+    "AO": (dict(kind="AO", cutoff=1.1, kT=1.0, well_depth=0.25), 12.0, 4),
+    "LJ6": (dict(kind="LJ", cutoff=2.5, kT=1.5, well_depth=1 / 1.5, lj_num=6,
+                 yukawa_strength=0.0, debye_length=0.5), 15.0, 6),
+    "LJ18Y": (dict(kind="LJ", cutoff=2.5, kT=1.0, well_depth=3.0, lj_num=18,
+                   yukawa_strength=8.0, debye_length=0.5), 15.0, 6),
+    "CAL": (dict(kind="CAL", cutoff=1.1, kT=1.0), 12.0, 4),
+}
+
+
+def _energy_system(psim, case, n, seed, precision=0):
+    p, box, scale = ENERGY_CASES[case]
+    args = {k: v for k, v in p.items() if k != "kind"}
+    force = psim.make_force(p["kind"], **args)
+    pos, rad = rsa_state(n, box, seed=seed)
+    g = psim.geometry(n, box, box / scale, scale)
+    s = psim.System(g, force, precision=precision)
+    s.upload(pos, rad)
+    return s, g, pos, rad, force
+
+
+@pytest.mark.parametrize("case", list(ENERGY_CASES))
+def test_energy_and_virial_match_pair_sums(psim, case):
+    n = 700
+    s, g, pos, rad, force = _energy_system(psim, case, n, seed=31)
+    u, w = s.energy()
+    p = ENERGY_CASES[case][0]
+    x = pos.reshape(-1, 3)
+    i, j = np.triu_indices(n, 1)
+    d = min_image(x[j] - x[i], g.box_size)
+    r = np.sqrt(np.sum(d * d, axis=1))
+    m = r < p["cutoff"]
+    uu, ff = _pair_u_f(p["kind"], p, r[m], rad[i][m] + rad[j][m])
+    assert u == pytest.approx(np.sum(uu) / n, rel=1e-12, abs=1e-14)
+    assert w == pytest.approx(np.sum(-ff * r[m]) / n, rel=1e-12, abs=1e-14)
+    s.close()
+
+
+@pytest.mark.parametrize("case", ["AO", "LJ18Y"])
+def test_energy_gradient_is_the_reference_force(psim, oracle_port, case):
+    # u(r) is pinned to the reference's force law: -dU/dx_i (central
+    # differences of the GPU energy) equals the oracle's force on i
+    n = 500
+    s, g, pos, rad, force = _energy_system(psim, case, n, seed=32)
+    og = oracle_port.geom(n, g.box_size, g.cell_size, g.cell_scale)
+    hi, cse, srt = oracle_port.build_cells(og, pos, rad)
+    F, err = oracle_port.forces(og, oracle_port.force_from_params(force.as_dict()), srt, hi, cse)
+    assert err == 0
+    h = 1e-6
+    worst = 0.0
+    for i in (0, 17, 123, 499):
+        for k in range(3):
+            e = np.zeros_like(pos)
+            e[3 * i + k] = h
+            s.upload(pos + e, rad)
+            up = s.energy()[0] * n
+            s.upload(pos - e, rad)
+            dn = s.energy()[0] * n
+            fd = -(up - dn) / (2 * h)
+            worst = max(worst, abs(fd - F[3 * i + k]) / max(1.0, abs(F[3 * i + k])))
+    # central differences at h = 1e-6: truncation ~h^2 F''' and rounding of
+    # the energy sum, both well under 1e-4 of the force here
+    assert worst < 1e-4
+    s.close()
