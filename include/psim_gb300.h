@@ -496,7 +496,10 @@ int psim_system_tracked_displacement(psim_system* sys, double* msd);
 /* system::updateInteractions (systemHandling.cpp:94-161): per particle, the
  * neighbours of its 27 cells closer than r_contact (the reference uses 1.2);
  * coor: n ints in original order (may be NULL), total: their sum (may be NULL).
- * r_contact <= cellSize.  Single systems only. */
+ * r_contact <= cellSize.  Single systems only.  Counted inside one force pass
+ * on the current state (the FP64 form with the reference's own test; the
+ * mixed form in FP32, through its pair list when r_contact <= cutOff), else
+ * by a separate 27-cell walk. */
 int psim_system_interactions(psim_system* sys, double r_contact, int32_t* coor, int64_t* total);
 /* analysisManager::findClusters / writeClusters (analysisCluster.cpp:26-78):
  * the connected components of the contact graph (pairs closer than r_contact,

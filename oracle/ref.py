@@ -48,6 +48,8 @@ def lib():
                                      + [C.c_int])
         _lib.psimref_foreign_forces.argtypes = ([C.c_char_p, C.c_char_p] + [C.c_int] * 4 +
                                                 [P] * 4 + [C.c_int])
+        _lib.psimref_analysis.argtypes = [C.c_int] * 4 + [P] * 7 + [C.c_double] + [P] * 4 + [
+            C.c_char_p]
         _lib.psimref_system_constants.argtypes = [C.c_char_p] + [C.POINTER(C.c_int)] * 4 + [
             C.POINTER(C.c_double)]
     return _lib
@@ -79,6 +81,24 @@ def foreign_forces(plugin_path, settings, n, box, cell_size, scale, sorted_, hi,
         return out, rc
     finally:
         os.unlink(path)
+
+
+def analysis(n, box, cell_size, scale, pos, pos0, vel, frc, frc0, radius, mass,
+             current_time, out_prefix):
+    """The reference's analysis of a state (see psimref_analysis): returns
+    (coordination numbers, cluster of each particle (-1: none), number of
+    clusters, [temperature, mean displacement, <EAP>]) and writes
+    out_prefix.txt / .xyz with writeSystem / writeSystemXYZ."""
+    f = lambda a: np.ascontiguousarray(a, np.float64)
+    coor = np.zeros(n, np.int32)
+    clu = np.zeros(n, np.int32)
+    nc = C.c_int()
+    stats = np.zeros(3)
+    lib().psimref_analysis(n, int(box), int(cell_size), scale, _p(f(pos)), _p(f(pos0)),
+                           _p(f(vel)), _p(f(frc)), _p(f(frc0)), _p(f(radius)), _p(f(mass)),
+                           float(current_time), _p(coor), _p(clu), C.byref(nc), _p(stats),
+                           out_prefix.encode())
+    return coor, clu, nc.value, stats
 
 
 def system_constants(settings_path):

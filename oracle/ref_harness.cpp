@@ -225,6 +225,44 @@ int psimref_foreign_forces(const char* plugin_path, const char* settings_path, i
     return 0;
 }
 
+// The reference's analysis of an injected state: the cell list and
+// system::updateInteractions (systemHandling.cpp:94-161) -> every particle's
+// coordination number (coor, original order); analysisManager::findClusters
+// (analysisCluster.cpp:26-83) -> the cluster of every particle in the order
+// findClusters returns them (-1: in no cluster of more than 4); getTemperature,
+// meanDisplacement (analysisGeneral.cpp:26-55) and the FP32 sum of
+// particle::calculatePotential (analysisOutput.cpp:117-123) -> stats[0..2];
+// writeSystem and writeSystemXYZ (analysisOutput.cpp:31-74) -> the files
+// out_prefix.txt and out_prefix.xyz.
+int psimref_analysis(int n, int box, int cell_size, int scale, const double* pos,
+                     const double* pos0, const double* vel, const double* frc,
+                     const double* frc0, const double* radius, const double* mass,
+                     double current_time, int* coor, int* cluster_of, int* n_clusters,
+                     double* stats, const char* out_prefix) {
+    Geometry g{n, box, cell_size, scale};
+    PSim::system* s = make_system(g, pos, pos0, vel, frc, frc0, radius, mass);
+    s->hashParticles();
+    s->sortParticles();
+    s->clearCells();
+    s->reorderParticles();
+    s->updateInteractions();
+    for (int i = 0; i < n; i++) coor[i] = s->particles[i]->getCoorNumber();
+    PSim::analysisManager am(std::string("/tmp/psimref_trial"), &s->state);
+    std::vector<std::vector<particle*>> clusters = am.findClusters(s->particles, n);
+    for (int i = 0; i < n; i++) cluster_of[i] = -1;
+    for (size_t c = 0; c < clusters.size(); c++)
+        for (particle* p : clusters[c]) cluster_of[(int)p->getName()] = (int)c;
+    *n_clusters = (int)clusters.size();
+    float pot = 0;
+    for (int i = 0; i < n; i++) pot += s->particles[i]->calculatePotential();
+    stats[0] = am.getTemperature(s->particles, n);
+    stats[1] = am.meanDisplacement(s->particles, n);
+    stats[2] = pot / double(n);
+    am.writeSystem(s->particles, n, std::string(out_prefix));
+    am.writeSystemXYZ(s->particles, n, 1, current_time, std::string(out_prefix));
+    return 0;
+}
+
 // vGB coefficients as the reference integrator's constructor computes them.
 void psimref_vgb_coeffs(const char* settings_path, double* out) {
     PSim::config cfg{std::string(settings_path)};

@@ -2546,6 +2546,41 @@ int psim_system_interactions(psim_system* s, double r_contact, int32_t* coor, in
     if (rc) return rc;
     ScopedBuf cb, tot;
     PSIM_CUDA(cb.ensure(4 * (size_t)s->n));
+    // updateInteractions fused into one force pass on the current state: the
+    // FP64 walk (the reference's own test, sqrt(r^2) < r_contact), the mixed
+    // walk, or the mixed pair list when every pair closer than r_contact is
+    // guaranteed to be in it (r_contact <= cutOff).  A plugin's pass, a batch,
+    // the block-per-cell layout or a list of a shorter cutoff take a separate
+    // walk instead.
+    if (!s->n_reps && !s->cfg.force_launch && s->fs.tile == 0 &&
+        (!s->list_on || r_contact <= max_cutoff(&s->cfg.force))) {
+        const Phase ph = phase_of(s->total);
+        const int n = s->n;
+        ScopedBuf f3;
+        PSIM_CUDA(f3.ensure(24 * (size_t)n));
+        ForceOut fo{f3.as<double>(), f3.as<double>() + n, f3.as<double>() + 2 * (size_t)n,
+                    s->err.as<uint32_t>(), nullptr};
+        fo.coor = cb.as<int>();
+        fo.cont = r_contact;
+        fo.cont2f = (float)(r_contact * r_contact);
+        const float keep = s->fs.pre_rc2f;   // the candidate bound must cover r_contact
+        s->fs.pre_rc2f = std::max(keep, prefilter_r2(r_contact, s->g.L));
+        const cudaError_t e = enqueue_force(s, ph, fo);
+        s->fs.pre_rc2f = keep;
+        PSIM_CUDA(e);
+        if ((rc = settle(s))) return rc;
+        std::vector<int> c((size_t)n), tg((size_t)n);
+        PSIM_CUDA(cudaMemcpy(c.data(), cb.p, 4 * (size_t)n, cudaMemcpyDeviceToHost));
+        PSIM_CUDA(cudaMemcpy(tg.data(), s->list_on ? store_tags(s) : s->tag[ph.ob].as<int>(),
+                             4 * (size_t)n, cudaMemcpyDeviceToHost));
+        int64_t t = 0;
+        for (int i = 0; i < n; ++i) {
+            t += c[(size_t)i];
+            if (coor) coor[tg[(size_t)i]] = c[(size_t)i];
+        }
+        if (total) *total = t;
+        return PSIM_OK;
+    }
     PSIM_CUDA(tot.ensure(8));
     PSIM_CUDA(cudaMemsetAsync(tot.p, 0, 8, s->st));
     PairScanArgs a{};

@@ -46,6 +46,7 @@ struct F64Body {
     using Shifted = Home;     // the FP64 form takes raw differences
     struct Acc {
         double n0, n1, n2, c0, c1, c2;
+        int cnt;
     };
     __device__ __forceinline__ const Aux* aux(const CellView& cv) const { return cv.posd; }
     // the body of replica r of a batch: its own pair functor and box
@@ -58,6 +59,7 @@ struct F64Body {
     }
     __device__ __forceinline__ void init(Acc& a) const {
         a.n0 = a.n1 = a.n2 = a.c0 = a.c1 = a.c2 = 0.0;
+        a.cnt = 0;
     }
     __device__ __forceinline__ void load_home(const CellView& cv, int i, Home& h) const {
         h.p = cv.posd[i];
@@ -75,6 +77,8 @@ struct F64Body {
         if (a1 > g.half) a1 -= g.L;
         if (a2 > g.half) a2 -= g.L;
         const double r2 = (a0 * a0) + (a1 * a1) + (a2 * a2);
+        // updateInteractions' test: r = sqrt(pbcDist) < 1.2 (systemHandling.cpp:112-115)
+        if (cont > 0.0 && sqrt(r2) < cont) ++a.cnt;
         if (r2 < pf.rc2) {
             const double r = sqrt(r2);
             const double size = h.p.w + pj.w;
@@ -126,8 +130,10 @@ struct F64Body {
         out.fx[i] = a.n0;
         out.fy[i] = a.n1;
         out.fz[i] = a.n2;
+        if (out.coor) out.coor[i] = a.cnt;
     }
     DevGeom geom;
+    double cont = 0.0;   // > 0: count the neighbours closer than cont (ForceOut::coor)
 };
 
 struct ComboPairF {
@@ -161,6 +167,7 @@ template <class Pair>
 struct MixedBody {
     Pair pf;
     float rc2f;
+    float cont2f = 0.f;  // > 0: count the neighbours with r^2 < cont2f (ForceOut::coor)
     using Aux = float4;  // the low parts of the neighbour positions
     static constexpr bool kBatchable = !std::is_same<Pair, ComboPairF>::value;
     struct Home {
@@ -172,6 +179,7 @@ struct MixedBody {
     };
     struct Acc {
         float s0, s1, s2, k0, k1, k2, p0, p1, p2;
+        int cnt;
     };
     __device__ __forceinline__ const Aux* aux(const CellView& cv) const { return cv.posl; }
     // the body of replica r of a batch: its own pair functor and cutoff
@@ -184,6 +192,7 @@ struct MixedBody {
     }
     __device__ __forceinline__ void init(Acc& a) const {
         a.s0 = a.s1 = a.s2 = a.k0 = a.k1 = a.k2 = a.p0 = a.p1 = a.p2 = 0.f;
+        a.cnt = 0;
     }
     __device__ __forceinline__ void load_home(const CellView& cv, int i, Home& h) const {
         h.lo = cv.posl[i];
@@ -205,6 +214,7 @@ struct MixedBody {
         const float d1 = (hj.y - hs.h.y) + (lj.y - hs.ly);
         const float d2 = (hj.z - hs.h.z) + (lj.z - hs.lz);
         const float r2 = d0 * d0 + d1 * d1 + d2 * d2;
+        if (cont2f > 0.f && r2 < cont2f) ++a.cnt;
         if (r2 < rc2f) {
             const float rinv = rsqrtf(r2);
             const float r = r2 * rinv;
@@ -220,10 +230,11 @@ struct MixedBody {
     // already formed), masked by the cutoff.  kUniform: every pair has the
     // contact diameter `size` (s2 = size^2), and the overlap test runs once
     // per particle on the smallest r^2 (rmin); otherwise per pair.
-    template <bool kUniform>
+    template <bool kUniform, bool kCount = false>
     __device__ __forceinline__ void eval_list(float d0, float d1, float d2, float size, float s2,
                                               Acc& a, float& rmin, uint32_t& err) const {
         const float r2 = d0 * d0 + d1 * d1 + d2 * d2;
+        if (kCount) a.cnt += r2 < cont2f ? 1 : 0;
         const bool in = r2 < rc2f;
         const float fr = list_fr32(pf, r2, size, s2);
         if (kUniform)
@@ -284,6 +295,7 @@ struct MixedBody {
         out.fx[i] = (double)a.s0 - (double)a.k0;
         out.fy[i] = (double)a.s1 - (double)a.k1;
         out.fz[i] = (double)a.s2 - (double)a.k2;
+        if (out.coor) out.coor[i] = a.cnt;
     }
 };
 

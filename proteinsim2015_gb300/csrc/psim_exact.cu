@@ -25,8 +25,10 @@ template <class Pair>
 static cudaError_t run_fp64(const Pair& p, const DevGeom& g, const CellView& cv,
                             const ForceOut& out, float pre, cudaStream_t st, int tile,
                             const BatchView* bv) {
-    if (tile && !bv) return launch_force_cells(F64Body<Pair>{p, g}, g, cv, out, pre, st);
-    return launch_force_pass(F64Body<Pair>{p, g}, g, cv, out, pre, st, bv);
+    F64Body<Pair> body{p, g};
+    body.cont = out.coor ? out.cont : 0.0;   // updateInteractions fused into the pass
+    if (tile && !bv) return launch_force_cells(body, g, cv, out, pre, st);
+    return launch_force_pass(body, g, cv, out, pre, st, bv);
 }
 
 template <int N>

@@ -276,7 +276,7 @@ __device__ __forceinline__ ListRec<false> load_rec(const float4* pos, uint32_t j
 // is d = (x_j,hi - x_i,hi) + (x_j,lo - x_i,lo): the first difference is exact
 // for nearby values and the second comes out of the record's decode
 // (compact) or one subtraction (full), so d carries one FP32 rounding.
-template <class Body, bool kCompact, bool kReplicas>
+template <class Body, bool kCompact, bool kReplicas, bool kCount = false>
 __global__ void __launch_bounds__(256)
 force_list_kernel(Body body0, DevGeom g, PairList pl, ForceOut out) {
     constexpr int kBatch = 4;
@@ -321,13 +321,14 @@ force_list_kernel(Body body0, DevGeom g, PairList pl, ForceOut out) {
                 const float d0 = (r[u].h.x - hh.x) + fmaf(lo_magic(w & 1023u), unit, cx);
                 const float d1 = (r[u].h.y - hh.y) + fmaf(lo_magic((w >> 10) & 1023u), unit, cy);
                 const float d2 = (r[u].h.z - hh.z) + fmaf(lo_magic((w >> 20) & 1023u), unit, cz);
-                body.template eval_list<true>(d0, d1, d2, usize, us2, acc, rmin, err);
+                body.template eval_list<true, kCount>(d0, d1, d2, usize, us2, acc, rmin, err);
             } else {
                 const float d0 = (r[u].h.x - hh.x) + (r[u].l.x - hl.x);
                 const float d1 = (r[u].h.y - hh.y) + (r[u].l.y - hl.y);
                 const float d2 = (r[u].h.z - hh.z) + (r[u].l.z - hl.z);
                 const float size = hh.w + r[u].h.w;
-                body.template eval_list<false>(d0, d1, d2, size, size * size, acc, rmin, err);
+                body.template eval_list<false, kCount>(d0, d1, d2, size, size * size, acc, rmin,
+                                                       err);
             }
         }
     };
@@ -382,6 +383,13 @@ cudaError_t launch_force_list(const Body& body, const DevGeom& g, const PairList
             return cudaGetLastError();
         }
         return cudaErrorInvalidValue;
+    }
+    if (out.coor) {   // the coordination numbers with the forces (one system)
+        if (pl.compact)
+            force_list_kernel<Body, true, false, true><<<blocks, 256, 0, st>>>(body, g, pl, out);
+        else
+            force_list_kernel<Body, false, false, true><<<blocks, 256, 0, st>>>(body, g, pl, out);
+        return cudaGetLastError();
     }
     if (pl.compact)
         force_list_kernel<Body, true, false><<<blocks, 256, 0, st>>>(body, g, pl, out);

@@ -42,6 +42,14 @@ struct ForceOut {
     double* fz;
     uint32_t* err;
     const int* gate;   // may be null; else the pass runs only when *gate != 0
+    // updateInteractions fused into the pass (systemHandling.cpp:94-161): when
+    // coor is set, the number of neighbours closer than `cont` is written per
+    // particle in the pass's order (the FP64 form tests sqrt(r^2) < cont as the
+    // reference does; the mixed form r^2 < cont2f).  The caller widens the
+    // candidate bound to cover cont; the block-per-cell layout does not count.
+    int* coor;
+    double cont;
+    float cont2f;
 };
 
 // Independent replicas in one launch: per warp a task (replica, first

@@ -57,7 +57,8 @@ cudaError_t launch_forces_mixed(const ForceSetup& fs, const DevGeom& g, const Ce
                                 const ForceOut& out, cudaStream_t st, const BatchView* bv) {
     if (bv && fs.kind == 4) return cudaErrorInvalidValue;  // batches hold single-plugin replicas
     return with_pair(fs, [&](auto p, float rc2f) {
-        const MixedBody<decltype(p)> body{p, rc2f};
+        MixedBody<decltype(p)> body{p, rc2f};
+        body.cont2f = out.coor ? out.cont2f : 0.f;   // updateInteractions fused into the pass
         if (fs.tile && !bv) return launch_force_cells(body, g, cv, out, fs.pre_rc2f, st);
         return launch_force_pass(body, g, cv, out, fs.pre_rc2f, st, bv);
     });
@@ -66,7 +67,9 @@ cudaError_t launch_forces_mixed(const ForceSetup& fs, const DevGeom& g, const Ce
 cudaError_t launch_forces_list(const ForceSetup& fs, const DevGeom& g, const PairList& pl,
                                const ForceOut& out, cudaStream_t st) {
     return with_pair(fs, [&](auto p, float rc2f) {
-        return launch_force_list(MixedBody<decltype(p)>{p, rc2f}, g, pl, out, st);
+        MixedBody<decltype(p)> body{p, rc2f};
+        body.cont2f = out.coor ? out.cont2f : 0.f;
+        return launch_force_list(body, g, pl, out, st);
     });
 }
 

@@ -7,6 +7,9 @@ inputs.  Inputs are stored next to the outputs so the fixtures stand alone
 (the GPU machine has no reference tree).
 
     python tests/golden/make_golden.py [--settings-only]
+
+--settings-only writes the settings and analysis fixtures but not
+reference_hotpath.npz.
 """
 import os
 import sys
@@ -61,11 +64,51 @@ def settings_fixtures():
     print("wrote", path, os.path.getsize(path), "bytes")
 
 
+def analysis_fixtures():
+    """reference_analysis.npz: an aggregated AO state (N = 2000, L = 18, 6
+    cells a side, 4 kT contact attraction, 2,000 steps of the oracle's loop
+    driven by the reference's own noise stream) and the reference's analysis
+    of it: updateInteractions' coordination numbers, findClusters' clusters,
+    getTemperature / meanDisplacement / <EAP>, and the text of writeSystem's
+    recovery.txt and writeSystemXYZ's .xyz frame."""
+    import tempfile
+    from oracle import port
+    port.build()
+    port.set_threads(os.cpu_count() or 1)
+    n, box, cs, scale, dt, steps = 2000, 18, 3, 6, 0.001, 2000   # box = cs * scale
+    pos, rad = state_small(n, box, seed=29)
+    vel = init.maxwell(n, 1.0, seed=29).reshape(-1)
+    st = port.State(pos, rad, vel=vel)
+    noise = port.ReferenceNoise(n, 90210)
+    err, *_ = port.run(port.geom(n, box, cs, scale),
+                       port.make_force(port.AO, 1.1, kT=1.0, well_depth=0.25),
+                       port.vgb_coeffs(1.0, dt, 1.0), dt, st, steps, noise.take(steps),
+                       vel_freq=0)
+    assert err == 0
+    d = tempfile.mkdtemp(prefix="psimref_analysis_")
+    prefix = os.path.join(d, "recovery")
+    t = steps * dt
+    coor, clu, nc, stats = ref.analysis(n, box, cs, scale, st.pos, st.pos0, st.vel, st.frc,
+                                        st.frc0, rad, st.mass, t, prefix)
+    with open(prefix + ".txt") as fh:
+        recovery = fh.read()
+    with open(prefix + ".xyz") as fh:
+        xyz = fh.read()
+    out = dict(geom=np.array([n, box, cs, scale]), time=np.array(t), pos=st.pos, pos0=st.pos0,
+               vel=st.vel, frc=st.frc, frc0=st.frc0, radius=rad, mass=st.mass,
+               coor=coor, cluster_of=clu, n_clusters=np.array(nc), stats=stats,
+               recovery_txt=np.array(recovery), xyz=np.array(xyz))
+    path = os.path.join(HERE, "reference_analysis.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path, os.path.getsize(path), "bytes", "clusters", nc, "mean coor", coor.mean())
+
+
 def main():
     if not ref.available():
         if not ref.build():
             sys.exit("reference sources not found; cannot generate golden fixtures")
     settings_fixtures()
+    analysis_fixtures()
     if "--settings-only" in sys.argv:
         return
     out = {}
