@@ -372,18 +372,33 @@ typedef struct {
     double yuk_amplitude;              /* kT wellDepth yukawaStrength of the LJ plugin */
     double yuk_length;                 /* debyeLength */
     double yuk_cutoff;                 /* its cutOff (0: no Yukawa term) */
+    /* the AO coefficients' range 1 + q (0: ao_cutoff); differentiating with
+     * respect to it holds the cutoff distance ao_cutoff fixed */
+    double ao_range;
+    /* the LennardJones plugin's LJ(n) term: fNet = -eps (2L - 1) 4n L / r,
+     * L = (sigma / r)^n (eps = kT wellDepth, sigma the contact diameter) */
+    double lj_epsilon, lj_sigma;
+    double lj_cutoff;                  /* 0: no LJ(n) term */
+    int32_t lj_n;
 } psim_adjoint_params;
 
 psim_adjoint* psim_adjoint_create(const psim_adjoint_config* cfg, int32_t device);
+/* The Philox Gaussians the systems and the adjoint draw (PSIM_NOISE_PHILOX):
+ * n_steps steps from first_step for particles 0..n-1 with `seed`, in the
+ * injected-noise layout out[((step - first_step) n + i) 6 + k] (host memory,
+ * n_steps n 6 doubles), computed on `device`.  With them a CPU checker can
+ * replay a Philox run exactly. */
+int psim_philox_noise(uint32_t seed, int32_t n, int64_t first_step, int32_t n_steps,
+                      double* out, int32_t device);
 void psim_adjoint_destroy(psim_adjoint* adj);
 /* The trajectory from pos0/vel0 (3n, original order; vel0 may be NULL):
  * g_mean (n_bins) and, if not NULL, the final positions (3n, unwrapped). */
 int psim_adjoint_forward(psim_adjoint* adj, const psim_adjoint_params* p, const double* pos0,
                          const double* vel0, double* g_mean, double* pos_final);
 /* Loss against g_target, its g_mean (may be NULL), and the gradient
- * grad[4] = dL/d(ao_well_depth, ao_cutoff, yuk_amplitude, yuk_length) -- the
- * AO cutoff through the AO coefficients only, its cutoff held fixed -- and,
- * if not NULL, dL/d(pos0) (3n). */
+ * grad[6] = dL/d(ao_well_depth, ao_range, yuk_amplitude, yuk_length,
+ * lj_epsilon, lj_sigma) -- the AO range through the AO coefficients only,
+ * the cutoff distance held fixed -- and, if not NULL, dL/d(pos0) (3n). */
 int psim_adjoint_gradient(psim_adjoint* adj, const psim_adjoint_params* p, const double* pos0,
                           const double* vel0, const double* g_target, double* loss,
                           double* g_mean, double* grad, double* grad_pos0);

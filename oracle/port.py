@@ -16,16 +16,18 @@ AO, LJ, CAL, AO_YUK = 1, 2, 3, 4
 
 
 def build(force=False):
-    """Compile psim_oracle.c (no FMA contraction, so x86 and Arm agree)."""
-    src = os.path.join(HERE, "psim_oracle.c")
+    """Compile psim_oracle.c and psim_tangent.c (no FMA contraction, so x86
+    and Arm agree)."""
+    srcs = [os.path.join(HERE, f) for f in ("psim_oracle.c", "psim_tangent.c")]
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(
-            os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "psim_oracle.h"))):
+            [os.path.getmtime(f) for f in srcs] + [os.path.getmtime(os.path.join(HERE,
+                                                                            "psim_oracle.h"))]):
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     tmp = LIB + ".tmp%d" % os.getpid()
-    subprocess.check_call(["gcc", "-O2", "-std=c99", "-fopenmp", "-fPIC", "-shared",
+    subprocess.check_call(["gcc", "-O2", "-std=gnu99", "-fopenmp", "-fPIC", "-shared",
                            "-ffp-contract=off", "-fno-fast-math", "-Wall",
-                           src, "-o", tmp, "-lm"])
+                           *srcs, "-o", tmp, "-lm"])
     os.replace(tmp, LIB)
     return LIB
 
@@ -49,6 +51,15 @@ class Vgb(C.Structure):
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class AdjParams(C.Structure):
+    """oracle_adj_params: the fields of psim_adjoint_params."""
+    _fields_ = [("kT", C.c_double), ("ao_well_depth", C.c_double), ("ao_cutoff", C.c_double),
+                ("yuk_amplitude", C.c_double), ("yuk_length", C.c_double),
+                ("yuk_cutoff", C.c_double), ("ao_range", C.c_double),
+                ("lj_epsilon", C.c_double), ("lj_sigma", C.c_double), ("lj_cutoff", C.c_double),
+                ("lj_n", C.c_int32)]
 
 
 class FastRandom(C.Structure):
@@ -89,6 +100,11 @@ def lib():
         _lib.oracle_fastrandom_g250.restype = C.c_double
         _lib.oracle_fastrandom_fill.argtypes = [C.POINTER(FastRandom), C.c_int, C.c_int, C.c_int,
                                                 C.c_int, P]
+        _lib.oracle_adjoint_tangent.argtypes = ([C.c_int, C.c_double, C.POINTER(AdjParams),
+                                                 C.POINTER(Vgb), C.c_double, C.c_double,
+                                                 C.c_int, C.c_int, C.c_double, C.c_double,
+                                                 C.c_int, C.c_double] + [P] * 7)
+        _lib.oracle_adjoint_tangent.restype = C.c_int
     return _lib
 
 
@@ -249,3 +265,23 @@ class ReferenceNoise:
                                      _p(out))
         self.first = 0
         return out
+
+
+def adjoint_tangent(box, params, gamma, dt, kT, mass, n_steps, sample_every, r_min, r_max,
+                    n_bins, sigma, pos0, vel0, noise, g_target):
+    """(loss, g_mean, grad[6]) of the differentiable trajectory by FP64
+    forward-mode tangents (psim_tangent.c); params: an object with the fields
+    of psim_adjoint_params; noise: n_steps*n*6 draws in the injected layout."""
+    n = len(pos0) // 3
+    p = AdjParams(**{k: getattr(params, k) for k, _ in AdjParams._fields_})
+    c = vgb_coeffs(gamma, dt, kT)
+    g = np.empty(n_bins)
+    grad = np.empty(6)
+    loss = np.zeros(1)
+    f = lambda a: None if a is None else np.ascontiguousarray(a, np.float64)
+    rc = lib().oracle_adjoint_tangent(n, float(box), C.byref(p), C.byref(c), dt, mass, n_steps,
+                                      sample_every, r_min, r_max, n_bins, sigma, _p(f(pos0)),
+                                      _p(f(vel0)), _p(f(noise)), _p(f(g_target)), _p(loss),
+                                      _p(g), _p(grad))
+    assert rc == 0, rc
+    return float(loss[0]), g, grad

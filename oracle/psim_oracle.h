@@ -152,6 +152,28 @@ double oracle_fastrandom_g250(oracle_fastrandom* r, int seed);
 void   oracle_fastrandom_fill(oracle_fastrandom* gens, int n, int seed, int first,
                               int n_steps, double* out);
 
+/* The differentiable trajectory's parameters, as psim_adjoint_params. */
+typedef struct {
+    double kT;
+    double ao_well_depth, ao_cutoff;
+    double yuk_amplitude, yuk_length, yuk_cutoff;
+    double ao_range;
+    double lj_epsilon, lj_sigma, lj_cutoff;
+    int32_t lj_n;
+} oracle_adj_params;
+
+/* psim_tangent.c: the loss of the differentiable trajectory (n_steps vGB
+ * steps from pos0/vel0, 3n AoS each, vel0 may be NULL, with the injected
+ * noise noise[(t n + i) 6 + k]; time-averaged smoothed g(r) against
+ * g_target) and its gradient grad[6] = dL/d(ao_well_depth, ao_range,
+ * yuk_amplitude, yuk_length, lj_epsilon, lj_sigma) by FP64 forward-mode
+ * tangents.  g_mean (n_bins) may be NULL.  Returns 0. */
+int oracle_adjoint_tangent(int n, double box, const oracle_adj_params* p, const oracle_vgb* c,
+                           double dt, double mass, int n_steps, int sample_every, double r_min,
+                           double r_max, int n_bins, double sigma, const double* pos0,
+                           const double* vel0, const double* noise, const double* g_target,
+                           double* loss, double* g_mean, double* grad);
+
 #ifdef __cplusplus
 }
 #endif

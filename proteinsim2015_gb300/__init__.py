@@ -153,6 +153,7 @@ def lib():
             "psim_system_track_start": ([P], C.c_int),
             "psim_system_tracked_displacement": ([P, C.POINTER(C.c_double)], C.c_int),
             "psim_system_interactions": ([P, C.c_double, P, C.POINTER(C.c_int64)], C.c_int),
+            "psim_philox_noise": ([C.c_uint32, C.c_int32, C.c_int64, C.c_int32, P, C.c_int32], C.c_int),
             "psim_system_energy": ([P, C.POINTER(C.c_double), C.POINTER(C.c_double)], C.c_int),
             "psim_system_rdf": ([P, C.c_double, C.c_double, C.c_int32, P], C.c_int),
             "psim_system_clusters": ([P, C.c_double, C.c_int32, P, C.POINTER(C.c_int32),
@@ -200,6 +201,17 @@ def _f64(a, n=None):
 
 def device_count():
     return lib().psim_device_count()
+
+
+def philox_noise(seed, n, first_step, n_steps, device=0):
+    """The Philox Gaussians a system or the adjoint draws for particles
+    0..n-1 at steps first_step .. first_step + n_steps - 1, in the injected
+    layout (n_steps * n * 6), computed on the GPU: a CPU checker replays a
+    Philox run with them."""
+    out = np.empty(int(n_steps) * int(n) * 6)
+    _check(lib().psim_philox_noise(int(seed) & 0xffffffff, int(n), int(first_step), int(n_steps),
+                                   _p(out), int(device)))
+    return out
 
 
 def measure_host_link(device=0):

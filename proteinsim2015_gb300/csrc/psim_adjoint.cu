@@ -27,12 +27,14 @@
 //
 // All arithmetic is FP64 and the forward matches the system's plain form
 // (same coefficients and Philox draws) up to rounding.  The pair force is the
-// AO plugin (AOPotential.cpp:50-130) plus the Yukawa term of the LennardJones
-// plugin with ljNum = 0 (LJPotential.cpp:96-109), each inside its own cutoff;
-// parameters th = (c1, c2, Y, lambda): the AO coefficients, the Yukawa
-// amplitude kT wellDepth yukawaStrength and its length.  The cutoffs are
-// fixed: a pair crossing a cutoff changes the force by a step, which no
-// derivative of the smooth part carries.
+// AO plugin (AOPotential.cpp:50-130), the Yukawa term of the LennardJones
+// plugin with ljNum = 0 and the plugin's LJ(n) term (LJPotential.cpp:96-109),
+// each inside its own cutoff; parameters th = (c1, c2, Y, lambda, eps,
+// sigma): the AO coefficients, the Yukawa amplitude kT wellDepth
+// yukawaStrength and its length, and the LJ energy kT wellDepth and contact
+// diameter (the plugin's size, L = (sigma/r)^n).  The cutoffs are fixed: a
+// pair crossing a cutoff changes the force by a step, which no derivative of
+// the smooth part carries.
 #include <cmath>
 #include <cstdint>
 #include <mutex>
@@ -44,19 +46,23 @@
 namespace psim {
 namespace {
 
+constexpr int kAdjTh = 6;    // parameters: c1, c2, Y, lambda, eps, sigma
+
 struct AdjPair {
     double c1, c2, ao_rc2;   // ao_rc2 = 0: no AO term
     double Y, lam, y_rc2;    // y_rc2 = 0: no Yukawa term
     double inv_lam;          // 1 / lam
+    double eps, sig, lj_rc2; // lj_rc2 = 0: no LJ(n) term
+    int ljn;
 };
 
 // s(r) = F_pair / r (force on i along x_j - x_i), ds/dr and ds/dth
 __device__ __forceinline__ void pair_terms(const AdjPair& q, double r2, double& s, double& ds,
-                                           double dth[4]) {
+                                           double dth[kAdjTh]) {
     const double ri = rsqrt(r2), r = r2 * ri;
     s = 0.0;
     ds = 0.0;
-    dth[0] = dth[1] = dth[2] = dth[3] = 0.0;
+    for (int k = 0; k < kAdjTh; ++k) dth[k] = 0.0;
     const double ri2 = ri * ri, ri3 = ri2 * ri;
     if (r2 < q.ao_rc2) {
         const double ri4 = ri2 * ri2, ri8 = ri4 * ri4, ri16 = ri8 * ri8, ri32 = ri16 * ri16;
@@ -73,6 +79,18 @@ __device__ __forceinline__ void pair_terms(const AdjPair& q, double r2, double& 
         ds += q.Y * e * ri3 * (r * q.inv_lam + 3.0 * lr * ri);
         dth[2] = -e * lr * ri3;
         dth[3] = -q.Y * e * ri3 * (r * lr * q.inv_lam * q.inv_lam + 1.0);
+    }
+    if (r2 < q.lj_rc2) {
+        // fNet = -eps (2L - 1) 4n L / r, L = (sigma / r)^n: s = -4n eps (2L - 1) L / r^2,
+        // ds/dr = 4n eps L (n (4L - 1) + 2 (2L - 1)) / r^3,
+        // ds/dsigma = -4n^2 eps (4L - 1) L / (sigma r^2)
+        const double n = (double)q.ljn;
+        const double L = powi_binary(q.sig * ri, q.ljn);
+        const double base = -4.0 * n * (2.0 * L - 1.0) * L * ri2;
+        s += q.eps * base;
+        ds += 4.0 * n * q.eps * L * (n * (4.0 * L - 1.0) + 2.0 * (2.0 * L - 1.0)) * ri3;
+        dth[4] = base;
+        dth[5] = -4.0 * n * n * q.eps * (4.0 * L - 1.0) * L * ri2 / q.sig;
     }
 }
 
@@ -171,7 +189,7 @@ __global__ void __launch_bounds__(128) adj_force_kernel(AdjWalk w, double rc2, d
     const double4_32a pi = w.sp[p];
     double f[3] = {0.0, 0.0, 0.0};
     for_pairs(w, p, pi, rc2, [&](int, const double* d, double r2) {
-        double s, ds, dth[4];
+        double s, ds, dth[kAdjTh];
         pair_terms(w.q, r2, s, ds, dth);
         for (int k = 0; k < 3; ++k) f[k] += s * d[k];
     });
@@ -229,13 +247,13 @@ struct AdjReverse {
     double cu0, cu1;           // u_{t-1} = cu0 lam_t + cu1 lam1
     const double* wgt;    // per bin: dL/d(smoothed count) of this step, or null
     AdjHist h;
-    double* part;         // per block: 4 parameter partials
+    double* part;         // per block: kAdjTh parameter partials
 };
 
 __global__ void __launch_bounds__(128) adj_reverse_kernel(AdjWalk w, double rc2, AdjReverse a) {
-    __shared__ double red[4][128];
+    __shared__ double red[kAdjTh][128];
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    double th[4] = {0.0, 0.0, 0.0, 0.0};
+    double th[kAdjTh] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     if (p < w.n) {
         const int i = w.order[p];
         const int n = w.n;
@@ -244,7 +262,7 @@ __global__ void __launch_bounds__(128) adj_reverse_kernel(AdjWalk w, double rc2,
         double ju[3] = {0.0, 0.0, 0.0}, gl[3] = {0.0, 0.0, 0.0};
         for_pairs(w, p, pi, rc2, [&](int q, const double* d, double r2) {
             const int j = w.order[q];
-            double s, ds, dth[4];
+            double s, ds, dth[kAdjTh];
             pair_terms(w.q, r2, s, ds, dth);
             const double r = sqrt(r2);
             const double du[3] = {a.u[j] - ui[0], a.u[n + j] - ui[1], a.u[2 * (size_t)n + j] - ui[2]};
@@ -252,7 +270,7 @@ __global__ void __launch_bounds__(128) adj_reverse_kernel(AdjWalk w, double rc2,
             const double c = ds / r;
             const double dui = d[0] * ui[0] + d[1] * ui[1] + d[2] * ui[2];
             for (int k = 0; k < 3; ++k) ju[k] += s * du[k] + c * d[k] * ddu;
-            for (int k = 0; k < 4; ++k) th[k] += dth[k] * dui;
+            for (int k = 0; k < kAdjTh; ++k) th[k] += dth[k] * dui;
             if (a.wgt) {
                 // d/dx_i of the smoothed counts of pairs (i, j) and (j, i)
                 double wr = 0.0;
@@ -269,20 +287,20 @@ __global__ void __launch_bounds__(128) adj_reverse_kernel(AdjWalk w, double rc2,
             a.u_prev[o] = a.cu0 * l0 + a.cu1 * a.lam1[o];
         }
     }
-    for (int k = 0; k < 4; ++k) red[k][threadIdx.x] = th[k];
+    for (int k = 0; k < kAdjTh; ++k) red[k][threadIdx.x] = th[k];
     __syncthreads();
-    if (threadIdx.x < 4) {
+    if (threadIdx.x < kAdjTh) {
         double t = 0.0;
         for (int m = 0; m < blockDim.x; ++m) t += red[threadIdx.x][m];
-        a.part[4 * (size_t)blockIdx.x + threadIdx.x] = t;
+        a.part[kAdjTh * (size_t)blockIdx.x + threadIdx.x] = t;
     }
 }
 
-// adds the block partials into acc[4] in block order (one thread block)
+// adds the block partials into acc[kAdjTh] in block order (one thread block)
 __global__ void adj_accumulate_kernel(const double* part, int blocks, double* acc) {
-    if (threadIdx.x < 4) {
+    if (threadIdx.x < kAdjTh) {
         double t = 0.0;
-        for (int b = 0; b < blocks; ++b) t += part[4 * (size_t)b + threadIdx.x];
+        for (int b = 0; b < blocks; ++b) t += part[kAdjTh * (size_t)b + threadIdx.x];
         acc[threadIdx.x] += t;
     }
 }
@@ -316,6 +334,16 @@ __global__ void __launch_bounds__(256) adj_step_kernel(AdjStep c, long long step
                     c.coeff0 * mc;
         }
     }
+}
+
+__global__ void __launch_bounds__(256) philox_noise_kernel(uint32_t seed, int n, long long first,
+                                                           int n_steps, double* out) {
+    const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (idx >= (long long)n * n_steps) return;
+    const int t = (int)(idx / n), i = (int)(idx % n);
+    double xi[6];
+    philox_gaussians6(seed, (uint32_t)i, (uint32_t)(first + t), xi);
+    for (int k = 0; k < 6; ++k) out[6 * idx + k] = xi[k];
 }
 
 }  // namespace
@@ -465,7 +493,10 @@ void set_pair(const psim_adjoint_params* p, AdjPair& q, double dwd[2], double dr
     dwd[0] = dwd[1] = drc[0] = drc[1] = 0.0;
     q = AdjPair{};
     if (p->ao_cutoff > 0.0) {
-        ao_coeffs_d(p->kT, p->ao_well_depth, p->ao_cutoff, c, dwd, drc);
+        // the coefficients' range (1 + q) and the cutoff distance: the same
+        // unless ao_range is given, which holds the cutoff while q moves
+        const double range = p->ao_range > 0.0 ? p->ao_range : p->ao_cutoff;
+        ao_coeffs_d(p->kT, p->ao_well_depth, range, c, dwd, drc);
         q.c1 = c[0];
         q.c2 = c[1];
         q.ao_rc2 = p->ao_cutoff * p->ao_cutoff;
@@ -475,6 +506,12 @@ void set_pair(const psim_adjoint_params* p, AdjPair& q, double dwd[2], double dr
         q.lam = p->yuk_length;
         q.inv_lam = 1.0 / p->yuk_length;
         q.y_rc2 = p->yuk_cutoff * p->yuk_cutoff;
+    }
+    if (p->lj_cutoff > 0.0) {
+        q.eps = p->lj_epsilon;
+        q.sig = p->lj_sigma;
+        q.ljn = p->lj_n;
+        q.lj_rc2 = p->lj_cutoff * p->lj_cutoff;
     }
 }
 
@@ -594,7 +631,7 @@ psim_adjoint* psim_adjoint_create(const psim_adjoint_config* cfg, int32_t device
               !a->traj.ensure(b3 * (size_t)(a->K + 2)) && !a->ck.ensure(3 * b3 * (size_t)nck) &&
               !a->lam[0].ensure(b3) && !a->lam[1].ensure(b3) && !a->lam[2].ensure(b3) &&
               !a->u[0].ensure(b3) && !a->u[1].ensure(b3) &&
-              !a->part.ensure(32 * (size_t)a->blocks128) && !a->acc.ensure(32) &&
+              !a->part.ensure(8 * kAdjTh * (size_t)a->blocks128) && !a->acc.ensure(8 * kAdjTh) &&
               !a->hsum.ensure(8 * (size_t)cfg->n_bins) && !a->wgt.ensure(8 * (size_t)cfg->n_bins);
     if (!ok) {
         adj_fail(PSIM_ERR_CUDA, "adjoint: device allocation failed");
@@ -602,6 +639,33 @@ psim_adjoint* psim_adjoint_create(const psim_adjoint_config* cfg, int32_t device
         return nullptr;
     }
     return a;
+}
+
+int psim_philox_noise(uint32_t seed, int32_t n, int64_t first_step, int32_t n_steps,
+                      double* out, int32_t device) {
+    if (!out || n < 0 || n_steps < 0 || first_step < 0)
+        return adj_fail(PSIM_ERR_INPUT, "philox noise: bad arguments");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev)
+        return adj_fail(PSIM_ERR_NO_DEVICE, "philox noise: no such CUDA device");
+    const long long cnt = (long long)n * n_steps;
+    if (cnt == 0) return PSIM_OK;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(device);
+    cudaError_t e;
+    {   // the buffer is freed with `device` current
+        Buf b;
+        e = b.ensure(48 * (size_t)cnt);
+        if (e == cudaSuccess) {
+            philox_noise_kernel<<<(unsigned)((cnt + 255) / 256), 256>>>(seed, n, first_step,
+                                                                        n_steps, b.as<double>());
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaMemcpy(out, b.p, 48 * (size_t)cnt, cudaMemcpyDeviceToHost);
+    }
+    cudaSetDevice(prev);
+    return e == cudaSuccess ? PSIM_OK : adj_fail(PSIM_ERR_CUDA, cudaGetErrorString(e));
 }
 
 void psim_adjoint_destroy(psim_adjoint* a) {
@@ -621,7 +685,7 @@ int psim_adjoint_forward(psim_adjoint* a, const psim_adjoint_params* p, const do
     AdjPair q;
     double dwd[2], drc[2];
     set_pair(p, q, dwd, drc);
-    a->rc2 = std::max(q.ao_rc2, q.y_rc2);
+    a->rc2 = std::max(std::max(q.ao_rc2, q.y_rc2), q.lj_rc2);
     if (a->rc2 > a->cfg.geom.cell_size * a->cfg.geom.cell_size)
         return adj_fail(PSIM_ERR_INPUT, "adjoint: a cutoff exceeds the cell size");
     int rc = forward_all(a, q, pos0, vel0);
@@ -652,9 +716,11 @@ int psim_adjoint_gradient(psim_adjoint* a, const psim_adjoint_params* p, const d
     AdjPair q;
     double dwd[2], drc[2];
     set_pair(p, q, dwd, drc);
-    a->rc2 = std::max(q.ao_rc2, q.y_rc2);
+    a->rc2 = std::max(std::max(q.ao_rc2, q.y_rc2), q.lj_rc2);
     if (a->rc2 > a->cfg.geom.cell_size * a->cfg.geom.cell_size)
         return adj_fail(PSIM_ERR_INPUT, "adjoint: a cutoff exceeds the cell size");
+    if (q.lj_rc2 > 0.0 && (!(q.sig > 0.0) || q.ljn < 0 || q.ljn > 64))
+        return adj_fail(PSIM_ERR_INPUT, "adjoint: LJ term needs sigma > 0 and 0 <= n <= 64");
     // forward: checkpoints and the loss
     int rc = forward_all(a, q, pos0, vel0);
     if (rc) return rc;
@@ -676,7 +742,7 @@ int psim_adjoint_gradient(psim_adjoint* a, const psim_adjoint_params* p, const d
     // reverse: lam_{T+1} = lam_{T+2} = 0, u_T = 0
     for (int k = 0; k < 3; ++k) ADJ_CUDA(cudaMemsetAsync(a->lam[k].p, 0, b3, a->st));
     ADJ_CUDA(cudaMemsetAsync(a->u[0].p, 0, b3, a->st));
-    ADJ_CUDA(cudaMemsetAsync(a->acc.p, 0, 32, a->st));
+    ADJ_CUDA(cudaMemsetAsync(a->acc.p, 0, 8 * kAdjTh, a->st));
     int l0 = 0, l1 = 1, l2 = 2, uc = 0;   // lam_t, lam_{t+1}, lam_{t+2}; u_t
     double* slot0 = pos_at(a, a->traj, 0);
     double* slot1 = pos_at(a, a->traj, 1);
@@ -724,8 +790,8 @@ int psim_adjoint_gradient(psim_adjoint* a, const psim_adjoint_params* p, const d
             uc = 1 - uc;
         }
     }
-    double th[4];
-    ADJ_CUDA(cudaMemcpyAsync(th, a->acc.p, 32, cudaMemcpyDeviceToHost, a->st));
+    double th[kAdjTh];
+    ADJ_CUDA(cudaMemcpyAsync(th, a->acc.p, 8 * kAdjTh, cudaMemcpyDeviceToHost, a->st));
     if (grad_pos0) {   // lam_0 (now lam[l1]) in original order
         const double* l = a->lam[l1].as<double>();
         ADJ_CUDA(launch_merge_xyz(n, l, l + n, l + 2 * (size_t)n, nullptr, nullptr,
@@ -733,11 +799,14 @@ int psim_adjoint_gradient(psim_adjoint* a, const psim_adjoint_params* p, const d
         ADJ_CUDA(cudaMemcpyAsync(grad_pos0, a->x0.p, b3, cudaMemcpyDeviceToHost, a->st));
     }
     ADJ_CUDA(cudaStreamSynchronize(a->st));
-    // th = dL/d(c1, c2, Y, lambda) -> dL/d(AO wellDepth, AO cutOff, Y, lambda)
+    // th = dL/d(c1, c2, Y, lambda, eps, sigma) -> dL/d(AO wellDepth, AO range,
+    // Y, lambda, eps, sigma)
     grad[0] = th[0] * dwd[0] + th[1] * dwd[1];
     grad[1] = th[0] * drc[0] + th[1] * drc[1];
     grad[2] = th[2];
     grad[3] = th[3];
+    grad[4] = th[4];
+    grad[5] = th[5];
     return PSIM_OK;
 }
 

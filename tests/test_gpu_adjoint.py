@@ -13,7 +13,7 @@ pytestmark = pytest.mark.gpu
 
 def setup(psim, n=300, phi=0.18, seed=90):
     box = (n * math.pi / 6.0 / phi) ** (1.0 / 3.0)
-    scale = 3                               # cells of >= 3.09: the Yukawa cutoff and g(r) reach
+    scale = max(3, int(box // 3.1))         # cells of >= 3.1: the Yukawa cutoff and g(r) reach
     pos, rad = rsa_state(n, box, seed=seed)
     vel = np.random.default_rng(seed).standard_normal(3 * n)
     return psim.geometry(n, box, box / scale, scale), pos, vel
@@ -89,7 +89,7 @@ def test_torch_function_and_cost(psim):
     loss.backward()
     p, J = adj.plugin_params(3.0, 0.1, 10.0, 4.0)
     _, _, grad, _ = a.gradient(p, pos, target, vel)
-    assert np.allclose(theta.grad.numpy(), J.T @ grad, rtol=1e-12)
+    assert np.allclose(theta.grad.numpy(), (J.T @ grad)[:4], rtol=1e-12)
     t0 = time.perf_counter()
     a.forward(p, pos, vel)
     t1 = time.perf_counter()
@@ -97,3 +97,67 @@ def test_torch_function_and_cost(psim):
     t2 = time.perf_counter()
     print("adjoint cost / forward:", (t2 - t1) / (t1 - t0))
     a.close()
+
+
+def _lj_params(adj, **kw):
+    d = dict(lj_epsilon=0.3, lj_sigma=1.0, lj_n=6, lj_cutoff=2.0)
+    d.update(kw)
+    return adj.plugin_params(3.0, 0.1, 10.0, 4.0, **d)
+
+
+def test_gradient_matches_forward_mode_tangent(psim, oracle_port):
+    # the FP64 reverse sweep on the GPU against FP64 forward-mode tangents on
+    # the CPU (oracle/psim_tangent.c), on the same trajectory: the GPU's own
+    # Philox draws replayed; all six plugin parameters, the LJ(n) term on
+    from proteinsim2015_gb300 import adjoint as adj
+    g, pos, vel = setup(psim, seed=93)
+    n, T, every, nb, seed = g.n_particles, 40, 4, 60, 19
+    a = adj.Adjoint(g, T, dt=0.001, seed=seed, checkpoint_every=16, sample_every=every, n_bins=nb)
+    p, _ = _lj_params(adj)
+    pt, _ = _lj_params(adj, lj_epsilon=0.33, lj_sigma=1.03)
+    target = a.forward(pt, pos, vel)
+    loss, gm, grad, _ = a.gradient(p, pos, target, vel)
+    a.close()
+    noise = psim.philox_noise(seed, n, 0, T)
+    tl, tg, tgrad = oracle_port.adjoint_tangent(g.box_size, p, 1.0, 0.001, 1.0, 1.0, T, every,
+                                                0.8, 3.0, nb, (3.0 - 0.8) / nb, pos, vel, noise,
+                                                target)
+    assert loss == pytest.approx(tl, rel=1e-9)
+    assert np.allclose(gm, tg, rtol=1e-9, atol=1e-12)
+    for k, name in enumerate(adj.GRAD_NAMES):
+        assert grad[k] == pytest.approx(tgrad[k], rel=1e-6, abs=1e-9 * max(abs(tgrad))), name
+
+
+def test_gradient_matches_central_differences_at_4096(psim):
+    # N = 4096, 200 steps: every parameter, q (the AO coefficients' range,
+    # the cutoff held) and the LJ epsilon and sigma included.  The pair
+    # forces jump at their cutoffs (the reference's AO soft core is cut at
+    # 1 + q), so the loss is only piecewise smooth: a step of 1e-7 relative
+    # keeps the +h and -h runs from differing by a pair crossing a cutoff,
+    # which at 1e-5 happens about twice per evaluation at this size.  Each
+    # forward run's smoothed g(r) is summed with atomics, so its loss carries
+    # ~1e-13 relative rounding noise; against the loss change of a 1e-7 step
+    # that bounds the agreement near 1e-4 (the exact comparison is the
+    # forward-mode tangent above).
+    from proteinsim2015_gb300 import adjoint as adj
+    g, pos, vel = setup(psim, n=4096, phi=0.15, seed=94)
+    a = adj.Adjoint(g, 200, dt=0.001, seed=23, checkpoint_every=50, sample_every=10, n_bins=100)
+    p, _ = _lj_params(adj)
+    pt, _ = _lj_params(adj, lj_epsilon=0.33, lj_sigma=1.03)
+    pt.ao_well_depth *= 1.1
+    target = a.forward(pt, pos, vel)
+    loss, _, grad, _ = a.gradient(p, pos, target, vel)
+    fds = []
+    for k, name in enumerate(adj.GRAD_NAMES):
+        v = getattr(p, name)
+        h = 1e-7 * abs(v)
+        qp, qm = adj.AdjointParams.from_buffer_copy(p), adj.AdjointParams.from_buffer_copy(p)
+        setattr(qp, name, v + h)
+        setattr(qm, name, v - h)
+        fd = (np.sum((a.forward(qp, pos, vel) - target) ** 2) -
+              np.sum((a.forward(qm, pos, vel) - target) ** 2)) / (2 * h)
+        fds.append((name, grad[k], fd, h))
+        print(name, grad[k], fd, abs(grad[k] - fd) / abs(fd))
+    a.close()
+    for name, gk, fd, h in fds:
+        assert gk == pytest.approx(fd, rel=5e-4, abs=1e-12 * loss / h), name
