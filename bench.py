@@ -538,8 +538,38 @@ def run_c0(psim, dev, steps=10000, cpu_budget_s=3.0):
     return out
 
 
+def profile_workload(args):
+    """A short run of one workload for a profiler capture; prints one JSON line."""
+    import proteinsim2015_gb300 as psim
+    dev = 0
+    if args.profile_workload == "batched":
+        # 64 of the 512 replicas: the same kernels on ~0.7 M particles, so a
+        # profiler's save and restore of device memory between passes stays small
+        out = run_batched(psim, dev, steps=args.steps, n_reps=64, tune=False)
+    elif args.profile_workload == "adjoint":
+        out = run_differentiable(psim, dev, steps=args.steps)
+    else:   # the 2^20 liquid in the plain FP64 form
+        w = workload()
+        n, box, scale = w["n"], w["box"], w["scale"]
+        g = psim.geometry(n, box, box / scale, scale)
+        p = psim.make_force("LJ", RC, kT=KT, well_depth=WD, lj_num=LJN, yukawa_strength=0.0)
+        s = psim.System(g, p, gamma=GAMMA, dt=DT, kT=KT, vel_freq=1000, seed=90210,
+                        precision=psim.PRECISION_FP64, device=dev)
+        s.upload(w["pos"], w["radius"], vel=w["vel"])
+        s.step(max(args.warmup, 1))
+        ms = s.time_steps(args.steps)
+        out = {"workload": "lj_rho0.8_N2^20_fp64", "value": n * args.steps / (ms * 1e-3),
+               "ms_per_step": ms / args.steps, "phases_ms": s.profile(2)}
+        s.close()
+    out["profile_only"] = True
+    print(json.dumps(out))
+    return 0
+
+
 def run_gpu(args):
     import proteinsim2015_gb300 as psim
+    if args.profile_only and args.profile_workload != "mixed":
+        return profile_workload(args)
     ws, rank, local = dist_env()
     dist = None
     if ws > 1:
@@ -731,6 +761,11 @@ def main():
                     help="pair-list skin of the mixed form (0: walk the 27 cells every step)")
     ap.add_argument("--profile-only", action="store_true",
                     help="time the mixed form and its phases only (short runs under ncu)")
+    ap.add_argument("--profile-workload", default="mixed",
+                    choices=["mixed", "fp64", "batched", "adjoint"],
+                    help="with --profile-only: the workload to run for --steps steps: the "
+                         "2^20 liquid in the mixed or the plain FP64 form, the 512 AO "
+                         "replicas with a pair list, or the differentiable trajectory")
     args = ap.parse_args()
     if args.cpu_baseline_json is not None:
         return cpu_baseline_child(args.cpu_baseline_json)
