@@ -296,6 +296,9 @@ def e2e_dropin(psim, w, state, min_steps=30, min_seconds=1.0):
     f = pinned(3 * n)
     hi, cse, srt = psim.cells_build(g, buf["pos"], rad, out=cells)
     t_cur = DT  # continue as a normal step
+    # one system stepped through the drop-ins: keep the force pass's pair list
+    # across calls (the library's default builds one per call)
+    psim.set_force_list_skin(-1.0)
     calls0, builds0 = psim.force_list_stats()
     n_steps = 0
     t0 = time.perf_counter()
@@ -316,6 +319,7 @@ def e2e_dropin(psim, w, state, min_steps=30, min_seconds=1.0):
     h2d = (32 * n + 8 * n + 8 * ncell) + (4 * 24 * n + 8 * n) + (24 * n + 8 * n)
     d2h = 24 * n + 4 * 24 * n + (8 * n + 8 * ncell + 32 * n)
     it.close()
+    psim.set_force_list_skin(0.0)
     lists = {"calls": calls1 - calls0, "builds": builds1 - builds0}
     return n * n_steps / el, h2d, d2h, lists, n_steps
 
@@ -381,6 +385,9 @@ def run_batched(psim, dev, steps=2000, n_reps=512, tune=True, skin=0.3):
                        precision=psim.PRECISION_MIXED, device=dev, skin=sk)
         b.upload(pos, np.full(b.n, 0.5), vel=vel)
         b.step(3)
+        lanes = None
+        if sk > 0 and tune:   # threads per particle of the list pass, on the live batch
+            lanes = batch.tune_lanes(b, steps=min(steps, 100))
         b0 = b.list_builds()
         ms = b.time_steps(steps)
         builds = b.list_builds() - b0
@@ -390,6 +397,9 @@ def run_batched(psim, dev, steps=2000, n_reps=512, tune=True, skin=0.3):
                "launches": steps * b.launches_per_step() + builds * b.launches_per_rebuild()}
         if sk > 0:
             out["list_builds"] = builds
+        if lanes:
+            out["lanes_per_particle"] = {"chosen": lanes[0],
+                                         "rates": {str(k): v for k, v in lanes[1].items()}}
         n = b.n
         b.close()
         return out, n
@@ -592,6 +602,10 @@ def run_gpu(args):
     # clocks are sampled every 100 ms over ~1.5 s of untimed steps of the same
     # workload and then over the timed steps, so the record covers the load
     # the timed steps run under
+    # threads per particle of the list force pass, tuned on the live system
+    # (untimed steps, part of the warm-up)
+    from proteinsim2015_gb300 import batch as _batch
+    lanes, lane_rates = _batch.tune_lanes(s, steps=200) if args.skin > 0 else (1, {})
     with ClockSampler(dev) as clk:
         s.time_steps(CLOCK_WINDOW_STEPS)
         builds0 = s.list_builds()
@@ -690,7 +704,7 @@ def run_gpu(args):
                    "cell_scale": scale, "cell_size": box / scale, "potential": "LJ 12-6 rc=2.5",
                    "kT": KT, "gamma": GAMMA, "dt": DT, "precision": "mixed",
                    "noise": "philox", "parallelism": "replicas" if ws > 1 else "single",
-                   "skin": args.skin, "pair_list": args.skin > 0,
+                   "skin": args.skin, "pair_list": args.skin > 0, "list_lanes": lanes,
                    "l2": "inputs larger than L2 (FP64 SoA state ~300 MB, sorted copies 32 MB)"},
         "plain_fp64": {"value": plain, "unit": UNIT, "steps": k64, "ms_per_step": ms64 / k64,
                        "force_ms": prof64["force_ms"]},
@@ -700,6 +714,7 @@ def run_gpu(args):
         "force_rel_err": ferr, "force_abs_err_max_over_rms_force": fmax,
         "phases_ms": {k: round(v, 5) for k, v in prof.items()},
         "pairs_per_particle": pairs,
+        "list_lanes_rates": {str(k): v for k, v in lane_rates.items()},
         "pair_list": {"skin": args.skin, "rebuilds": builds, "steps": steps_run,
                       "rebuild_every": (steps_run / builds) if builds else None},
         "e2e": {"value": e2e_v, "unit": UNIT, "h2d_bytes_per_step": h2d,

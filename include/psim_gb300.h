@@ -267,10 +267,13 @@ int psim_force_evaluate_plugin(psim_force_launch_fn launch, const psim_force_par
  * original index) has moved skin/2 since that build; it builds a new list
  * otherwise, and whenever n, the grid or the cutoff changed.  The forces are
  * those of this call's positions either way (every pair within cutOff is in
- * the list); only the FP32 summation order follows the list.  skin < 0
- * (default): the smaller of 0.4 and cellSize - cutOff, if at least 0.1, else
- * none; skin > 0: that skin, at most cellSize - cutOff; 0: a list of each
- * call's own pairs, built every call.  No counterpart in the reference. */
+ * the list); only the FP32 summation order follows the list.  skin 0
+ * (default): a list of each call's own pairs, built every call, so that a
+ * call depends on its arguments alone, as the reference's does; skin < 0:
+ * the smaller of 0.4 and cellSize - cutOff, if at least 0.1, else none;
+ * skin > 0: that skin, at most cellSize - cutOff.  A caller that steps one
+ * system through the drop-ins opts in to the kept list.  No counterpart in
+ * the reference. */
 int psim_force_set_list_skin(double skin);
 /* Mixed-precision psim_force_evaluate calls so far, and the pair lists they
  * built. */
@@ -540,6 +543,13 @@ int psim_system_rdf(psim_system* sys, double r_min, double r_max, int32_t n_bins
  * r_ij . f_ij / N (pressure = rho (kT + virial / 3)).  Single systems with a
  * library functor only (a plugin's energy is not known here). */
 int psim_system_energy(psim_system* sys, double* potential, double* virial);
+
+/* Threads per particle of the pair-list force pass (mixed form with a skin,
+ * compact records): 1 (default), 2 or 4.  The lanes of a particle walk every
+ * lanes-th group of its list and their sums are added in lane order, so the
+ * forces do not depend on the timing of the run; an autotuner picks the
+ * fastest (no reference counterpart). */
+int psim_system_set_list_lanes(psim_system* sys, int32_t lanes);
 
 /* Pair-list rebuilds since the upload (0 without a skin; the list the upload
  * builds is not counted). */

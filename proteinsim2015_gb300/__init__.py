@@ -154,6 +154,7 @@ def lib():
             "psim_system_tracked_displacement": ([P, C.POINTER(C.c_double)], C.c_int),
             "psim_system_interactions": ([P, C.c_double, P, C.POINTER(C.c_int64)], C.c_int),
             "psim_philox_noise": ([C.c_uint32, C.c_int32, C.c_int64, C.c_int32, P, C.c_int32], C.c_int),
+            "psim_system_set_list_lanes": ([P, C.c_int32], C.c_int),
             "psim_system_energy": ([P, C.POINTER(C.c_double), C.POINTER(C.c_double)], C.c_int),
             "psim_system_rdf": ([P, C.c_double, C.c_double, C.c_int32, P], C.c_int),
             "psim_system_clusters": ([P, C.c_double, C.c_int32, P, C.POINTER(C.c_int32),
@@ -430,7 +431,8 @@ def set_force_list_skin(skin=-1.0):
     """The pair-list skin of force_evaluate's mixed precision: the list is kept
     across calls while no particle has moved skin/2 since its build.  < 0:
     automatic (the smaller of 0.4 and cellSize - cutOff, if at least 0.1);
-    0: a list of each call's own pairs, built every call."""
+    0 (the library's default): a list of each call's own pairs, built every
+    call, so each call stands alone."""
     _check(lib().psim_force_set_list_skin(float(skin)))
 
 
@@ -632,6 +634,10 @@ class System:
         u, w = C.c_double(), C.c_double()
         _check(lib().psim_system_energy(self._h, C.byref(u), C.byref(w)))
         return u.value, w.value
+
+    def set_list_lanes(self, lanes):
+        """Threads per particle (1, 2 or 4) of the pair-list force pass."""
+        _check(lib().psim_system_set_list_lanes(self._h, int(lanes)))
 
     def list_builds(self):
         b = C.c_int32()

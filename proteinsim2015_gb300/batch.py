@@ -84,7 +84,8 @@ def size_bucket(d, cutoff, edges=(0.5, 1.0, 2.0)):
 
 def autotune(psim, draws, candidates=(1.0, 1.25, 1.5, 2.0), per_bucket=24, steps=40,
              dt=0.001, device=0, seed=7):
-    """Cell-size factor per size bucket, from timed sub-batches.
+    """Cell-size factor per size bucket, from timed sub-batches (the cell
+    walk; the pair-list pass's threads per particle: tune_lanes).
 
     For each bucket, up to ``per_bucket`` of its replicas (drawn with ``seed``)
     are batched at every candidate factor, warmed up, and timed over ``steps``
@@ -114,3 +115,20 @@ def autotune(psim, draws, candidates=(1.0, 1.25, 1.5, 2.0), per_bucket=24, steps
         report[b] = (best[b], rates)
     factors = [best[size_bucket(d, 1.0 + d["q"])] for d in draws]
     return factors, report
+
+
+def tune_lanes(system, candidates=(1, 2, 4), steps=100, warmup=5):
+    """Threads per particle of a system's pair-list force pass (a System or
+    Batch with a skin): each candidate is timed over ``steps`` steps of the
+    live system (after ``warmup`` steps that capture its graphs), the fastest
+    is kept set.  The steps advance the state, as warm-up steps do.  Returns
+    (lanes, {lanes: particle-steps/s})."""
+    rates = {}
+    for lanes in candidates:
+        system.set_list_lanes(lanes)
+        system.step(warmup)
+        ms = system.time_steps(steps)
+        rates[lanes] = system.n * steps / (ms * 1e-3)
+    best = max(rates, key=rates.get)
+    system.set_list_lanes(best)
+    return best, rates

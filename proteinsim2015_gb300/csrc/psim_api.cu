@@ -465,7 +465,9 @@ struct Workspace {
                    L == o.L && cs == o.cs && rc == o.rc && skin == o.skin;
         }
     } lkey;
-    double lskin = -1.0;        // the list's skin: < 0 automatic, 0 none
+    // the list's skin: 0 (default) none -- each call stands alone, as the
+    // reference's call does; < 0 automatic; > 0 that skin
+    double lskin = 0.0;
     long long lbuilds = 0, lcalls = 0;
 };
 Workspace g_ws;
@@ -1147,6 +1149,7 @@ struct psim_system {
     // slot (ping-pong with the order), positions at the build, entries,
     // counts, and the two step-parity rebuild flags
     bool list_on = false;
+    int list_lanes = 1;   // threads per particle of the list force pass (1, 2 or 4)
     double skin = 0.0;
     int lcap = 0, hcap = 0;
     float lpre = 0.f, ldisp2 = 0.f, hr = 0.f;
@@ -1257,6 +1260,7 @@ cudaError_t enqueue_force(psim_system* s, const Phase& ph, const ForceOut& fo) {
     if (s->n_reps && s->list_on) {   // each particle with its replica's pair functor
         PairList pl{nullptr, s->lpos.as<float4>(), s->lcount.as<int>(), s->list.as<uint32_t>(),
                     s->n, s->lcompact, s->lradius, s->lunit, s->b_rep.as<int>(), s->b_pairs.p};
+        pl.lanes = s->list_lanes;
         return launch_forces_list(s->fs, s->g, pl, fo, s->st);
     }
     if (s->n_reps) {
@@ -1271,6 +1275,7 @@ cudaError_t enqueue_force(psim_system* s, const Phase& ph, const ForceOut& fo) {
         // the storage order is the list order: no slot table
         PairList pl{nullptr, s->lpos.as<float4>(), s->lcount.as<int>(),
                     s->list.as<uint32_t>(), s->n, s->lcompact, s->lradius, s->lunit};
+        pl.lanes = s->list_lanes;
         return launch_forces_list(s->fs, s->g, pl, fo, s->st);
     }
     return launch_forces_mixed(s->fs, s->g, cv, fo, s->st);
@@ -2665,6 +2670,20 @@ int psim_system_rdf(psim_system* s, double r_min, double r_max, int32_t n_bins, 
         const double r0 = r_min + k * dr, r1 = r0 + dr;
         const double shell = 4.0 / 3.0 * M_PI * (r1 * r1 * r1 - r0 * r0 * r0);
         g_r[k] = s->n ? (double)h[(size_t)k] / (s->n * rho * shell) : 0.0;
+    }
+    return PSIM_OK;
+}
+
+int psim_system_set_list_lanes(psim_system* s, int32_t lanes) {
+    if (!s) return fail(PSIM_ERR_INPUT, "NULL system");
+    if (lanes != 1 && lanes != 2 && lanes != 4)
+        return fail(PSIM_ERR_INPUT, "lanes per particle must be 1, 2 or 4 (got %d)", lanes);
+    DeviceGuard dg(s->device);
+    int rc = settle(s);
+    if (rc) return rc;
+    if (lanes != s->list_lanes) {
+        drop_graphs(s);   // the captured steps hold the kernel of the old setting
+        s->list_lanes = lanes;
     }
     return PSIM_OK;
 }

@@ -250,6 +250,27 @@ struct MixedBody {
     __device__ __forceinline__ void list_overlap(float rmin, float s2, uint32_t& err) const {
         if (rmin < fminf(0.64f * s2, rc2f)) err |= EBIT_OVERLAP;
     }
+    // the sums `own` of another lane of the same particle (mask: that
+    // particle's lanes, src: the lane within its width-lane segment), added
+    // into a with compensation; every lane of the mask calls it with its own
+    // unmerged sums, and lane 0 keeps the result
+    __device__ __forceinline__ void merge_lane(Acc& a, const Acc& own, unsigned mask, int src,
+                                               int width) const {
+        const float t[6] = {__shfl_sync(mask, own.s0, src, width),
+                            __shfl_sync(mask, own.s1, src, width),
+                            __shfl_sync(mask, own.s2, src, width),
+                            __shfl_sync(mask, own.k0, src, width),
+                            __shfl_sync(mask, own.k1, src, width),
+                            __shfl_sync(mask, own.k2, src, width)};
+        const int c = __shfl_sync(mask, own.cnt, src, width);
+        kahan_add(a.s0, a.k0, t[0]);
+        kahan_add(a.s1, a.k1, t[1]);
+        kahan_add(a.s2, a.k2, t[2]);
+        kahan_add(a.s0, a.k0, -t[3]);
+        kahan_add(a.s1, a.k1, -t[4]);
+        kahan_add(a.s2, a.k2, -t[5]);
+        a.cnt += c;
+    }
     __device__ __forceinline__ void fold(Acc& a) const {
         kahan_add(a.s0, a.k0, a.p0);
         kahan_add(a.s1, a.k1, a.p1);
@@ -287,14 +308,17 @@ struct MixedBody {
             kahan_add(S1, C1, -f[4 * stride + t]);
             kahan_add(S2, C2, -f[5 * stride + t]);
         }
-        out.fx[i] = (double)S0 - (double)C0;
-        out.fy[i] = (double)S1 - (double)C1;
-        out.fz[i] = (double)S2 - (double)C2;
+        out.fx[i] = widen_f32(S0) - widen_f32(C0);
+        out.fy[i] = widen_f32(S1) - widen_f32(C1);
+        out.fz[i] = widen_f32(S2) - widen_f32(C2);
     }
+    // the compensated sum s - k formed in FP64 (exact: both parts fit 48
+    // bits); the floats are widened with integer operations, as the FP64
+    // unit that would convert them runs at 1/64 of the FP32 rate on GB300
     __device__ __forceinline__ void store(const ForceOut& out, int i, const Acc& a) const {
-        out.fx[i] = (double)a.s0 - (double)a.k0;
-        out.fy[i] = (double)a.s1 - (double)a.k1;
-        out.fz[i] = (double)a.s2 - (double)a.k2;
+        out.fx[i] = widen_f32(a.s0) - widen_f32(a.k0);
+        out.fy[i] = widen_f32(a.s1) - widen_f32(a.k1);
+        out.fz[i] = widen_f32(a.s2) - widen_f32(a.k2);
         if (out.coor) out.coor[i] = a.cnt;
     }
 };

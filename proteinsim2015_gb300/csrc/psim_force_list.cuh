@@ -266,8 +266,9 @@ __device__ __forceinline__ ListRec<false> load_rec(const float4* pos, uint32_t j
     return r;
 }
 
-// A thread per particle (current storage order f): its list slot, its list,
-// its neighbours' records; the force is stored at f.  The list is walked in
+// A thread per particle (current storage order f) -- or kLanes threads, each
+// walking every kLanes-th group of its list -- its list slot, its list, its
+// neighbours' records; the force is stored at f.  The list is walked in
 // batches of 4 entries (lists are padded to multiples of 8, kListFold).  Each
 // batch's records are loaded one batch ahead of its pair terms, and its list
 // entries -- streamed from DRAM -- one batch ahead of the records, so the
@@ -275,14 +276,27 @@ __device__ __forceinline__ ListRec<false> load_rec(const float4* pos, uint32_t j
 // the image the pair needs: no periodic arithmetic per pair.  A separation
 // is d = (x_j,hi - x_i,hi) + (x_j,lo - x_i,lo): the first difference is exact
 // for nearby values and the second comes out of the record's decode
-// (compact) or one subtraction (full), so d carries one FP32 rounding.
-template <class Body, bool kCompact, bool kReplicas, bool kCount = false>
+// (compact) or one subtraction (full), so d carries one FP32 rounding.  The
+// lanes of a particle are adjacent in one warp; lane 0 adds the others' sums
+// in lane order, so the result does not depend on scheduling.
+template <class Body, bool kCompact, bool kReplicas, bool kCount = false, int kLanes = 1>
 __global__ void __launch_bounds__(256)
 force_list_kernel(Body body0, DevGeom g, PairList pl, ForceOut out) {
     constexpr int kBatch = 4;
     static_assert(kListFold == 2 * kBatch, "a fold is two batches");
-    const int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= g.n || *out.err) return;
+    static_assert(kLanes == 1 || kLanes == 2 || kLanes == 4, "1, 2 or 4 lanes per particle");
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int f = t / kLanes;
+    const int lane = t % kLanes;
+    if (kLanes == 1) {
+        if (f >= g.n || *out.err) return;
+    } else {
+        // every lane of a particle must take the same path: the error word
+        // is read once per warp (all 32 threads are present here)
+        const bool failed =
+            __shfl_sync(0xffffffffu, (threadIdx.x & 31) == 0 ? (*out.err != 0) : false, 0);
+        if (failed || f >= g.n) return;   // f is the same for all lanes of a particle
+    }
     // a batch: the pair functor of the particle's replica (its neighbours are
     // all of the same replica)
     const Body body = kReplicas ? body0.for_replica(pl.pairs, pl.rep[f], g) : body0;
@@ -310,7 +324,9 @@ force_list_kernel(Body body0, DevGeom g, PairList pl, ForceOut out) {
     body.init(acc);
     uint32_t err = 0;
     float rmin = 3.0e38f;
-    const int cnt = pl.count[s];   // a multiple of kListFold
+    // this lane's groups: lane, lane + kLanes, ... of the particle's cnt / 8
+    const int groups = pl.count[s] / kListFold;
+    const int cnt = groups > lane ? (groups - lane + kLanes - 1) / kLanes * kListFold : 0;
     using Rec = ListRec<kCompact>;
     const Rec none{};
     auto terms = [&](const Rec* r) {
@@ -334,8 +350,9 @@ force_list_kernel(Body body0, DevGeom g, PairList pl, ForceOut out) {
     };
     // groups of 8 entries (one 32-byte load) one group ahead; records one
     // batch of 4 ahead of their pair terms
-    const uint4* gp = reinterpret_cast<const uint4*>(pl.list + (size_t)s * kListFold);
-    const size_t gstride = (size_t)pl.stride * kListFold / 4;   // uint4 per group row
+    const uint4* gp =
+        reinterpret_cast<const uint4*>(pl.list + ((size_t)lane * pl.stride + s) * kListFold);
+    const size_t gstride = (size_t)pl.stride * kListFold / 4 * kLanes;   // uint4 per step
     uint4 ea = make_uint4(0u, 0u, 0u, 0u), eb = ea;
     Rec r[kBatch], rn[kBatch];
     if (cnt > 0) {
@@ -364,38 +381,70 @@ force_list_kernel(Body body0, DevGeom g, PairList pl, ForceOut out) {
         body.fold(acc);
         eb = nb;
     }
+    if constexpr (kLanes > 1) {
+        // lane 0 adds the other lanes' sums in lane order
+        const unsigned seg = (threadIdx.x & 31) & ~(unsigned)(kLanes - 1);
+        const unsigned mask = ((1u << kLanes) - 1u) << seg;
+        const typename Body::Acc own = acc;
+#pragma unroll
+        for (int o = 1; o < kLanes; ++o) body.merge_lane(acc, own, mask, o, kLanes);
+#pragma unroll
+        for (int o = kLanes / 2; o > 0; o >>= 1) {
+            rmin = fminf(rmin, __shfl_xor_sync(mask, rmin, o, kLanes));
+            err |= __shfl_xor_sync(mask, err, o, kLanes);
+        }
+        if (lane != 0) return;
+    }
     if (kCompact) body.list_overlap(rmin, us2, err);
     body.store(out, f, acc);
     if (err) atomicOr(out.err, err);
+}
+
+// The list pass with `lanes` threads per particle (kMulti: the 2- and 4-lane
+// kernels are built for this variant; otherwise one lane).
+template <class Body, bool kCompact, bool kReplicas, bool kCount, bool kMulti>
+cudaError_t launch_list_lanes(const Body& body, const DevGeom& g, const PairList& pl,
+                              const ForceOut& out, int lanes, cudaStream_t st) {
+    if constexpr (kMulti) {
+        if (lanes == 2 || lanes == 4) {
+            const int blocks = (int)(((long long)g.n * lanes + 255) / 256);
+            if (lanes == 4)
+                force_list_kernel<Body, kCompact, kReplicas, kCount, 4>
+                    <<<blocks, 256, 0, st>>>(body, g, pl, out);
+            else
+                force_list_kernel<Body, kCompact, kReplicas, kCount, 2>
+                    <<<blocks, 256, 0, st>>>(body, g, pl, out);
+            return cudaGetLastError();
+        }
+    }
+    force_list_kernel<Body, kCompact, kReplicas, kCount, 1><<<(g.n + 255) / 256, 256, 0, st>>>(
+        body, g, pl, out);
+    return cudaGetLastError();
 }
 
 template <class Body>
 cudaError_t launch_force_list(const Body& body, const DevGeom& g, const PairList& pl,
                               const ForceOut& out, cudaStream_t st) {
     if (g.n == 0) return cudaSuccess;
-    const int blocks = (g.n + 255) / 256;
+    // several lanes per particle for compact records without the count; one
+    // lane otherwise
+    const int lanes = (pl.compact && !out.coor && (pl.lanes == 2 || pl.lanes == 4)) ? pl.lanes : 1;
     if (pl.rep) {
         if constexpr (Body::kBatchable) {
             if (pl.compact)
-                force_list_kernel<Body, true, true><<<blocks, 256, 0, st>>>(body, g, pl, out);
-            else
-                force_list_kernel<Body, false, true><<<blocks, 256, 0, st>>>(body, g, pl, out);
-            return cudaGetLastError();
+                return launch_list_lanes<Body, true, true, false, true>(body, g, pl, out, lanes, st);
+            return launch_list_lanes<Body, false, true, false, false>(body, g, pl, out, 1, st);
         }
         return cudaErrorInvalidValue;
     }
     if (out.coor) {   // the coordination numbers with the forces (one system)
         if (pl.compact)
-            force_list_kernel<Body, true, false, true><<<blocks, 256, 0, st>>>(body, g, pl, out);
-        else
-            force_list_kernel<Body, false, false, true><<<blocks, 256, 0, st>>>(body, g, pl, out);
-        return cudaGetLastError();
+            return launch_list_lanes<Body, true, false, true, false>(body, g, pl, out, 1, st);
+        return launch_list_lanes<Body, false, false, true, false>(body, g, pl, out, 1, st);
     }
     if (pl.compact)
-        force_list_kernel<Body, true, false><<<blocks, 256, 0, st>>>(body, g, pl, out);
-    else
-        force_list_kernel<Body, false, false><<<blocks, 256, 0, st>>>(body, g, pl, out);
-    return cudaGetLastError();
+        return launch_list_lanes<Body, true, false, false, true>(body, g, pl, out, lanes, st);
+    return launch_list_lanes<Body, false, false, false, false>(body, g, pl, out, 1, st);
 }
 
 }  // namespace psim

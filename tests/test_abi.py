@@ -139,7 +139,7 @@ def test_force_list_settings_need_no_gpu(psim):
     # the drop-in pair list's skin and counters are host state: settable and
     # readable without a device; a NaN skin is refused
     psim.set_force_list_skin(0.25)
-    psim.set_force_list_skin(-1.0)
+    psim.set_force_list_skin(0.0)
     with pytest.raises(psim.PsimError) as e:
         psim.set_force_list_skin(float("nan"))
     assert e.value.code == psim.ERR_INPUT

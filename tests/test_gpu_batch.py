@@ -114,3 +114,30 @@ def test_batch_pair_list_needs_room(psim):
     with pytest.raises(psim.PsimError) as e:
         psim.Batch([(g, f, 1)], skin=g.cell_size)   # cellSize < cutOff + skin
     assert e.value.code == psim.ERR_INPUT
+
+
+def test_batch_list_lanes_and_tuner(psim):
+    # the batched list pass with 1, 2 and 4 threads per particle, and the
+    # tuner that picks one on the live batch
+    from proteinsim2015_gb300 import batch
+    skin = 0.2
+    reps, states = [], []
+    for k, (n, phi, a, q) in enumerate(REPLICAS):
+        g0, f, pos = ao_replica(psim, n, phi, a, q, seed=70 + k)
+        box = g0.box_size
+        scale = max(3, int(np.floor(box / (f.cutoff + skin))))
+        reps.append((psim.geometry(n, box, box / scale, scale), f, 2000 + 13 * k))
+        states.append(pos)
+    b = psim.Batch(reps, gamma=1.0, dt=0.001, kT=1.0, vel_freq=7, skin=skin)
+    b.upload(np.concatenate(states), np.full(b.n, 0.5))
+    forces = {}
+    for lanes in (1, 2, 4):
+        b.set_list_lanes(lanes)
+        forces[lanes] = b.forces()
+    for lanes in (2, 4):
+        assert np.linalg.norm(forces[lanes] - forces[1]) < 1e-6 * np.linalg.norm(forces[1])
+    best, rates = batch.tune_lanes(b, steps=20, warmup=2)
+    assert best in (1, 2, 4) and set(rates) == {1, 2, 4} and all(r > 0 for r in rates.values())
+    b.close()
+    with pytest.raises(psim.PsimError):
+        psim.System(reps[0][0], reps[0][1]).set_list_lanes(3)

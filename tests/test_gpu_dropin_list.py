@@ -18,7 +18,7 @@ KT = 1.5
 def skin_reset(psim):
     psim.set_force_list_skin(-1.0)
     yield
-    psim.set_force_list_skin(-1.0)
+    psim.set_force_list_skin(0.0)   # the library's default: each call stands alone
 
 
 def liquid(psim, seed=60):

@@ -167,3 +167,27 @@ def test_pairlist_with_unequal_radii(psim):
     d = got["pos"] - ref["pos"]
     d -= g.box_size * np.round(d / g.box_size)
     assert np.max(np.abs(d)) < 1e-6
+
+
+@pytest.mark.parametrize("lanes", [2, 4])
+def test_lanes_per_particle_give_the_same_forces(psim, lanes):
+    # the list pass with 2 or 4 threads per particle: the same pair terms, the
+    # lanes' Kahan sums added in lane order -- against the one-lane pass and
+    # FP64 within the mixed form's tolerance, and reproducible run to run
+    g, p, pos, rad = lj_liquid(psim)
+    f64 = psim.System(g, p, precision=0)
+    f64.upload(pos, rad)
+    ref = f64.forces()
+    f64.close()
+    s = psim.System(g, p, precision=1, skin=0.4)
+    s.upload(pos, rad)
+    one = s.forces()
+    s.set_list_lanes(lanes)
+    many = s.forces()
+    again = s.forces()
+    assert np.array_equal(many, again)
+    assert rel_norm(many, ref) < 1e-5 and rel_norm(many, one) < 1e-6
+    # stepping: graphs captured with the new setting
+    s.step(20)
+    assert np.all(np.isfinite(s.download()["pos"]))
+    s.close()
