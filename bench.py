@@ -603,11 +603,14 @@ def run_gpu(args):
     # workload and then over the timed steps, so the record covers the load
     # the timed steps run under
     # threads per particle of the list force pass, tuned on the live system
-    # (untimed steps, part of the warm-up)
+    # (untimed steps, part of the warm-up); a profile-only run stays short:
+    # one lane, no clock window
     from proteinsim2015_gb300 import batch as _batch
-    lanes, lane_rates = _batch.tune_lanes(s, steps=200) if args.skin > 0 else (1, {})
+    tune = args.skin > 0 and not args.profile_only
+    lanes, lane_rates = _batch.tune_lanes(s, steps=200) if tune else (1, {})
     with ClockSampler(dev) as clk:
-        s.time_steps(CLOCK_WINDOW_STEPS)
+        if not args.profile_only:
+            s.time_steps(CLOCK_WINDOW_STEPS)
         builds0 = s.list_builds()
         ms = s.time_steps(args.steps)
         builds_timed = s.list_builds() - builds0
