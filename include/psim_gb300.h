@@ -136,7 +136,7 @@ typedef struct {
  * potential needs no rebuild of the library.  It returns 0 or a PSIM_ERR_*
  * code (PSIM_ERR_CUDA for a failed launch); physical errors (overlap,
  * non-finite force) are latched in *err as the library's own passes do. */
-#define PSIM_FORCE_ABI 1
+#define PSIM_FORCE_ABI 2
 typedef enum {
     PSIM_PASS_FP64 = 0,   /* plain FP64 form, 27-cell walk over pos_fp64 */
     PSIM_PASS_MIXED = 1,  /* FP32 pairs + Kahan sums, 27-cell walk over pos_hi/pos_lo */
@@ -167,7 +167,7 @@ typedef struct {
     int32_t list_stride;
     int32_t list_compact;
     float list_radius;                /* the one radius of compact records */
-    float list_lo_unit;               /* unit of compact records' low parts */
+    float list_unit;                  /* unit 2^-k of compact records' fixed-point coordinates */
     /* output, in the pass's order (sorted or list order) */
     double* fx;
     double* fy;

@@ -26,6 +26,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libpsim_gb300.so")
 PLUGIN_DIR = os.path.join(HERE, "plugins")
+# PSIM_FORCE_ABI of include/psim_gb300.h: the device entry a plugin exports
+FORCE_ABI = 2
 
 OK = 0
 ERR_LOAD = 100
@@ -329,7 +331,7 @@ class ForcePlugin:
         for sym in ("getForce", "psim_plugin_abi", "psim_plugin_params", "psim_force_launch"):
             if not hasattr(self.lib, sym):
                 raise PsimError(ERR_LOAD, "could not find symbol %s in %s" % (sym, path))
-        if self.lib.psim_plugin_abi() != 1:
+        if self.lib.psim_plugin_abi() != FORCE_ABI:
             raise PsimError(ERR_LOAD, "%s was built for another device-entry ABI" % path)
         fn = self.lib.psim_plugin_params
         fn.argtypes = [C.c_char_p, C.POINTER(ForceParams)]

@@ -157,6 +157,16 @@ double max_cutoff(const psim_force_params* p) {
     return p->kind == 4 ? std::max(p->cutoff, p->cutoff2) : p->cutoff;
 }
 
+// The unit 2^-k of compact list records (compact_record).  A listed pair is
+// within rc + skin at the build and each particle moves less than skin / 2
+// before the next one, so separations stay below B = rc + 2 skin + 1; k is
+// the largest with 2 B 2^k <= 2^31, so that the integer difference of two
+// coordinates never wraps (B < 2^(ilogb(B) + 1)).
+float fixed_unit(double rc, double skin) {
+    const double B = rc + 2.0 * skin + 1.0;
+    return (float)std::ldexp(1.0, std::ilogb(B) + 2 - 31);
+}
+
 int make_geom(const psim_geometry* gm, double rc_max, DevGeom* g) {
     if (!gm) return fail(PSIM_ERR_INPUT, "geometry is NULL");
     if (gm->n_particles < 0) return fail(PSIM_ERR_INPUT, "negative particle count");
@@ -293,7 +303,7 @@ struct ForceRunner {
             a.list_stride = pl->stride;
             a.list_compact = pl->compact;
             a.list_radius = pl->radius;
-            a.list_lo_unit = pl->lo_unit;
+            a.list_unit = pl->unit;
         }
         a.fx = out.fx;
         a.fy = out.fy;
@@ -514,7 +524,7 @@ int ws_begin(Workspace& w) {
 
 extern "C" {
 
-int psim_abi_version(void) { return 3; }
+int psim_abi_version(void) { return 4; }
 
 // Lets other translation units of this library report through
 // psim_last_error_string (not part of the public header).
@@ -807,8 +817,7 @@ int force_evaluate(psim_force_launch_fn plugin, const psim_force_params* params,
         w.lkey.valid = false;
         const bool compact = hflags[1] == 0;
         const float R = compact ? (float)sorted[3] : 0.f;
-        const double M = g.L + 2.0 * (rcm + skin) + 1.0;   // bounds every record coordinate
-        const float unit = (float)std::ldexp(1.0, std::ilogb(M) - 31);
+        const float unit = fixed_unit(rcm, skin);
         const size_t rec = compact ? 16 : 32;
         PSIM_CUDA(w.lpos.ensure(rec * (n + 1 + (size_t)z.hcap)));
         PSIM_CUDA(w.lhalo.ensure(4 * n));
@@ -817,10 +826,12 @@ int force_evaluate(psim_force_launch_fn plugin, const psim_force_params* params,
         PSIM_CUDA(w.lcount.ensure(4 * n));
         PSIM_CUDA(w.lslot_of.ensure(4 * n));
         PSIM_CUDA(cudaMemsetAsync(w.lhcount.p, 0, 4, st));
-        // the ghost record that pads the lists, far from every particle
-        static const float4 ghost[2] = {make_float4(1e18f, 1e18f, 1e18f, 0.f),
-                                        make_float4(0.f, 0.f, 0.f, 0.f)};
-        PSIM_CUDA(cudaMemcpyAsync(w.lpos.as<char>() + rec * n, ghost, rec,
+        // the ghost record that pads the lists, out of range of every particle
+        static const float4 ghost_full[2] = {make_float4(1e18f, 1e18f, 1e18f, 0.f),
+                                             make_float4(0.f, 0.f, 0.f, 0.f)};
+        static const float4 ghost_compact = make_float4(0.f, 0.f, 0.f, kGhostBias);
+        PSIM_CUDA(cudaMemcpyAsync(w.lpos.as<char>() + rec * n,
+                                  compact ? &ghost_compact : ghost_full, rec,
                                   cudaMemcpyHostToDevice, st));
         PSIM_CUDA(launch_list_records(g.n, w.posh.as<float4>(), w.posl.as<float4>(),
                                       w.lpos.as<float4>(), w.lhalo.as<int>(),
@@ -1171,9 +1182,9 @@ struct psim_system {
     int n_reps = 0, n_tasks = 0;
     DevBuf b_tasks, b_geoms, b_pairs, b_pre, b_rep, b_seeds;
     // a batch with a pair list: per replica the list radius squared and the
-    // halo radius; the largest box and cutoff (the compact records' unit)
+    // halo radius; the largest cutoff (the compact records' unit)
     DevBuf b_lpre, b_hr;
-    double lmaxL = 0.0, lmaxrc = 0.0;
+    double lmaxrc = 0.0;
     // displacement tracker: box images crossed per particle and the start
     // positions (original order), counted by the integrator once started
     DevBuf img, track_start;
@@ -1874,7 +1885,6 @@ psim_system* psim_batch_create_list(const psim_replica* reps, int32_t n_reps,
             pre_max = std::max(pre_max, z.pre);
             lpre[(size_t)r] = z.pre;
             hr[(size_t)r] = z.hr;
-            s->lmaxL = std::max(s->lmaxL, geoms[r].L);
             s->lmaxrc = std::max(s->lmaxrc, max_cutoff(&reps[r].force));
         }
         s->lcap = cap;
@@ -2138,19 +2148,17 @@ int psim_system_upload(psim_system* s, const double* pos, const double* pos0, co
     ca.posl = s->cfg.precision == PSIM_PRECISION_MIXED ? s->posl.as<float4>() : nullptr;
     if (s->list_on) {
         // compact records when all radii are equal; the ghost record n that
-        // pads the lists lies far from every particle (zero low parts)
+        // pads the lists is out of range of every particle (far away for
+        // full records, an r^2 bias for compact ones)
         int compact = n > 0 ? 1 : 0;
         for (int i = 1; i < n && compact; ++i) compact = radius[i] == radius[0];
         const float R = n > 0 ? (float)radius[0] : 0.f;
         if (compact != s->lcompact || R != s->lradius) drop_graphs(s);
         s->lcompact = compact;
         s->lradius = R;
-        // low-part unit: |lo| of a record stays below the last place of its
-        // high part, or ~2x that after a halo shift; M bounds every coordinate
-        const double M = s->n_reps ? s->lmaxL + 2.0 * (s->lmaxrc + s->skin) + 1.0
-                                   : s->g.L + 2.0 * (max_cutoff(&s->cfg.force) + s->skin) + 1.0;
-        s->lunit = (float)std::ldexp(1.0, std::ilogb(M) - 31);
-        const float4 ghost[2] = {make_float4(1e18f, 1e18f, 1e18f, compact ? 0.f : R),
+        s->lunit = fixed_unit(s->n_reps ? s->lmaxrc : max_cutoff(&s->cfg.force), s->skin);
+        const float4 ghost[2] = {compact ? make_float4(0.f, 0.f, 0.f, kGhostBias)
+                                         : make_float4(1e18f, 1e18f, 1e18f, R),
                                  make_float4(0.f, 0.f, 0.f, 0.f)};
         float4* grec = s->lpos.as<float4>() + (compact ? 1 : 2) * (size_t)n;
         PSIM_CUDA(cudaMemcpyAsync(grec, ghost, compact ? 16 : 32, cudaMemcpyHostToDevice, st));

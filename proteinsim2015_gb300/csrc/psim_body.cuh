@@ -229,11 +229,13 @@ struct MixedBody {
     // the pair-list pass: one entry at separation d (the float-pair difference
     // already formed), masked by the cutoff.  kUniform: every pair has the
     // contact diameter `size` (s2 = size^2), and the overlap test runs once
-    // per particle on the smallest r^2 (rmin); otherwise per pair.
+    // per particle on the smallest r^2 (rmin); otherwise per pair.  bias is
+    // added to r^2: 0, or the compact ghost record's kGhostBias.
     template <bool kUniform, bool kCount = false>
     __device__ __forceinline__ void eval_list(float d0, float d1, float d2, float size, float s2,
-                                              Acc& a, float& rmin, uint32_t& err) const {
-        const float r2 = d0 * d0 + d1 * d1 + d2 * d2;
+                                              Acc& a, float& rmin, uint32_t& err,
+                                              float bias = 0.f) const {
+        const float r2 = fmaf(d0, d0, fmaf(d1, d1, fmaf(d2, d2, bias)));
         if (kCount) a.cnt += r2 < cont2f ? 1 : 0;
         const bool in = r2 < rc2f;
         const float fr = list_fr32(pf, r2, size, s2);

@@ -197,26 +197,34 @@ __device__ __forceinline__ void halo_shift(uint32_t flags, int num, int sh[3]) {
 }
 // ------------------------------------------------- pair-list position records
 // A full record is 32 bytes: {x, y, z, R} high parts and the low parts.  When
-// every particle has the same radius a compact 16-byte record suffices: the
-// high parts and, in .w, each low part as a 10-bit code in units of lo_unit
-// (code - 512) * lo_unit, lo_unit = U / 1024 with U twice the last place of
-// the largest coordinate a record can hold, so |lo| < U / 2 always.  The
-// code is exact to lo_unit / 2 -- ~7e-9 for a 109-wide box -- an absolute
-// error far under the FP32 rounding of a pair separation.
-__device__ __forceinline__ uint32_t lo_code(float lo, float inv_unit) {
-    const int q = __float2int_rn(lo * inv_unit) + 512;
-    return (uint32_t)(q < 0 ? 0 : (q > 1023 ? 1023 : q));
+// every particle has the same radius a compact 16-byte record suffices: each
+// coordinate as a 32-bit fixed-point number, the position in units of
+// unit = 2^-k rounded to the nearest and taken modulo 2^32, and in .w an r^2
+// bias (0; the ghost record's is kGhostBias, which puts it out of range of
+// every particle).  k is chosen so that every separation a list can hold is
+// below 2^31 units: the separation of two records is then the exact integer
+// difference of their coordinates (wrapping modulo 2^32 cancels), and one
+// conversion to FP32 and a power-of-two scale make it a float with a single
+// rounding.  Each coordinate is within one unit of the position (unit
+// 2^-27 ~ 7.5e-9 for LJ rc 2.5 with skin 0.4, fixed_unit).
+constexpr float kGhostBias = 1e30f;
+__device__ __forceinline__ uint32_t fixed_coord(float h, float l, float inv_unit) {
+    // h 2^k is exact (a power-of-two scale) and an integer for |h| >= 2^(24-k);
+    // the low part adds its rounded share
+    const long long a = __float2ll_rn(h * inv_unit);
+    const long long b = (long long)__float2int_rn(l * inv_unit);
+    return (uint32_t)(unsigned long long)(a + b);
 }
 __device__ __forceinline__ float4 compact_record(const float4& h, const float4& l,
                                                  float inv_unit) {
-    const uint32_t w = lo_code(l.x, inv_unit) | (lo_code(l.y, inv_unit) << 10) |
-                       (lo_code(l.z, inv_unit) << 20);
-    return make_float4(h.x, h.y, h.z, __uint_as_float(w));
+    return make_float4(__uint_as_float(fixed_coord(h.x, l.x, inv_unit)),
+                       __uint_as_float(fixed_coord(h.y, l.y, inv_unit)),
+                       __uint_as_float(fixed_coord(h.z, l.z, inv_unit)), 0.f);
 }
-// 2^23 + code as a float, so that fma(magic, unit, -(2^23 + 512) unit) is the
-// low part exactly
-__device__ __forceinline__ float lo_magic(uint32_t code) {
-    return __uint_as_float(0x4B000000u | code);
+// The separation coordinate b - a of two compact-record coordinates (raw
+// bits), in length units: the integer difference, converted and scaled.
+__device__ __forceinline__ float fixed_sep(float b, uint32_t a, float unit) {
+    return (float)(int)(__float_as_uint(b) - a) * unit;
 }
 // record `slot` of a full (inv_unit == 0) or compact record array
 __device__ __forceinline__ void store_record(float4* pos, float inv_unit, size_t slot,

@@ -274,9 +274,10 @@ __device__ __forceinline__ ListRec<false> load_rec(const float4* pos, uint32_t j
 // entries -- streamed from DRAM -- one batch ahead of the records, so the
 // latency of both overlaps the terms of the batch before.  Every record holds
 // the image the pair needs: no periodic arithmetic per pair.  A separation
-// is d = (x_j,hi - x_i,hi) + (x_j,lo - x_i,lo): the first difference is exact
-// for nearby values and the second comes out of the record's decode
-// (compact) or one subtraction (full), so d carries one FP32 rounding.  The
+// is, for compact records, the exact integer difference of the fixed-point
+// coordinates, converted and scaled by a power of two (fixed_sep); for full
+// records d = (x_j,hi - x_i,hi) + (x_j,lo - x_i,lo), the first difference
+// exact for nearby values.  Either way d carries one FP32 rounding.  The
 // lanes of a particle are adjacent in one warp; lane 0 adds the others' sums
 // in lane order, so the result does not depend on scheduling.
 template <class Body, bool kCompact, bool kReplicas, bool kCount = false, int kLanes = 1>
@@ -302,19 +303,16 @@ force_list_kernel(Body body0, DevGeom g, PairList pl, ForceOut out) {
     const Body body = kReplicas ? body0.for_replica(pl.pairs, pl.rep[f], g) : body0;
     const int s = pl.lslot ? pl.lslot[f] : f;   // no slot table: storage order is list order
     float4 hh, hl;
-    // compact records: a neighbour's low part minus the home's comes out of one
-    // FMA per axis, fma(2^23 + code, unit, c) with c = -(2^23 + 512) unit - l_i
-    float cx = 0.f, cy = 0.f, cz = 0.f;
-    const float unit = pl.lo_unit;
+    // compact records: the home's fixed-point coordinates
+    uint32_t ux = 0u, uy = 0u, uz = 0u;
+    const float unit = pl.unit;
     if (kCompact) {
         const float4 c = pl.pos[s];
-        const uint32_t w = __float_as_uint(c.w);
-        const float nb = -8389120.0f * unit;   // -(2^23 + 512) unit, exact
-        cx = nb - fmaf(lo_magic(w & 1023u), unit, nb);
-        cy = nb - fmaf(lo_magic((w >> 10) & 1023u), unit, nb);
-        cz = nb - fmaf(lo_magic((w >> 20) & 1023u), unit, nb);
-        hh = make_float4(c.x, c.y, c.z, pl.radius);
-        hl = make_float4(0.f, 0.f, 0.f, 0.f);
+        ux = __float_as_uint(c.x);
+        uy = __float_as_uint(c.y);
+        uz = __float_as_uint(c.z);
+        hh = make_float4(0.f, 0.f, 0.f, pl.radius);
+        hl = hh;
     } else {
         hh = pl.pos[2 * (size_t)s];
         hl = pl.pos[2 * (size_t)s + 1];
@@ -333,11 +331,11 @@ force_list_kernel(Body body0, DevGeom g, PairList pl, ForceOut out) {
 #pragma unroll
         for (int u = 0; u < kBatch; ++u) {
             if constexpr (kCompact) {
-                const uint32_t w = __float_as_uint(r[u].h.w);
-                const float d0 = (r[u].h.x - hh.x) + fmaf(lo_magic(w & 1023u), unit, cx);
-                const float d1 = (r[u].h.y - hh.y) + fmaf(lo_magic((w >> 10) & 1023u), unit, cy);
-                const float d2 = (r[u].h.z - hh.z) + fmaf(lo_magic((w >> 20) & 1023u), unit, cz);
-                body.template eval_list<true, kCount>(d0, d1, d2, usize, us2, acc, rmin, err);
+                const float d0 = fixed_sep(r[u].h.x, ux, unit);
+                const float d1 = fixed_sep(r[u].h.y, uy, unit);
+                const float d2 = fixed_sep(r[u].h.z, uz, unit);
+                body.template eval_list<true, kCount>(d0, d1, d2, usize, us2, acc, rmin, err,
+                                                      r[u].h.w);
             } else {
                 const float d0 = (r[u].h.x - hh.x) + (r[u].l.x - hl.x);
                 const float d1 = (r[u].h.y - hh.y) + (r[u].l.y - hl.y);
@@ -353,16 +351,18 @@ force_list_kernel(Body body0, DevGeom g, PairList pl, ForceOut out) {
     const uint4* gp =
         reinterpret_cast<const uint4*>(pl.list + ((size_t)lane * pl.stride + s) * kListFold);
     const size_t gstride = (size_t)pl.stride * kListFold / 4 * kLanes;   // uint4 per step
+    // past the list's end the entries read as slot 0, a valid record: the
+    // record loads need no condition
     uint4 ea = make_uint4(0u, 0u, 0u, 0u), eb = ea;
     Rec r[kBatch], rn[kBatch];
     if (cnt > 0) {
         ea = __ldg(gp);
         eb = __ldg(gp + 1);
     }
-    r[0] = cnt > 0 ? load_rec(pl.pos, ea.x, none) : none;
-    r[1] = cnt > 0 ? load_rec(pl.pos, ea.y, none) : none;
-    r[2] = cnt > 0 ? load_rec(pl.pos, ea.z, none) : none;
-    r[3] = cnt > 0 ? load_rec(pl.pos, ea.w, none) : none;
+    r[0] = load_rec(pl.pos, ea.x, none);
+    r[1] = load_rec(pl.pos, ea.y, none);
+    r[2] = load_rec(pl.pos, ea.z, none);
+    r[3] = load_rec(pl.pos, ea.w, none);
     for (int k0 = 0; k0 < cnt; k0 += kListFold) {
         const bool more = k0 + kListFold < cnt;
         gp += gstride;
@@ -373,10 +373,10 @@ force_list_kernel(Body body0, DevGeom g, PairList pl, ForceOut out) {
         rn[2] = load_rec(pl.pos, eb.z, none);
         rn[3] = load_rec(pl.pos, eb.w, none);
         terms(r);
-        r[0] = more ? load_rec(pl.pos, na.x, none) : none;
-        r[1] = more ? load_rec(pl.pos, na.y, none) : none;
-        r[2] = more ? load_rec(pl.pos, na.z, none) : none;
-        r[3] = more ? load_rec(pl.pos, na.w, none) : none;
+        r[0] = load_rec(pl.pos, na.x, none);
+        r[1] = load_rec(pl.pos, na.y, none);
+        r[2] = load_rec(pl.pos, na.z, none);
+        r[3] = load_rec(pl.pos, na.w, none);
         terms(rn);
         body.fold(acc);
         eb = nb;

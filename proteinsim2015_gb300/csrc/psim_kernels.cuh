@@ -80,15 +80,15 @@ struct PairList {
     const int* lslot;      // list slot of each current storage slot (null: the same slot)
     // list order, unwrapped, one record per slot (+ the ghost slot n and the
     // halo records): full, pos[2 s] = {x, y, z, R} high parts and pos[2 s + 1]
-    // the low parts; or compact (one float4, compact_record, low parts in
-    // units of lo_unit) when every particle has the radius `radius`
+    // the low parts; or compact (one float4, compact_record: fixed-point
+    // coordinates in units of `unit`) when every particle has the radius `radius`
     const float4* pos;
     const int* count;      // entries of each list slot (a multiple of kListFold)
     const uint32_t* list;
     int stride;
     int compact;
     float radius;
-    float lo_unit;
+    float unit;            // compact records: the fixed-point unit 2^-k (compact_record)
     // a batch of replicas (rep null: one system): each storage slot's replica
     // and the replicas' pair functors
     const int* rep;
@@ -182,7 +182,7 @@ struct VgbSystemArgs {
     const int* lslot;
     const float4* lbuild;       // list order: positions at the build, .w radius
     float4* lpos;               // PairList::pos
-    float linv_unit;            // 1 / PairList::lo_unit (compact), or 0 (full records)
+    float linv_unit;            // 1 / PairList::unit (compact), or 0 (full records)
     int* lflag_set;
     int* lflag_clear;
     float ldisp2;
@@ -292,7 +292,7 @@ struct CanonArgs {
     int* lslot_out;
     float4* lbuild;
     float4* lpos;           // PairList::pos, written with posh/posl
-    float linv_unit;        // 1 / PairList::lo_unit (compact), or 0 (full records)
+    float linv_unit;        // 1 / PairList::unit (compact), or 0 (full records)
     // halo records of the particles within hr of a face (rebuild only):
     // lhalo per slot, records n + 1 + [0, hcap) handed out by *lhcount
     int* lhalo;

@@ -90,7 +90,7 @@ int plugin_launch_mixed(const Pair& p, const psim_force_args* a, cudaStream_t st
         pl.stride = a->list_stride;
         pl.compact = a->list_compact;
         pl.radius = a->list_radius;
-        pl.lo_unit = a->list_lo_unit;
+        pl.unit = a->list_unit;
         return plugin_status(launch_force_list(body, g, pl, out, st));
     }
     const CellView cv = plugin_cells(a);

@@ -31,7 +31,7 @@ def test_library_exports_every_declared_symbol(psim):
 
 
 def test_abi_version_and_no_device_is_reported(psim):
-    assert psim.lib().psim_abi_version() == 3
+    assert psim.lib().psim_abi_version() == 4
     if psim.device_count() == 0:
         g = psim.geometry(4, 12, 3, 4)
         with pytest.raises(psim.PsimError) as e:

@@ -43,7 +43,7 @@ def test_plugin_exports_factory_and_device_entry(psim, name):
     for sym in ("getForce", "psim_plugin_abi", "psim_plugin_device_params", "psim_force_launch",
                 "psim_plugin_params"):
         assert hasattr(lib, sym), sym
-    assert lib.psim_plugin_abi() == 1
+    assert lib.psim_plugin_abi() == 2
     plug = psim.ForcePlugin(os.path.join(psim.PLUGIN_DIR, name + ".so"))
     assert plug.launch and plug.params.cutoff > 0
 
