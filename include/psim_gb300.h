@@ -545,10 +545,10 @@ int psim_system_rdf(psim_system* sys, double r_min, double r_max, int32_t n_bins
 int psim_system_energy(psim_system* sys, double* potential, double* virial);
 
 /* Threads per particle of the pair-list force pass (mixed form with a skin,
- * compact records): 1 (default), 2 or 4.  The lanes of a particle walk every
- * lanes-th group of its list and their sums are added in lane order, so the
- * forces do not depend on the timing of the run; an autotuner picks the
- * fastest (no reference counterpart). */
+ * compact records): 1 (default), 2 or 4.  Each lane of a particle takes its
+ * 8 / lanes entries of every group of 8 list entries, and the lanes' sums are
+ * added in lane order, so the forces do not depend on the timing of the run;
+ * an autotuner picks the fastest (no reference counterpart). */
 int psim_system_set_list_lanes(psim_system* sys, int32_t lanes);
 
 /* Pair-list rebuilds since the upload (0 without a skin; the list the upload

@@ -45,8 +45,8 @@ namespace psim {
 // run is sorted by x too, and two binary searches cut it to the particles
 // within the row's x reach of the home: about 250 candidates per particle
 // instead of about 410 at cellSize ~ rc + skin.
-// Lists are padded to a multiple of kListFold with the ghost record, a
-// far-away dummy particle, so the force pass reads whole batches.
+// Lists are padded to a multiple of kListFold with the ghost record, a dummy
+// out of range of every particle, so the force pass reads whole batches.
 // st.global of v at p when w holds; no branch around it
 __device__ __forceinline__ void store_if(uint32_t* p, uint32_t v, bool w) {
     asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %2, 0;\n\t@q st.global.u32 [%0], %1;\n\t}"
@@ -245,6 +245,15 @@ __device__ __forceinline__ void load_record(const float4* pos, uint32_t j, float
         : "l"(a));
 }
 
+// One group of kListFold = 8 list entries (32 bytes, 32-byte aligned) in a
+// single 256-bit load through the read-only path: a warp's request covers
+// its 1 KB once, where two 128-bit loads would each cover all of it.
+__device__ __forceinline__ void load_group(const uint32_t* p, uint4& a, uint4& b) {
+    asm("ld.global.nc.v8.u32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=r"(a.x), "=r"(a.y), "=r"(a.z), "=r"(a.w), "=r"(b.x), "=r"(b.y), "=r"(b.z), "=r"(b.w)
+        : "l"(p));
+}
+
 // A neighbour record as the force pass holds it between its load and its
 // pair term: one float4 (compact) or the high and low halves (full).
 template <bool kCompact>
@@ -266,10 +275,15 @@ __device__ __forceinline__ ListRec<false> load_rec(const float4* pos, uint32_t j
     return r;
 }
 
-// A thread per particle (current storage order f) -- or kLanes threads, each
-// walking every kLanes-th group of its list -- its list slot, its list, its
-// neighbours' records; the force is stored at f.  The list is walked in
-// batches of 4 entries (lists are padded to multiples of 8, kListFold).  Each
+// A thread per particle (current storage order f) -- or kLanes threads, lane
+// l taking entries [l E, (l + 1) E) of every group of 8 (E = 8 / kLanes) --
+// its list slot, its list, its neighbours' records; the force is stored at f.
+// With several lanes a warp covers 32 / kLanes particles, mostly of one cell,
+// whose entries at the same place of their lists lie close together in the
+// same rows of cells: fewer L1 wavefronts per record gather, and the lanes of
+// a particle do equal work.  A lane walks its entries in views of 8 (kLanes
+// groups' parts; a group past the list's end reads as the ghost record), in
+// batches of 4 (lists are padded to multiples of 8, kListFold).  Each
 // batch's records are loaded one batch ahead of its pair terms, and its list
 // entries -- streamed from DRAM -- one batch ahead of the records, so the
 // latency of both overlaps the terms of the batch before.  Every record holds
@@ -322,9 +336,9 @@ force_list_kernel(Body body0, DevGeom g, PairList pl, ForceOut out) {
     body.init(acc);
     uint32_t err = 0;
     float rmin = 3.0e38f;
-    // this lane's groups: lane, lane + kLanes, ... of the particle's cnt / 8
+    // this lane's views of 8 entries: its parts of kLanes groups each
     const int groups = pl.count[s] / kListFold;
-    const int cnt = groups > lane ? (groups - lane + kLanes - 1) / kLanes * kListFold : 0;
+    const int views = (groups + kLanes - 1) / kLanes;
     using Rec = ListRec<kCompact>;
     const Rec none{};
     auto terms = [&](const Rec* r) {
@@ -348,26 +362,45 @@ force_list_kernel(Body body0, DevGeom g, PairList pl, ForceOut out) {
     };
     // groups of 8 entries (one 32-byte load) one group ahead; records one
     // batch of 4 ahead of their pair terms
-    const uint4* gp =
-        reinterpret_cast<const uint4*>(pl.list + ((size_t)lane * pl.stride + s) * kListFold);
-    const size_t gstride = (size_t)pl.stride * kListFold / 4 * kLanes;   // uint4 per step
+    constexpr int kE = kListFold / kLanes;   // entries of each group this lane takes
+    const uint32_t* gp = pl.list + (size_t)s * kListFold + lane * kE;
+    const size_t gs = (size_t)pl.stride * kListFold;   // one group
+    const uint32_t gh = (uint32_t)pl.stride;           // the ghost record (slot n)
+    // view m of this lane: its parts of groups kLanes m ... kLanes m + kLanes - 1
+    // (gp at the first; group kLanes m exists)
+    auto load_view = [&](const uint32_t* p, int m, uint4& a, uint4& b) {
+        if constexpr (kLanes == 1) {
+            load_group(p, a, b);
+        } else if constexpr (kLanes == 2) {
+            a = __ldg(reinterpret_cast<const uint4*>(p));
+            b = 2 * m + 1 < groups ? __ldg(reinterpret_cast<const uint4*>(p + gs))
+                                   : make_uint4(gh, gh, gh, gh);
+        } else {
+            const uint2 gg = make_uint2(gh, gh);
+            const uint2 q0 = __ldg(reinterpret_cast<const uint2*>(p));
+            const uint2 q1 = 4 * m + 1 < groups ? __ldg(reinterpret_cast<const uint2*>(p + gs)) : gg;
+            const uint2 q2 =
+                4 * m + 2 < groups ? __ldg(reinterpret_cast<const uint2*>(p + 2 * gs)) : gg;
+            const uint2 q3 =
+                4 * m + 3 < groups ? __ldg(reinterpret_cast<const uint2*>(p + 3 * gs)) : gg;
+            a = make_uint4(q0.x, q0.y, q1.x, q1.y);
+            b = make_uint4(q2.x, q2.y, q3.x, q3.y);
+        }
+    };
     // past the list's end the entries read as slot 0, a valid record: the
     // record loads need no condition
     uint4 ea = make_uint4(0u, 0u, 0u, 0u), eb = ea;
     Rec r[kBatch], rn[kBatch];
-    if (cnt > 0) {
-        ea = __ldg(gp);
-        eb = __ldg(gp + 1);
-    }
+    if (views > 0) load_view(gp, 0, ea, eb);
     r[0] = load_rec(pl.pos, ea.x, none);
     r[1] = load_rec(pl.pos, ea.y, none);
     r[2] = load_rec(pl.pos, ea.z, none);
     r[3] = load_rec(pl.pos, ea.w, none);
-    for (int k0 = 0; k0 < cnt; k0 += kListFold) {
-        const bool more = k0 + kListFold < cnt;
-        gp += gstride;
-        const uint4 na = more ? __ldg(gp) : make_uint4(0u, 0u, 0u, 0u);
-        const uint4 nb = more ? __ldg(gp + 1) : make_uint4(0u, 0u, 0u, 0u);
+    for (int m = 0; m < views; ++m) {
+        const bool more = m + 1 < views;
+        gp += gs * kLanes;
+        uint4 na = make_uint4(0u, 0u, 0u, 0u), nb = na;
+        if (more) load_view(gp, m + 1, na, nb);
         rn[0] = load_rec(pl.pos, eb.x, none);
         rn[1] = load_rec(pl.pos, eb.y, none);
         rn[2] = load_rec(pl.pos, eb.z, none);

@@ -93,9 +93,10 @@ struct PairList {
     // and the replicas' pair functors
     const int* rep;
     const void* pairs;
-    // threads per particle of the force pass (0 or 1, 2, 4): the lanes of a
-    // particle walk every lanes-th group of its list and add their sums in
-    // lane order (compact records; full records take one lane)
+    // threads per particle of the force pass (0 or 1, 2, 4): each lane of a
+    // particle takes its 8 / lanes entries of every group and the lanes' sums
+    // are added in lane order (compact records; full records take one lane).
+    // The ghost record is slot `stride` (n).
     int lanes;
 };
 cudaError_t launch_forces_list(const ForceSetup& fs, const DevGeom& g, const PairList& pl,
