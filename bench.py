@@ -130,21 +130,28 @@ class ClockSampler:
 
 
 # the dominant kernel of the mixed step and the ncu summary that gives its
-# DRAM traffic per launch (a line "dram_bytes_per_launch: B")
-FORCE_KERNEL = "force_list_kernel<MixedBody<LJPure<6>>, 1>"
+# DRAM traffic per launch (a line "dram_bytes_per_launch: B") and its L1
+# data-pipe load ("l1_data_pipe_wavefronts_per_launch: W",
+# "l1_data_pipe_pct_of_peak: P")
+FORCE_KERNEL = "force_list_kernel<MixedBody<LJPure<6>>, 1, 0, 0, 1>"
 FORCE_PROFILE = os.path.join(ROOT, "profiles", "force_list_lj_rho0.8_n2e20.txt")
 
 
-def profiled_traffic(path):
-    """DRAM bytes per launch (read + write) from a committed ncu summary, or None."""
+def profiled_value(path, key):
+    """The number on the line "key: value" of a committed ncu summary, or None."""
     try:
         with open(path) as fh:
             for line in fh:
-                if line.startswith("dram_bytes_per_launch:"):
+                if line.startswith(key + ":"):
                     return float(line.split(":", 1)[1])
     except OSError:
         pass
     return None
+
+
+def profiled_traffic(path):
+    """DRAM bytes per launch (read + write) from a committed ncu summary, or None."""
+    return profiled_value(path, "dram_bytes_per_launch")
 
 
 def measured_peaks():
@@ -738,7 +745,15 @@ def run_gpu(args):
                      "algorithmic": "%d FLOP/pair x %.2f pairs/particle x N per launch" % (
                          FLOPS_PER_PAIR_LJ, pairs),
                      "peak_source": "measured FP32 FMA probe (MEASURED_PEAKS.json has no FP32 figure)",
-                     "hbm_peak_gbs": peaks.get("hbm_gbs")},
+                     "hbm_peak_gbs": peaks.get("hbm_gbs"),
+                     # the bound the pass meets: the L1 data pipe (one
+                     # wavefront per cycle per SM) serving the record gathers
+                     "l1_data_pipe": {
+                         "wavefronts_per_launch": profiled_value(
+                             FORCE_PROFILE, "l1_data_pipe_wavefronts_per_launch"),
+                         "frac": (profiled_value(FORCE_PROFILE, "l1_data_pipe_pct_of_peak") or 0.0)
+                         / 100.0 or None,
+                         "source": "ncu summary " + os.path.relpath(FORCE_PROFILE, ROOT)}},
         "step_roofline": {
             "flops_per_particle_step": pairs * FLOPS_PER_PAIR_LJ + FLOPS_VGB,
             "bytes_per_particle_step": BYTES_PER_PARTICLE_STEP,
