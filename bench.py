@@ -460,7 +460,7 @@ def run_differentiable(psim, dev, steps=2000):
             "note": "q through the AO coefficients; the cutoff 1 + q is held fixed"}
 
 
-def run_gel(psim, dev, steps=1000, skin=0.0, chunk=100):
+def run_gel(psim, dev, steps=1000, skin=0.0, chunk=100, n=1 << 23):
     """The gel stress workload: N = 2^23 AO colloids at phi = 0.30 (q = 0.08,
     6 kT contact attraction, cutoff 1.08), seeded RSA start, gamma = 1,
     dt = 1e-3, mixed form.  skin 0: the cell list is rebuilt every step and
@@ -469,7 +469,7 @@ def run_gel(psim, dev, steps=1000, skin=0.0, chunk=100):
     and mean particles per cell every `chunk` steps while the colloids
     aggregate, the clusters and the kinetic temperature at the end."""
     from proteinsim2015_gb300 import init, batch
-    n, phi = 1 << 23, 0.30
+    phi = 0.30
     box = (n * math.pi / 6.0 / phi) ** (1.0 / 3.0)
     f = batch.ao_params(psim, 6.0, 0.08)
     # cells of at least cutOff + skin and of the 1.2 contact distance the
@@ -491,7 +491,8 @@ def run_gel(psim, dev, steps=1000, skin=0.0, chunk=100):
     done = max(1, steps // chunk) * chunk
     prof = s.profile(5)
     _, groups, avg = s.clusters(1.2, 4)
-    out = {"workload": "c4_gel_ao_phi0.30_N2^23", "n_particles": n, "box": box,
+    out = {"workload": "c4_gel_ao_phi0.30_N2^%d" % int(round(math.log2(n))), "n_particles": n,
+           "box": box,
            "cell_scale": scale, "skin": skin, "steps": done,
            "value": n * done / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms / done,
            "phases_ms": {k: round(v, 5) for k, v in prof.items()},
@@ -565,6 +566,11 @@ def profile_workload(args):
         out = run_batched(psim, dev, steps=args.steps, n_reps=64, tune=False)
     elif args.profile_workload == "adjoint":
         out = run_differentiable(psim, dev, steps=args.steps)
+    elif args.profile_workload == "gel":
+        # the gel's kernels (27-cell walk, cell list rebuilt every step) on a
+        # quarter of its particles at the same volume fraction, so a
+        # profiler's save and restore of device memory stays small
+        out = run_gel(psim, dev, steps=args.steps, chunk=args.steps, n=1 << 21)
     else:   # the 2^20 liquid in the plain FP64 form
         w = workload()
         n, box, scale = w["n"], w["box"], w["scale"]
@@ -795,10 +801,11 @@ def main():
     ap.add_argument("--profile-only", action="store_true",
                     help="time the mixed form and its phases only (short runs under ncu)")
     ap.add_argument("--profile-workload", default="mixed",
-                    choices=["mixed", "fp64", "batched", "adjoint"],
+                    choices=["mixed", "fp64", "batched", "adjoint", "gel"],
                     help="with --profile-only: the workload to run for --steps steps: the "
                          "2^20 liquid in the mixed or the plain FP64 form, the 512 AO "
-                         "replicas with a pair list, or the differentiable trajectory")
+                         "replicas with a pair list, the differentiable trajectory, or the "
+                         "gel at 2^21 particles")
     args = ap.parse_args()
     if args.cpu_baseline_json is not None:
         return cpu_baseline_child(args.cpu_baseline_json)
