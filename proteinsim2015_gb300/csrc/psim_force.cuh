@@ -201,6 +201,136 @@ force_pass_kernel(Body body, DevGeom g, CellView cv, ForceOut out, float pre_rc2
                     s_hi[w], s_aux[w], s_q[w]);
 }
 
+// A sparse grid (a few particles per cell, like the gel's one): a thread per
+// sorted particle walks its 9 rows of cells straight from global memory (the
+// runs are short and L1-resident) and keeps its in-range candidates in a
+// queue across rows, each entry with its row's periodic image (5 bits above
+// the 27-bit slot).  The warp drains the queues when one is nearly full and
+// at the end, so a lane runs the pair body about as often as the warp's
+// busiest lane has neighbours in all 27 cells, where the staged walk drains
+// after every row.  The image is applied to the neighbour (Body::image).
+// A grid takes this walk when it holds fewer than kSparseOccupancy particles
+// per cell on average -- a single system and each replica of a batch by the
+// same rule, so that a replica steps alike in both.
+constexpr int kSparseQueue = kQueue;          // the staged walk's queue rows, reused
+constexpr int kSparseMaxN = 1 << 27;          // slots the queue entries can hold
+constexpr int kSparseCentre = 13;             // image code of (0, 0, 0)
+constexpr double kSparseOccupancy = 4.0;
+
+template <class Body>
+__host__ __device__ __forceinline__ bool sparse_grid(const DevGeom& g) {
+    if constexpr (Body::kSparseWalk)
+        return (double)g.n < kSparseOccupancy * (double)g.ncell && g.n <= kSparseMaxN;
+    return false;
+}
+
+template <class Body>
+__device__ __forceinline__ void force_sparse_warp(const Body& body, const DevGeom& g,
+                                                  const CellView& cv, const ForceOut& out,
+                                                  float pre_rc2, int i, int lane,
+                                                  uint32_t (*q)[32]) {
+    using Aux = typename Body::Aux;
+    const Aux* g_aux = body.aux(cv);
+    const bool active = i < g.p1;
+    float4 hi = make_float4(0.f, 0.f, 0.f, 0.f);
+    int cx = 0, cy = 0, cz = 0;
+    typename Body::Home home;
+    typename Body::Acc acc;
+    body.init(acc);
+    if (active) {
+        hi = cv.posh[i];
+        const int c = cv.cellid[i] - g.c0;
+        cx = c % g.s;
+        cy = (c / g.s) % g.s;
+        cz = c / g.s2;
+        body.load_home(cv, i, home);
+    }
+    typename Body::Shifted hs;
+    body.shift(home, hi, 0, 0, 0, g, hs);
+    uint32_t err = 0;
+    int cnt = 0;
+    const int jlast = g.p1 - 1;
+    auto drain = [&]() {
+        const int kmax = __reduce_max_sync(0xffffffffu, cnt);
+        for (int k = 0; k < kmax; ++k) {
+            if (k < cnt) {
+                const uint32_t e = q[k][lane];
+                const int j = (int)(e & (uint32_t)(kSparseMaxN - 1));
+                const int img = (int)(e >> 27);
+                float4 hj = __ldg(&cv.posh[j]);
+                Aux aj = g_aux[j];
+                if (img != kSparseCentre)
+                    body.image(hj, aj, img % 3 - 1, (img / 3) % 3 - 1, img / 9 - 1, g);
+                body.eval(hj, aj, hs, acc, err);
+            }
+        }
+        body.fold(acc);
+        cnt = 0;
+    };
+    for (int row = 0; row < 9; ++row) {
+        const int dz = row / 3 - 1, dy = row % 3 - 1;
+        int sy, sz;
+        const int y = wrap_cell(cy + dy, g.s, sy);
+        const int z = wrap_cell(cz + dz, g.s, sz);
+        const int base = g.c0 + g.s * y + g.s2 * z;
+#pragma unroll 1
+        for (int part = 0; part < 2; ++part) {
+            // part 0: the cells of [cx-1, cx+1] inside the grid, contiguous;
+            // part 1: the one cell that wraps around in x (if any)
+            int a = 0, len = 0, sx = 0;
+            if (active) {
+                if (part == 0) {
+                    const int xa = cx > 0 ? cx - 1 : 0;
+                    const int xb = cx < g.s - 1 ? cx + 1 : g.s - 1;
+                    a = cv.cstart[base + xa];
+                    len = cv.cstart[base + xb] + cv.ccount[base + xb] - a;
+                } else if (cx == 0 || cx == g.s - 1) {
+                    const int xw = cx == 0 ? g.s - 1 : 0;
+                    sx = cx == 0 ? -1 : 1;
+                    a = cv.cstart[base + xw];
+                    len = cv.ccount[base + xw];
+                }
+            }
+            const int lmax = __reduce_max_sync(0xffffffffu, len);
+            if (lmax == 0) continue;
+            // the neighbour's image is +s L: x_j + s L - x_i
+            const float hx = hi.x - (float)sx * g.Lhi;
+            const float hy = hi.y - (float)sy * g.Lhi;
+            const float hz = hi.z - (float)sz * g.Lhi;
+            const uint32_t code = (uint32_t)((sx + 1) + 3 * (sy + 1) + 9 * (sz + 1)) << 27;
+            for (int t0 = 0; t0 < lmax; t0 += kUnroll) {
+#pragma unroll
+                for (int u = 0; u < kUnroll; ++u) {
+                    const int t = t0 + u;
+                    const int j = min(a + t, jlast);
+                    const float4 hj = __ldg(&cv.posh[j]);
+                    const float ex = hj.x - hx, ey = hj.y - hy, ez = hj.z - hz;
+                    const float r2 = ex * ex + ey * ey + ez * ez;
+                    const bool in = (t < len) & (r2 < pre_rc2) & (j != i);
+                    q[cnt][lane] = (uint32_t)j | code;
+                    cnt += in ? 1 : 0;
+                }
+                // at most kSparseQueue - kUnroll entries before a batch of
+                // kUnroll: slots stay below kQueueCap
+                if (__any_sync(0xffffffffu, cnt > kSparseQueue - kUnroll)) drain();
+            }
+        }
+    }
+    drain();
+    if (active) body.store(out, i, acc);
+    if (err) atomicOr(out.err, err);
+}
+
+template <class Body>
+__global__ void __launch_bounds__(kForceWarps * 32)
+force_sparse_kernel(Body body, DevGeom g, CellView cv, ForceOut out, float pre_rc2) {
+    __shared__ uint32_t s_q[kForceWarps][kQueueCap][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (pass_failed(out, lane)) return;  // warp-uniform
+    force_sparse_warp(body, g, cv, out, pre_rc2, blockIdx.x * blockDim.x + threadIdx.x, lane,
+                      s_q[w]);
+}
+
 // A batch of replicas: each warp takes a task (replica, first particle) and
 // that replica's geometry, pair functor and prefilter bound.
 template <class Body>
@@ -216,7 +346,11 @@ force_batch_kernel(Body body0, CellView cv, ForceOut out, BatchView bv) {
     const int2 t = bv.tasks[task];
     const DevGeom g = bv.geoms[t.x];
     const Body body = body0.for_replica(bv.pairs, t.x, g);
-    force_pass_warp(body, g, cv, out, bv.pre[t.x], t.y + lane, lane, s_hi[w], s_aux[w], s_q[w]);
+    if (sparse_grid<Body>(g))   // the rule a single system of this replica follows
+        force_sparse_warp(body, g, cv, out, bv.pre[t.x], t.y + lane, lane, s_q[w]);
+    else
+        force_pass_warp(body, g, cv, out, bv.pre[t.x], t.y + lane, lane, s_hi[w], s_aux[w],
+                        s_q[w]);
 }
 
 template <class Body>
@@ -234,6 +368,13 @@ cudaError_t launch_force_pass(const Body& body, const DevGeom& g, const CellView
         return cudaErrorInvalidValue;
     }
     if (g.n == 0) return cudaSuccess;
+    if (sparse_grid<Body>(g)) {
+        // few particles per cell: the runs are too short for the staged
+        // walk's per-row drains to pay
+        force_sparse_kernel<Body><<<(g.n + threads - 1) / threads, threads, 0, st>>>(
+            body, g, cv, out, pre_rc2);
+        return cudaGetLastError();
+    }
     force_pass_kernel<Body><<<(g.n + threads - 1) / threads, threads, 0, st>>>(body, g, cv, out,
                                                                               pre_rc2);
     return cudaGetLastError();

@@ -229,3 +229,37 @@ def test_pairlist_in_a_large_box(psim):
     # 1.1e-8, largest 4.3e-6, one particle of 2e5)
     assert np.percentile(np.abs(d), 99.9) < 1e-6
     assert np.max(np.abs(d)) < 1e-4
+
+
+def test_sparse_cell_walk_matches_fp64(psim):
+    # AO colloids at the gel's volume fraction on cells of 1.2 (one particle
+    # per cell on average): the mixed form without a skin takes the sparse
+    # walk (queues kept across the 27 cells, images applied to the
+    # neighbour), the plain FP64 form the staged walk in the reference's
+    # order -- the same forces, and the same bits run to run
+    from proteinsim2015_gb300 import batch, init
+    n, phi = 20000, 0.30
+    box = (n * np.pi / 6.0 / phi) ** (1.0 / 3.0)
+    f = batch.ao_params(psim, 6.0, 0.08)
+    scale = int(box // 1.2)
+    g = psim.geometry(n, box, box / scale, scale)
+    assert n < 4 * scale ** 3
+    pos = init.rsa(n, box, 1.0, seed=51).reshape(-1)
+    rad = np.full(n, 0.5)
+    f64 = psim.System(g, f, precision=0)
+    f64.upload(pos, rad)
+    ref = f64.forces()
+    f64.close()
+    outs = []
+    for _ in range(2):
+        s = psim.System(g, f, gamma=1.0, dt=0.001, kT=1.0, precision=1,
+                        noise_mode=psim.NOISE_PHILOX)
+        s.upload(pos, rad)
+        got = s.forces()
+        assert rel_norm(got, ref) < 1e-5
+        s.step(25)
+        outs.append((got, s.download()))
+        s.close()
+    assert np.array_equal(outs[0][0], outs[1][0])
+    for k in outs[0][1]:
+        assert np.array_equal(outs[0][1][k], outs[1][1][k])
