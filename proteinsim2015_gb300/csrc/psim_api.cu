@@ -264,6 +264,16 @@ int choose_tile(const DevGeom&) {
     return 0;
 }
 
+// The mixed form's 27-cell walk: the direct walk (0), or as PSIM_FORCE_WALK
+// names it ("staged": 1, "direct": 2), for measurement.
+int choose_walk() {
+    if (const char* v = std::getenv("PSIM_FORCE_WALK")) {
+        if (!std::strcmp(v, "staged")) return 1;
+        if (!std::strcmp(v, "direct")) return 2;
+    }
+    return 0;
+}
+
 // One force pass: the library's own functor for the parameters' kind, or a
 // plugin's device entry (psim_force_launch) with the same arrays.  pass:
 // psim_force_pass; cv for the cell walks, pl for the pair list.
@@ -711,6 +721,7 @@ int force_evaluate(psim_force_launch_fn plugin, const psim_force_params* params,
     if ((rc = ensure_device())) return rc;
     ForceSetup fs = make_setup(params, g.L);
     fs.tile = choose_tile(g);
+    fs.walk = choose_walk();
     const ForceRunner fr{&fs, plugin, params};
     Workspace& w = g_ws;
     std::lock_guard<std::mutex> lk(w.mu);
@@ -1832,6 +1843,7 @@ psim_system* psim_batch_create_list(const psim_replica* reps, int32_t n_reps,
     if (!s) return nullptr;
     DeviceGuard dg(s->device);
     s->fs.tile = 0;
+    s->fs.walk = choose_walk();
     // warp tasks aligned to the replicas' particle ranges
     std::vector<int2> tasks;
     std::vector<int> rep((size_t)P);
@@ -1949,6 +1961,7 @@ psim_system* system_new(const psim_system_config* cfg, const DevGeom& g, bool ba
     s->vp = vp;
     s->fs = make_setup(&cfg->force, g.L);
     s->fs.tile = choose_tile(g);
+    s->fs.walk = choose_walk();
     s->n = g.n;
     s->ncell = g.ncell;
     if (list_on) {

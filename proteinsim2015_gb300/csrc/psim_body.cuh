@@ -41,7 +41,7 @@ struct F64Body {
     using Aux = double4_32a;  // the FP64 neighbour positions {x, y, z, R}
     static constexpr bool kBatchable = !std::is_same<Pair, ComboPair>::value;
     // the reference's summation order and image rules: always the staged walk
-    static constexpr bool kSparseWalk = false;
+    static constexpr bool kDirectWalk = false;
     struct Home {
         double4_32a p;
     };
@@ -172,9 +172,8 @@ struct MixedBody {
     float cont2f = 0.f;  // > 0: count the neighbours with r^2 < cont2f (ForceOut::coor)
     using Aux = float4;  // the low parts of the neighbour positions
     static constexpr bool kBatchable = !std::is_same<Pair, ComboPairF>::value;
-    // on sparse grids the walk that keeps its queues across rows
-    // (force_sparse_kernel) may take the pass
-    static constexpr bool kSparseWalk = true;
+    // the 27-cell walk that keeps its queues across rows (force_direct_kernel)
+    static constexpr bool kDirectWalk = true;
     struct Home {
         float4 lo;
     };

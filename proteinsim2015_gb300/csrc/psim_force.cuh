@@ -26,7 +26,9 @@
 //
 // Body supplies the precision-specific parts (psim_exact.cu: FP64 plain form
 // with the reference's image rules; psim_mixed.cu: FP32 pairs with Kahan
-// sums).
+// sums).  The staged walk serves the FP64 form; the mixed form takes the
+// direct walk (force_direct_kernel, below), which reads the rows through L1
+// and keeps its queues across rows.
 #pragma once
 
 #include <climits>
@@ -201,31 +203,34 @@ force_pass_kernel(Body body, DevGeom g, CellView cv, ForceOut out, float pre_rc2
                     s_hi[w], s_aux[w], s_q[w]);
 }
 
-// A sparse grid (a few particles per cell, like the gel's one): a thread per
-// sorted particle walks its 9 rows of cells straight from global memory (the
-// runs are short and L1-resident) and keeps its in-range candidates in a
-// queue across rows, each entry with its row's periodic image (5 bits above
-// the 27-bit slot).  The warp drains the queues when one is nearly full and
-// at the end, so a lane runs the pair body about as often as the warp's
-// busiest lane has neighbours in all 27 cells, where the staged walk drains
-// after every row.  The image is applied to the neighbour (Body::image).
-// A grid takes this walk when it holds fewer than kSparseOccupancy particles
-// per cell on average -- a single system and each replica of a batch by the
-// same rule, so that a replica steps alike in both.
-constexpr int kSparseQueue = kQueue;          // the staged walk's queue rows, reused
-constexpr int kSparseMaxN = 1 << 27;          // slots the queue entries can hold
-constexpr int kSparseCentre = 13;             // image code of (0, 0, 0)
-constexpr double kSparseOccupancy = 4.0;
+// The mixed form's 27-cell walk (the direct walk): a thread per sorted
+// particle walks its 9 rows of cells straight from global memory and keeps
+// its in-range candidates in a queue across rows, each entry with its row's
+// periodic image (5 bits above the 27-bit slot).  The warp drains the queues
+// when one is nearly full and at the end, so a lane runs the pair body about
+// as often as the warp's busiest lane has neighbours in all 27 cells, where
+// the staged walk drains after every row.  The particles of a warp mostly
+// share their rows' runs, so the candidate reads broadcast through L1 about
+// as well as they would from a shared-memory stage.  Measured on GB300 the
+// direct walk beat the staged walk at every occupancy tried (1 to 21
+// particles per cell: force pass 3-37% shorter).  The image is applied to
+// the neighbour (Body::image).  A single system and each replica of a batch
+// follow the same rule, so that a replica steps alike in both.  The FP64
+// form keeps the staged walk: its sums follow the reference's cell order.
+constexpr int kDirectQueue = kQueue;          // the staged walk's queue rows, reused
+constexpr int kDirectMaxN = 1 << 27;          // slots the queue entries can hold
+constexpr int kDirectCentre = 13;             // image code of (0, 0, 0)
 
+// walk: 0 the body's own choice, 1 the staged walk, 2 the direct walk (where
+// the body allows it)
 template <class Body>
-__host__ __device__ __forceinline__ bool sparse_grid(const DevGeom& g) {
-    if constexpr (Body::kSparseWalk)
-        return (double)g.n < kSparseOccupancy * (double)g.ncell && g.n <= kSparseMaxN;
+__host__ __device__ __forceinline__ bool direct_walk(const DevGeom& g, int walk = 0) {
+    if constexpr (Body::kDirectWalk) return g.n <= kDirectMaxN && walk != 1;
     return false;
 }
 
 template <class Body>
-__device__ __forceinline__ void force_sparse_warp(const Body& body, const DevGeom& g,
+__device__ __forceinline__ void force_direct_warp(const Body& body, const DevGeom& g,
                                                   const CellView& cv, const ForceOut& out,
                                                   float pre_rc2, int i, int lane,
                                                   uint32_t (*q)[32]) {
@@ -255,11 +260,11 @@ __device__ __forceinline__ void force_sparse_warp(const Body& body, const DevGeo
         for (int k = 0; k < kmax; ++k) {
             if (k < cnt) {
                 const uint32_t e = q[k][lane];
-                const int j = (int)(e & (uint32_t)(kSparseMaxN - 1));
+                const int j = (int)(e & (uint32_t)(kDirectMaxN - 1));
                 const int img = (int)(e >> 27);
                 float4 hj = __ldg(&cv.posh[j]);
                 Aux aj = g_aux[j];
-                if (img != kSparseCentre)
+                if (img != kDirectCentre)
                     body.image(hj, aj, img % 3 - 1, (img / 3) % 3 - 1, img / 9 - 1, g);
                 body.eval(hj, aj, hs, acc, err);
             }
@@ -310,9 +315,9 @@ __device__ __forceinline__ void force_sparse_warp(const Body& body, const DevGeo
                     q[cnt][lane] = (uint32_t)j | code;
                     cnt += in ? 1 : 0;
                 }
-                // at most kSparseQueue - kUnroll entries before a batch of
+                // at most kDirectQueue - kUnroll entries before a batch of
                 // kUnroll: slots stay below kQueueCap
-                if (__any_sync(0xffffffffu, cnt > kSparseQueue - kUnroll)) drain();
+                if (__any_sync(0xffffffffu, cnt > kDirectQueue - kUnroll)) drain();
             }
         }
     }
@@ -323,11 +328,11 @@ __device__ __forceinline__ void force_sparse_warp(const Body& body, const DevGeo
 
 template <class Body>
 __global__ void __launch_bounds__(kForceWarps * 32)
-force_sparse_kernel(Body body, DevGeom g, CellView cv, ForceOut out, float pre_rc2) {
+force_direct_kernel(Body body, DevGeom g, CellView cv, ForceOut out, float pre_rc2) {
     __shared__ uint32_t s_q[kForceWarps][kQueueCap][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     if (pass_failed(out, lane)) return;  // warp-uniform
-    force_sparse_warp(body, g, cv, out, pre_rc2, blockIdx.x * blockDim.x + threadIdx.x, lane,
+    force_direct_warp(body, g, cv, out, pre_rc2, blockIdx.x * blockDim.x + threadIdx.x, lane,
                       s_q[w]);
 }
 
@@ -335,7 +340,7 @@ force_sparse_kernel(Body body, DevGeom g, CellView cv, ForceOut out, float pre_r
 // that replica's geometry, pair functor and prefilter bound.
 template <class Body>
 __global__ void __launch_bounds__(kForceWarps * 32)
-force_batch_kernel(Body body0, CellView cv, ForceOut out, BatchView bv) {
+force_batch_kernel(Body body0, CellView cv, ForceOut out, BatchView bv, int walk) {
     __shared__ float4 s_hi[kForceWarps][kStagePad];
     __shared__ typename Body::Aux s_aux[kForceWarps][kStage];
     __shared__ uint32_t s_q[kForceWarps][kQueueCap][32];
@@ -346,8 +351,8 @@ force_batch_kernel(Body body0, CellView cv, ForceOut out, BatchView bv) {
     const int2 t = bv.tasks[task];
     const DevGeom g = bv.geoms[t.x];
     const Body body = body0.for_replica(bv.pairs, t.x, g);
-    if (sparse_grid<Body>(g))   // the rule a single system of this replica follows
-        force_sparse_warp(body, g, cv, out, bv.pre[t.x], t.y + lane, lane, s_q[w]);
+    if (direct_walk<Body>(g, walk))   // the rule a single system of this replica follows
+        force_direct_warp(body, g, cv, out, bv.pre[t.x], t.y + lane, lane, s_q[w]);
     else
         force_pass_warp(body, g, cv, out, bv.pre[t.x], t.y + lane, lane, s_hi[w], s_aux[w],
                         s_q[w]);
@@ -356,22 +361,20 @@ force_batch_kernel(Body body0, CellView cv, ForceOut out, BatchView bv) {
 template <class Body>
 cudaError_t launch_force_pass(const Body& body, const DevGeom& g, const CellView& cv,
                               const ForceOut& out, float pre_rc2, cudaStream_t st,
-                              const BatchView* bv = nullptr) {
+                              const BatchView* bv = nullptr, int walk = 0) {
     const int threads = kForceWarps * 32;
     if (bv && bv->tasks) {
         if constexpr (Body::kBatchable) {
             if (bv->n_tasks == 0) return cudaSuccess;
             const int blocks = (bv->n_tasks + kForceWarps - 1) / kForceWarps;
-            force_batch_kernel<Body><<<blocks, threads, 0, st>>>(body, cv, out, *bv);
+            force_batch_kernel<Body><<<blocks, threads, 0, st>>>(body, cv, out, *bv, walk);
             return cudaGetLastError();
         }
         return cudaErrorInvalidValue;
     }
     if (g.n == 0) return cudaSuccess;
-    if (sparse_grid<Body>(g)) {
-        // few particles per cell: the runs are too short for the staged
-        // walk's per-row drains to pay
-        force_sparse_kernel<Body><<<(g.n + threads - 1) / threads, threads, 0, st>>>(
+    if (direct_walk<Body>(g, walk)) {
+        force_direct_kernel<Body><<<(g.n + threads - 1) / threads, threads, 0, st>>>(
             body, g, cv, out, pre_rc2);
         return cudaGetLastError();
     }

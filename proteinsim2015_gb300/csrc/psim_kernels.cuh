@@ -23,6 +23,7 @@ struct ForceSetup {
     double rc_max;     // largest cutoff: cell_size must be >= rc_max
     float pre_rc2f;    // conservative FP32 prefilter bound on r^2 (FP64 form)
     int tile;          // 0: a warp per 32 consecutive particles; 1: a block per home cell
+    int walk;          // with tile 0, the mixed form's walk: 0 direct (default), 1 staged, 2 direct
     int lj_pure;       // LennardJones with yukawaStrength 0 in every replica
 };
 

@@ -60,7 +60,7 @@ cudaError_t launch_forces_mixed(const ForceSetup& fs, const DevGeom& g, const Ce
         MixedBody<decltype(p)> body{p, rc2f};
         body.cont2f = out.coor ? out.cont2f : 0.f;   // updateInteractions fused into the pass
         if (fs.tile && !bv) return launch_force_cells(body, g, cv, out, fs.pre_rc2f, st);
-        return launch_force_pass(body, g, cv, out, fs.pre_rc2f, st, bv);
+        return launch_force_pass(body, g, cv, out, fs.pre_rc2f, st, bv, fs.walk);
     });
 }
 

@@ -231,9 +231,9 @@ def test_pairlist_in_a_large_box(psim):
     assert np.max(np.abs(d)) < 1e-4
 
 
-def test_sparse_cell_walk_matches_fp64(psim):
+def test_direct_walk_on_a_sparse_grid_matches_fp64(psim):
     # AO colloids at the gel's volume fraction on cells of 1.2 (one particle
-    # per cell on average): the mixed form without a skin takes the sparse
+    # per cell on average): the mixed form without a skin takes the direct
     # walk (queues kept across the 27 cells, images applied to the
     # neighbour), the plain FP64 form the staged walk in the reference's
     # order -- the same forces, and the same bits run to run
