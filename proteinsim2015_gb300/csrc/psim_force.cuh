@@ -216,7 +216,9 @@ force_pass_kernel(Body body, DevGeom g, CellView cv, ForceOut out, float pre_rc2
 // particles per cell: force pass 3-37% shorter).  The image is applied to
 // the neighbour (Body::image).  A single system and each replica of a batch
 // follow the same rule, so that a replica steps alike in both.  The FP64
-// form keeps the staged walk: its sums follow the reference's cell order.
+// form keeps the staged walk, whose sums follow the reference's cell order:
+// a direct walk with a fold marker at each row's end gave the same bits but
+// measured 6-18% slower (its 32-byte FP64 neighbour loads through L1).
 constexpr int kDirectQueue = kQueue;          // the staged walk's queue rows, reused
 constexpr int kDirectMaxN = 1 << 27;          // slots the queue entries can hold
 constexpr int kDirectCentre = 13;             // image code of (0, 0, 0)

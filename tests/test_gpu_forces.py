@@ -122,3 +122,40 @@ def test_malformed_cell_list_is_refused(psim):
         with pytest.raises(psim.PsimError) as e:
             psim.force_evaluate(p, g, srt, h, c)
         assert e.value.code == psim.ERR_INPUT
+
+
+@pytest.mark.parametrize("system", ["lj_dense", "ao_sparse"])
+def test_walk_choice_keeps_the_fp64_sums(psim, monkeypatch, system):
+    # PSIM_FORCE_WALK picks the mixed form's 27-cell walk (the staged or the
+    # direct one: the same pair terms, summed in another cadence, within the
+    # mixed tolerance); the FP64 form always takes the staged walk in the
+    # reference's order, so its forces do not move by a bit, through the
+    # drop-in and a system
+    if system == "lj_dense":   # ~32 particles per cell
+        pos, rad, box = lattice_state(8, (4 / 0.8) ** (1 / 3), 0.08, seed=52)
+        n, scale = len(rad), 4
+        p = psim.make_force("LJ", 2.5, kT=1.5, well_depth=1 / 1.5, lj_num=6,
+                            yukawa_strength=0.0)
+    else:                      # ~0.3 particles per cell
+        n, box, scale = 3000, 30.0, 25
+        pos, rad = rsa_state(n, box, seed=53)
+        p = psim.make_force("AO", 1.1, kT=1.0, well_depth=0.25)
+    g = psim.geometry(n, box, box / scale, scale)
+    hi, cse, srt = psim.cells_build(g, pos, rad)
+    out = {}
+    for walk in ("staged", "direct"):
+        monkeypatch.setenv("PSIM_FORCE_WALK", walk)
+        f64 = psim.force_evaluate(p, g, srt, hi, cse, precision=psim.PRECISION_FP64)
+        s = psim.System(g, p, precision=psim.PRECISION_FP64)
+        s.upload(pos, rad)
+        fs = s.forces()
+        s.close()
+        s = psim.System(g, p, precision=psim.PRECISION_MIXED)
+        s.upload(pos, rad)
+        fm = s.forces()
+        s.close()
+        out[walk] = (f64, fs, fm)
+    assert np.array_equal(out["staged"][0], out["direct"][0])
+    assert np.array_equal(out["staged"][1], out["direct"][1])
+    assert rel_norm(out["direct"][2], out["direct"][1]) < FORCE_TOL_MIXED
+    assert rel_norm(out["staged"][2], out["direct"][1]) < FORCE_TOL_MIXED
