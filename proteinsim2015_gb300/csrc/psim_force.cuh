@@ -224,10 +224,12 @@ constexpr int kDirectMaxN = 1 << 27;          // slots the queue entries can hol
 constexpr int kDirectCentre = 13;             // image code of (0, 0, 0)
 
 // walk: 0 the body's own choice, 1 the staged walk, 2 the direct walk (where
-// the body allows it)
+// the body allows it).  A queue entry holds a storage slot in 27 bits: the
+// grid's particles (a replica's, in a batch: global slots up to p1) must end
+// below 2^27.
 template <class Body>
 __host__ __device__ __forceinline__ bool direct_walk(const DevGeom& g, int walk = 0) {
-    if constexpr (Body::kDirectWalk) return g.n <= kDirectMaxN && walk != 1;
+    if constexpr (Body::kDirectWalk) return g.p1 <= kDirectMaxN && walk != 1;
     return false;
 }
 
