@@ -571,18 +571,21 @@ def profile_workload(args):
         # quarter of its particles at the same volume fraction, so a
         # profiler's save and restore of device memory stays small
         out = run_gel(psim, dev, steps=args.steps, chunk=args.steps, n=1 << 21)
-    else:   # the 2^20 liquid in the plain FP64 form
+    else:   # the 2^20 liquid in the plain FP64 form, or the mixed form's 27-cell walk
         w = workload()
         n, box, scale = w["n"], w["box"], w["scale"]
         g = psim.geometry(n, box, box / scale, scale)
         p = psim.make_force("LJ", RC, kT=KT, well_depth=WD, lj_num=LJN, yukawa_strength=0.0)
+        fp64 = args.profile_workload == "fp64"
         s = psim.System(g, p, gamma=GAMMA, dt=DT, kT=KT, vel_freq=1000, seed=90210,
-                        precision=psim.PRECISION_FP64, device=dev)
+                        precision=psim.PRECISION_FP64 if fp64 else psim.PRECISION_MIXED,
+                        device=dev)
         s.upload(w["pos"], w["radius"], vel=w["vel"])
         s.step(max(args.warmup, 1))
         ms = s.time_steps(args.steps)
-        out = {"workload": "lj_rho0.8_N2^20_fp64", "value": n * args.steps / (ms * 1e-3),
-               "ms_per_step": ms / args.steps, "phases_ms": s.profile(2)}
+        out = {"workload": "lj_rho0.8_N2^20_" + ("fp64" if fp64 else "mixed_walk"),
+               "value": n * args.steps / (ms * 1e-3), "ms_per_step": ms / args.steps,
+               "phases_ms": s.profile(2)}
         s.close()
     out["profile_only"] = True
     print(json.dumps(out))
@@ -801,11 +804,12 @@ def main():
     ap.add_argument("--profile-only", action="store_true",
                     help="time the mixed form and its phases only (short runs under ncu)")
     ap.add_argument("--profile-workload", default="mixed",
-                    choices=["mixed", "fp64", "batched", "adjoint", "gel"],
+                    choices=["mixed", "fp64", "walk", "batched", "adjoint", "gel"],
                     help="with --profile-only: the workload to run for --steps steps: the "
-                         "2^20 liquid in the mixed or the plain FP64 form, the 512 AO "
-                         "replicas with a pair list, the differentiable trajectory, or the "
-                         "gel at 2^21 particles")
+                         "2^20 liquid in the mixed form, in the plain FP64 form, or in the "
+                         "mixed form without a skin (the 27-cell walk), the 512 AO replicas "
+                         "with a pair list, the differentiable trajectory, or the gel at "
+                         "2^21 particles")
     args = ap.parse_args()
     if args.cpu_baseline_json is not None:
         return cpu_baseline_child(args.cpu_baseline_json)
