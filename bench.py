@@ -53,13 +53,15 @@ SKIN = 0.4
 CLOCK_WINDOW_STEPS = 6000
 
 
-def workload(cells=64):
+def workload(cells=64, skin=SKIN):
+    """The 2^20 LJ liquid (FCC start, rho = 0.8) on the finest grid of cells of
+    at least cutOff + skin."""
     from proteinsim2015_gb300 import init
     a = (4.0 / 0.8) ** (1.0 / 3.0)
     box = cells * a
     pos = init.fcc(cells, a).reshape(-1)
     n = pos.size // 3
-    scale = int(math.floor(box / (RC + SKIN)))
+    scale = int(math.floor(box / (RC + max(skin, 0.0))))
     vel = init.maxwell(n, KT, seed=90210).reshape(-1)
     return dict(n=n, box=box, scale=scale, cell_size=box / scale, pos=pos, vel=vel,
                 radius=np.full(n, 0.5), cells=cells)
@@ -604,7 +606,7 @@ def run_gpu(args):
     dev = local
     if psim.device_count() <= dev:
         raise SystemExit("no CUDA device %d" % dev)
-    w = workload()
+    w = workload(skin=args.skin)
     n, box, scale = w["n"], w["box"], w["scale"]
     g = psim.geometry(n, box, box / scale, scale)
     p = psim.make_force("LJ", RC, kT=KT, well_depth=WD, lj_num=LJN, yukawa_strength=0.0)
